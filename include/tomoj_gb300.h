@@ -1,0 +1,170 @@
+/*
+ * tomoj_gb300.h -- C ABI of the GB300 projection / backprojection engine.
+ *
+ * The engine is a drop-in for TomoJ's Projector plug-in surface
+ * (TomoJ_Base/src/main/java/fr/curie/tomoj/tomography/projectors/Projector.java)
+ * and for the iteration drivers that call it
+ * (TomoJ_Base/src/main/java/fr/curie/tomoj/tomography/TomoReconstruction2.java).
+ * Every entry point is a plain C function taking POD structs, pointers and
+ * sizes, returns a tomo_status (0 = success), and never throws; the last error
+ * message of the calling thread is available from tomo_last_error().
+ *
+ * Data layouts (identical to the reference's in-memory layouts):
+ *   volume      float32 [D][H][W]   (D slices of W x H, x fastest;
+ *                                    TomoReconstruction2 ImageStack)
+ *   tilt-series float32 [N][h][w]   (TiltSeries ImageStack)
+ *   euler       float64 [N][3][3]   row-major (AffineAlignment.getEulerMatrix)
+ *   transform   float64 [N][6]      java.awt.geom.AffineTransform flat matrix
+ *                                    {m00, m10, m01, m11, m02, m12}
+ *
+ * A handle is thread-compatible (one thread at a time).  All device work of a
+ * handle runs on its stream (tomo_set_stream; default: a stream the handle
+ * creates).  Calls that take host pointers copy synchronously on that stream.
+ */
+#ifndef TOMOJ_GB300_H
+#define TOMOJ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TOMO_ABI_VERSION 1
+
+typedef int32_t tomo_status;
+#define TOMO_OK 0
+#define TOMO_ERR_INVALID (-1)     /* bad argument or size */
+#define TOMO_ERR_CUDA (-2)        /* CUDA runtime error (message in tomo_last_error) */
+#define TOMO_ERR_NOMEM (-3)       /* admission control: not enough free HBM under the limit */
+#define TOMO_ERR_STATE (-4)       /* call out of order (e.g. backproject with no projection) */
+#define TOMO_ERR_UNSUPPORTED (-5) /* geometry or option not supported by this build */
+#define TOMO_ERR_CANCELLED (-6)   /* tomo_cancel() was called */
+#define TOMO_ERR_DEVICE (-7)      /* a kernel reported an error status (bounded wait expired) */
+
+/* TiltSeries fill types (TiltSeries.FILL_*) used when aligning projections. */
+#define TOMO_FILL_NONE 0
+#define TOMO_FILL_AVG 1
+#define TOMO_FILL_NAN 2
+
+/* WBP weighting filters.  RADERMACHER is FFTWeighting (FFTWeighting.java:31-112);
+ * RAMP and HAMMING_RAMP are row filters with no counterpart in the reference. */
+#define TOMO_WEIGHT_NONE 0
+#define TOMO_WEIGHT_RADERMACHER 1
+#define TOMO_WEIGHT_RAMP 2
+#define TOMO_WEIGHT_HAMMING_RAMP 3
+
+/* Storage precision of the volume (accumulation is always FP32). */
+#define TOMO_PREC_FP32 0
+
+typedef struct tomo_geom {
+    int32_t W, H, D;        /* volume width (x), height (y: tilt-axis rows), depth (z) */
+    int32_t w, h;           /* projection width, height */
+    int32_t nproj;          /* projections in the tilt-series */
+    double vol_center[3];   /* TomoReconstruction2 centres; NaN = default (n-1)/2 */
+    double proj_center[4];  /* TiltSeries centerX, centerY (forward projection) and
+                               projectionCenterX, projectionCenterY (backprojection);
+                               NaN = default (n-1)/2 */
+    double scale;           /* projection/volume scale (VoxelProjector3D.setScale); 0 = 1 */
+} tomo_geom;
+
+typedef struct tomo_params {
+    int32_t positivity;     /* VoxelProjector3D.setPositivityConstraint */
+    int32_t long_object;    /* VoxelProjector3D.setLongObjectCompensation */
+    int32_t fill;           /* TOMO_FILL_* for tomo_load_series alignment */
+    int32_t normalize;      /* TiltSeries.setNormalize: (x-mean)/stdDev per tilt */
+    int32_t precision;      /* TOMO_PREC_* */
+    int32_t reserved[3];
+} tomo_params;
+
+typedef struct tomo_projector tomo_projector;
+
+/* ---- library ---------------------------------------------------------- */
+int32_t tomo_abi_version(void);
+const char* tomo_last_error(void);
+/* Upper bound on device bytes the library may hold across all handles
+ * (admission control; 0 = no limit besides free HBM). */
+tomo_status tomo_set_memory_limit(uint64_t bytes);
+uint64_t tomo_memory_in_use(void);
+/* Number of kernels this library launched since load (all handles). */
+uint64_t tomo_kernel_launches(void);
+
+/* ---- lifetime ----------------------------------------------------------
+ * Replaces the Projector constructor (Projector.java:30-40), which captures
+ * dimensions and centres from the TiltSeries and TomoReconstruction2. */
+tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_projector** out);
+tomo_status tomo_destroy(tomo_projector* p);
+/* cudaStream_t passed as void*; NULL returns to the handle's own stream. */
+tomo_status tomo_set_stream(tomo_projector* p, void* stream);
+
+/* ---- data ---------------------------------------------------------------
+ * Uploads the unaligned tilt-series and per-tilt geometry and builds the
+ * aligned projections that TiltSeries.getPixels(i) returns
+ * (TiltSeries.java:678-687 -> AffineAlignment.applyTransformOnImage,
+ * AffineAlignment.java:136-259).  transforms may be NULL (identity); stats
+ * (per tilt {mean, stdDev}) may be NULL (0, 1).  pixels_on_device != 0 means
+ * `pixels` is a device pointer. */
+tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pixels_on_device, const double* euler,
+                             const double* transforms, const double* stats);
+/* The aligned projection `index` as the projector sees it (host copy). */
+tomo_status tomo_get_aligned(tomo_projector* p, int32_t index, float* out_host);
+/* Volume rows [y0,y1) from/to a host or device buffer laid out [D][y1-y0][W]. */
+tomo_status tomo_set_volume(tomo_projector* p, const float* src, int32_t on_device, int32_t y0, int32_t y1);
+tomo_status tomo_get_volume(tomo_projector* p, float* dst, int32_t on_device, int32_t y0, int32_t y1);
+tomo_status tomo_fill_volume(tomo_projector* p, float value);
+/* Device pointer of the resident volume [D][H][W] (valid until tomo_destroy). */
+tomo_status tomo_volume_device_ptr(tomo_projector* p, float** out);
+
+/* ---- Projector surface (Projector.java:130-156) ------------------------- */
+tomo_status tomo_add_projection(tomo_projector* p, int32_t index);          /* addProjection(int) */
+tomo_status tomo_clear_projections(tomo_projector* p);                      /* clearAllProjections() */
+tomo_status tomo_project(tomo_projector* p, int32_t y0, int32_t y1);       /* project(y0,y1) */
+/* projectAndDifference(factor,y0,y1): err_out[k] = sum of squared differences of
+ * the k-th added projection (may be NULL). */
+tomo_status tomo_project_and_difference(tomo_projector* p, double factor, int32_t y0, int32_t y1, double* err_out);
+tomo_status tomo_backproject(tomo_projector* p, int32_t y0, int32_t y1);   /* backproject(y0,y1) */
+tomo_status tomo_start_iteration(tomo_projector* p);                        /* startOfIteration() */
+tomo_status tomo_end_iteration(tomo_projector* p);                          /* endOfIteration() */
+/* getProjection(k): forward projection of the k-th added projection (w*h floats). */
+tomo_status tomo_get_projection(tomo_projector* p, int32_t k, float* out_host);
+tomo_status tomo_get_norm(tomo_projector* p, int32_t k, float* out_host);
+tomo_status tomo_get_difference(tomo_projector* p, int32_t k, float* out_host);
+int32_t tomo_projection_count(tomo_projector* p);
+
+/* ---- options ------------------------------------------------------------ */
+/* WBP weighting applied before every backprojection of original projections
+ * (VoxelProjector3D.java:163-166).  radius: FFTWeighting diameter / w
+ * (ReconstructionParameters.java:320).  tilt_axes: per-tilt axis angle in
+ * degrees (NULL = 0); only 0 is supported on the device. */
+tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, const double* tilt_axes);
+/* TVM regularisation run at endOfIteration (TVMProjector3D.java:135-157):
+ * ROF denoise with theta, g, dt for `iterations` inner steps; iterations 0 disables. */
+tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int32_t iterations);
+/* FISTA momentum wrapper (FistaProjector3D.java). */
+tomo_status tomo_set_fista(tomo_projector* p, int32_t enabled);
+
+/* ---- drivers (TomoReconstruction2) --------------------------------------- */
+/* WBP(ts, projector, params, y0, y1) with update 0 (TomoReconstruction2.java:499-538). */
+tomo_status tomo_run_wbp(tomo_projector* p, int32_t y0, int32_t y1);
+/* OSSART(ts, projector, params, y0, y1) (TomoReconstruction2.java:548-634):
+ * update 0 = SIRT (all projections per update), 1 = ART.  The first projection
+ * of every iteration's ordering comes from tomo_first_index(seed, iteration)
+ * instead of Math.random().  err_out (n_iter*5, may be NULL) receives
+ * {average, min, argmin, max, argmax} per iteration.  Iterations run as one
+ * CUDA graph per iteration when use_graph != 0. */
+tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int32_t update, uint64_t seed,
+                            int32_t y0, int32_t y1, int32_t use_graph, double* err_out);
+/* Deterministic replacement for the random first index of orderShuffleART. */
+int32_t tomo_first_index(uint64_t seed, int32_t iteration, int32_t nproj);
+/* orderShuffleART ordering (TomoReconstruction2.java:735-781) for a first index. */
+tomo_status tomo_order(tomo_projector* p, int32_t first, int32_t* order_out);
+/* Same ordering for explicit Euler matrices (nproj x 9); needs no handle or GPU. */
+tomo_status tomo_order_shuffle(int32_t nproj, const double* euler, int32_t first, int32_t* order_out);
+/* Cooperative cancel, polled between updates (TomoReconstruction2.interrupt). */
+tomo_status tomo_cancel(tomo_projector* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TOMOJ_GB300_H */

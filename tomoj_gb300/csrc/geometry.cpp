@@ -1,0 +1,233 @@
+// Host-side geometry: per-ray and per-column tables built with the reference's
+// exact double arithmetic, the orderShuffleART ordering and the WBP row filters.
+// Compiled with -ffp-contract=off so that a*b+c is rounded twice, as in Java.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "tomo_internal.h"
+
+namespace tomo {
+
+namespace {
+
+constexpr double kAcc = (double)1e-10f;  // VoxelProjector3D.ACCURACY, a float constant (VoxelProjector3D.java:33)
+
+long long to_fix(double v) { return (long long)std::llrint(v * kFix); }
+
+// Finds the contiguous run of z in [0, n) where in(z) holds, starting from real
+// estimates za, zb of its two ends.  `in` must describe an interval.
+template <class F>
+void find_interval(int n, double za, double zb, F in, int* lo_out, int* cnt_out) {
+    if (za > zb) std::swap(za, zb);
+    *lo_out = 0;
+    *cnt_out = 0;
+    if (n <= 0) return;
+    auto clampi = [n](double v) -> int {
+        if (!(v == v)) return 0;
+        if (v < 0) return 0;
+        if (v > n - 1) return n - 1;
+        return (int)v;
+    };
+    // A point inside the interval, if any, is within a couple of steps of the estimate.
+    int seed = -1;
+    const int cands[] = {clampi(std::ceil(za)), clampi(std::floor(zb)), clampi(std::floor(0.5 * (za + zb))),
+                         clampi(std::ceil(za) + 1), clampi(std::floor(zb) - 1), clampi(std::ceil(za) - 1),
+                         clampi(std::floor(zb) + 1)};
+    for (int c : cands)
+        if (in(c)) { seed = c; break; }
+    if (seed < 0) return;
+    int lo = seed, hi = seed;
+    while (lo > 0 && in(lo - 1)) lo--;
+    while (hi + 1 < n && in(hi + 1)) hi++;
+    *lo_out = lo;
+    *cnt_out = hi - lo + 1;
+}
+
+}  // namespace
+
+bool tilt_is_separable(const double* R, const Geometry& g) {
+    if (g.scale != 1.0) return false;
+    if (!(R[0] != 0.0)) return false;
+    if (R[1] != 0.0 || R[3] != 0.0 || R[4] != 1.0 || R[5] != 0.0) return false;
+    const double o1 = g.pc[1] - g.vc[1], o3 = g.pc[3] - g.vc[1];
+    return o1 == std::floor(o1) && o3 == std::floor(o3);
+}
+
+// Forward-projection ray table of one tilt, following
+// VoxelProjector3D.projectJosephPartial (VoxelProjector3D.java:671-821) for a
+// separable tilt: the x position of ray i at plane z is the accumulated double
+// oldx + (z+1) dirX + volcenterx; the ray counts a plane when
+// x + ACCURACY >= 0 && x < W, and one extra normIncrement when it leaves the
+// volume laterally.
+void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays) {
+    const double dirY = -(R[5] - R[3] * R[2] / R[0]) / (R[4] - R[3] * R[1] / R[0]);
+    const double dirX = (R[1] * (-dirY) - R[2]) / R[0];
+    const double ninc = std::sqrt(dirX * dirX + dirY * dirY + 1);
+    const double vcx = g.vc[0], vcz = g.vc[2];
+    const double bXmax = (double)((float)g.W + 1e-10f);
+    tilt->step = to_fix(dirX);
+    tilt->ninc = ninc;
+    const int D = g.D;
+    // norm_sum is a float accumulating a double increment: norm(k) for k increments.
+    std::vector<float> normtab((size_t)D + 2, 0.0f);
+    for (int k = 1; k < D + 2; k++) normtab[k] = (float)((double)normtab[k - 1] + ninc);
+
+    for (int i = 0; i < g.w; i++) {
+        const double icentered = (i - g.pc[0]) / g.scale;
+        // oldy is jcentered on a separable tilt and R[1] * oldy is a signed zero.
+        double oldx0 = icentered - R[1] * 0.0 - R[2] * (-1 - vcz);
+        oldx0 /= R[0];
+        auto in_exact = [&](double x) { return x + kAcc >= 0 && x < bXmax; };
+        auto x_of = [&](int z) { return oldx0 + (z + 1) * dirX + vcx; };
+        bool near = false;
+        auto in_fast = [&](int z) {
+            const double x = x_of(z);
+            if (std::fabs(x + kAcc) < 1e-8 || std::fabs(x - bXmax) < 1e-8) near = true;
+            return in_exact(x);
+        };
+        int lo = 0, cnt = 0;
+        if (dirX == 0.0) {
+            if (in_exact(oldx0 + vcx)) { lo = 0; cnt = D; }
+        } else {
+            const double za = (-kAcc - vcx - oldx0) / dirX - 1.0;
+            const double zb = (bXmax - vcx - oldx0) / dirX - 1.0;
+            find_interval(D, za, zb, in_fast, &lo, &cnt);
+            if (near) {
+                // Replay the reference's accumulation exactly for rays that graze a border.
+                std::vector<char> flag((size_t)D, 0);
+                double oldx = oldx0;
+                for (int z = 0; z < D; z++) {
+                    const double xc = oldx + dirX;
+                    flag[z] = in_exact(xc + vcx);
+                    oldx = xc;
+                }
+                lo = 0;
+                cnt = 0;
+                int z = 0;
+                while (z < D && !flag[z]) z++;
+                if (z < D) {
+                    lo = z;
+                    while (z < D && flag[z]) z++;
+                    cnt = z - lo;
+                }
+            }
+        }
+        int incr = cnt;
+        if (cnt > 0 && lo + cnt - 1 < D - 1) incr++;  // extra increment when the ray exits the volume
+        FpRay r;
+        r.zab = (int32_t)((uint32_t)lo | ((uint32_t)cnt << 16));
+        r.norm = cnt > 0 ? normtab[incr] : 0.0f;
+        r.X0 = to_fix(oldx0 + dirX + vcx);
+        rays[i] = r;
+    }
+}
+
+// Backprojection tables of one tilt, following VoxelProjector3D.backProjectPartial
+// (VoxelProjector3D.java:221-308): xx = ((x~ R00 + y~ R01) + z~ R02) * scale + cix,
+// and a voxel contributes when 0 <= xx < w.  On a separable tilt y~ R01 is a
+// signed zero, so the decision depends on (x, z) only.
+void build_bp_tables(const Geometry& g, const double* R, BpTilt* tilt, int32_t* zint) {
+    const double cix = g.pc[2];
+    tilt->C = to_fix(R[0]);
+    tilt->S = to_fix(R[2]);
+    tilt->K = to_fix(cix - g.vc[0] * R[0] - g.vc[2] * R[2]);
+    for (int x = 0; x < g.W; x++) {
+        const double xt = x - g.vc[0];
+        const double a = xt * R[0] + 0.0 * R[1];
+        auto xx_of = [&](int k) {
+            const double z = k - g.vc[2];
+            return (a + z * R[2]) * g.scale + cix;
+        };
+        auto in = [&](int k) {
+            const double xx = xx_of(k);
+            return xx >= 0 && xx < g.w;
+        };
+        int lo = 0, cnt = 0;
+        if (R[2] == 0.0) {
+            if (in(0)) { lo = 0; cnt = g.D; }
+        } else {
+            const double za = (0.0 - cix - a) / R[2] + g.vc[2];
+            const double zb = ((double)g.w - cix - a) / R[2] + g.vc[2];
+            find_interval(g.D, za, zb, in, &lo, &cnt);
+        }
+        zint[x] = (int32_t)((uint32_t)lo | ((uint32_t)cnt << 16));
+    }
+}
+
+// TomoReconstruction2.orderShuffleART (TomoReconstruction2.java:735-781) with a
+// given first index: then repeatedly the remaining projection whose beam
+// direction (row 2 of its Euler matrix) is most perpendicular to the last one.
+void order_shuffle(int n, const double* euler, int first, int* out) {
+    std::vector<char> todo((size_t)n, 1);
+    int cc = 0, im = first;
+    while (cc < n) {
+        if (cc != 0) {
+            double mini = 1.7976931348623157e308;
+            int omini = -1;
+            const double* a = euler + 9 * im + 6;
+            for (int o = 0; o < n; o++) {
+                if (!todo[o]) continue;
+                const double* b = euler + 9 * o + 6;
+                const double sp = std::fabs(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+                if (sp < mini) { mini = sp; omini = o; }
+            }
+            im = omini;
+        }
+        if (todo[im]) { out[cc++] = im; todo[im] = 0; }
+    }
+}
+
+// SplitMix64 of (seed, iteration): the deterministic stand-in for Math.random().
+int first_index(uint64_t seed, int iteration, int nproj) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ULL * (uint64_t)(iteration + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z = z ^ (z >> 31);
+    return nproj > 0 ? (int)(z % (uint64_t)nproj) : 0;
+}
+
+// One row of the WBP frequency mask (row filters only depend on the column frequency).
+//  RADERMACHER: FFTWeighting.createWeightingMask (FFTWeighting.java:31-65) with a
+//               zero tilt-axis angle, where the mask is independent of the row.
+//  RAMP:        d_theta * |k| / w, DC term d_theta / (4 w).
+//  HAMMING_RAMP: RAMP * (0.54 + 0.46 cos(2 pi k / w)).
+// d_theta is the mean tilt spacing in radians (pi / N for a single tilt).
+void weighting_row_filter(int kind, int w, int nproj, const double* sint, const double* tilts_deg, double diameter,
+                          float* mask_row) {
+    const double cx = w / 2.0;
+    if (kind == 1) {
+        for (int i = 0; i < w; i++) {
+            const double ci = (i > cx) ? i - w : i;
+            double weight = 0;
+            for (int p = 0; p < nproj; p++) {
+                const double zj = (ci * sint[p] * 1.0 + 0.0 * sint[p] * 0.0) / w;
+                double value = diameter * M_PI * zj;
+                if (value == 0)
+                    value = 1;
+                else
+                    value = std::sin(value) / value;
+                weight += value;
+            }
+            if (weight < 0.005) weight = (double)0.005f;
+            weight *= diameter;
+            mask_row[i] = (float)(1 / weight);
+        }
+        return;
+    }
+    double tmin = 0, tmax = 0;
+    for (int p = 0; p < nproj; p++) {
+        if (p == 0 || tilts_deg[p] < tmin) tmin = tilts_deg[p];
+        if (p == 0 || tilts_deg[p] > tmax) tmax = tilts_deg[p];
+    }
+    const double dtheta = nproj > 1 ? (tmax - tmin) * (M_PI / 180.0) / (nproj - 1) : M_PI;
+    for (int i = 0; i < w; i++) {
+        const double ci = (i > cx) ? i - w : i;
+        double m = (ci == 0) ? dtheta / (4.0 * w) : dtheta * std::fabs(ci) / w;
+        if (kind == 3) m *= 0.54 + 0.46 * std::cos(2.0 * M_PI * ci / w);
+        mask_row[i] = (float)m;
+    }
+}
+
+}  // namespace tomo

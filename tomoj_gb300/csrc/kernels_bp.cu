@@ -1,0 +1,210 @@
+// Voxel-driven backprojection fused with the relaxation update (separable geometry).
+//
+// Reference: VoxelProjector3D.backproject / backProjectPartial
+// (TomoJ_Base/.../projectors/VoxelProjector3D.java:155-308) with ImageJ's
+// bilinear getInterpolatedValue.  The reference adds one tilt at a time to the
+// float volume (planez[i+jj] += value, then NaN/Inf -> 0 and optional
+// positivity); here every voxel is loaded once, all tilts of the update are
+// added to it in the same order with the same float rounding and checks, and it
+// is stored once.  The SIRT/OS-SART relaxation factor is already folded into the
+// difference images by the forward kernel (VoxelProjector3D.difference).
+//
+// CTA tile: 64 x-columns x 64 z-planes of one volume row.  Thread (tx, tzg)
+// owns the 16 voxels z = z0 + 16*tzg + k of column x0 + tx.  Per chunk of 32
+// tilts the CTA stages, for each tilt, the segment of the image row the tile
+// projects onto as (value, slope) pairs read with 128-bit loads, plus each
+// column's exact z-interval of voxels that fall inside the projection.
+#include <cmath>
+
+#include "device_util.cuh"
+#include "tomo_internal.h"
+
+namespace tomo {
+namespace {
+
+constexpr int kBpThreads = 256;
+constexpr int kTX = 64;
+constexpr int kTZ = 64;
+constexpr int kKZ = 16;      // voxels per thread along z
+constexpr int kTC = 32;      // tilts staged per chunk
+constexpr int kSeg = 96;     // >= 63 * (|cos| + |sin|) + 3 pairs per tilt segment
+constexpr int kRawSeg = 104; // floats staged per tilt (kSeg + 1 rounded up to float4, + alignment slack)
+
+struct BpShared {
+    float2 seg[kTC][kSeg];
+    float raw[kTC][kRawSeg];
+    int seg_start[kTC];
+    int raw_start[kTC];
+    long long K[kTC], C[kTC], S[kTC];
+    int zint[kTC][kTX];
+};
+
+template <bool SANITIZE, bool POS>
+__device__ __forceinline__ void bp_add(float& vox, float val) {
+    if (SANITIZE) {
+        if (!isnan(val)) {
+            float v = vox + val;
+            if (isnan(v) || isinf(v)) v = 0.0f;
+            if (POS && v < 0.0f) v = 0.0f;
+            vox = v;
+        }
+    } else {
+        float v = vox + val;
+        if (POS && v < 0.0f) v = 0.0f;
+        vox = v;
+    }
+}
+
+template <bool SANITIZE, bool POS>
+__global__ void __launch_bounds__(kBpThreads) bp_separable_kernel(BpLaunch a) {
+    __shared__ __align__(16) BpShared sh;
+    const int tid = threadIdx.x;
+    const int tx = tid & (kTX - 1);
+    const int tzg = tid >> 6;
+    const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
+    const int x0 = blockIdx.x * kTX;
+    const int z0 = blockIdx.y * kTZ;
+    const int r = a.y0 + blockIdx.z;
+    const int jp = r + a.row_off;  // projection row seen by this volume row
+    if (jp < 0 || jp >= h) return;  // no tilt reaches this row (yy outside [0,h))
+    const int x = x0 + tx;
+    const int zs = z0 + tzg * kKZ;
+    const bool xin = x < W;
+
+    float vox[kKZ];
+#pragma unroll
+    for (int k = 0; k < kKZ; k++) {
+        const int z = zs + k;
+        vox[k] = (xin && z < D) ? a.vol[((size_t)z * H + r) * W + x] : 0.0f;
+    }
+
+    const int xa = x0, xb = min(x0 + kTX - 1, W - 1);
+    const int za = z0, zb = min(z0 + kTZ - 1, D - 1);
+    const bool vec4 = ((w & 3) == 0) && ((reinterpret_cast<uintptr_t>(a.img) & 15) == 0);
+
+    for (int c0 = 0; c0 < a.T; c0 += kTC) {
+        const int tc = min(kTC, a.T - c0);
+        // --- per-tilt setup: fixed-point coefficients and segment start --------------
+        if (tid < tc) {
+            const int tilt = a.tilts[c0 + tid];
+            const BpTilt b = a.btilt[tilt];
+            sh.K[tid] = b.K;
+            sh.C[tid] = b.C;
+            sh.S[tid] = b.S;
+            const long long p00 = b.K + (long long)xa * b.C + (long long)za * b.S;
+            const long long p10 = b.K + (long long)xb * b.C + (long long)za * b.S;
+            const long long p01 = b.K + (long long)xa * b.C + (long long)zb * b.S;
+            const long long p11 = b.K + (long long)xb * b.C + (long long)zb * b.S;
+            const long long mn = min(min(p00, p10), min(p01, p11));
+            const int s = (int)(mn >> 32);
+            sh.seg_start[tid] = s;
+            sh.raw_start[tid] = s & ~3;
+        }
+        for (int e = tid; e < tc * kTX; e += kBpThreads) {
+            const int t = e / kTX, xx = e % kTX;
+            const int xc = x0 + xx;
+            sh.zint[t][xx] = (xc < W) ? a.zint[(size_t)a.tilts[c0 + t] * W + xc] : 0;
+        }
+        __syncthreads();
+        // --- stage image segments: 128-bit loads of the row, then (value, slope) pairs --
+        for (int e = tid; e < tc * (kRawSeg / 4); e += kBpThreads) {
+            const int t = e / (kRawSeg / 4), v = e % (kRawSeg / 4);
+            const float* row = a.img + ((size_t)(c0 + t) * h + jp) * w;
+            const int k0 = sh.raw_start[t] + 4 * v;
+            float4 q;
+            if (vec4 && k0 >= 0 && k0 + 3 < w) {
+                q = *reinterpret_cast<const float4*>(row + k0);
+            } else {
+                q.x = row[min(max(k0 + 0, 0), w - 1)];
+                q.y = row[min(max(k0 + 1, 0), w - 1)];
+                q.z = row[min(max(k0 + 2, 0), w - 1)];
+                q.w = row[min(max(k0 + 3, 0), w - 1)];
+            }
+            *reinterpret_cast<float4*>(&sh.raw[t][4 * v]) = q;
+        }
+        __syncthreads();
+        for (int e = tid; e < tc * kSeg; e += kBpThreads) {
+            const int t = e / kSeg, m = e % kSeg;
+            const int k = sh.seg_start[t] + m;       // image column of this pair
+            const int o = k - sh.raw_start[t];        // offset in the staged floats
+            const float* row = a.img + ((size_t)(c0 + t) * h + jp) * w;
+            float v0, d = 0.0f;
+            int k0, k1;
+            if (k >= 0 && k < w - 1) {
+                v0 = sh.raw[t][o];
+                d = sh.raw[t][o + 1] - v0;
+                k0 = k;
+                k1 = k + 1;
+            } else {
+                // ImageJ edge value: the last column is its own right neighbour; k < 0 only
+                // arises from fixed-point rounding of positions just above 0.
+                k0 = k1 = (k < 0) ? 0 : w - 1;
+                v0 = row[k0];
+            }
+            if (SANITIZE) {
+                // getInterpolatedValue blends in the next row with weight 0, so a
+                // non-finite neighbour there still turns the sample into NaN.
+                const float* up = (jp < h - 1) ? row + w : row;
+                if (!isfinite(up[k0]) || !isfinite(up[k1])) v0 = __int_as_float(0x7fc00000);
+            }
+            sh.seg[t][m] = make_float2(v0, d);
+        }
+        __syncthreads();
+        // --- accumulate the chunk's tilts in update order ----------------------------------
+        for (int t = 0; t < tc; t++) {
+            long long X = sh.K[t] + (long long)x * sh.C[t] + (long long)zs * sh.S[t];
+            const long long S = sh.S[t];
+            const int zi = sh.zint[t][tx];
+            const int kl = (zi & 0xFFFF) - zs;
+            const int cnt = (int)((uint32_t)zi >> 16);
+            const float2* seg = &sh.seg[t][0] - sh.seg_start[t];
+            const bool full = xin && kl <= 0 && kl + cnt >= kKZ;
+            if (__all_sync(0xffffffffu, full)) {
+#pragma unroll
+                for (int k = 0; k < kKZ; k++) {
+                    const float2 p = seg[(int)(X >> 32)];
+                    bp_add<SANITIZE, POS>(vox[k], fmaf(fix_frac((uint32_t)X), p.y, p.x));
+                    X += S;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < kKZ; k++) {
+                    if ((unsigned)(k - kl) < (unsigned)cnt) {
+                        const float2 p = seg[(int)(X >> 32)];
+                        bp_add<SANITIZE, POS>(vox[k], fmaf(fix_frac((uint32_t)X), p.y, p.x));
+                    }
+                    X += S;
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int k = 0; k < kKZ; k++) {
+        const int z = zs + k;
+        if (xin && z < D) a.vol[((size_t)z * H + r) * W + x] = vox[k];
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s) {
+    if (a.T <= 0 || a.y1 <= a.y0) return cudaSuccess;
+    dim3 grid((a.W + kTX - 1) / kTX, (a.D + kTZ - 1) / kTZ, a.y1 - a.y0);
+    if (a.sanitize) {
+        if (a.positivity)
+            bp_separable_kernel<true, true><<<grid, kBpThreads, 0, s>>>(a);
+        else
+            bp_separable_kernel<true, false><<<grid, kBpThreads, 0, s>>>(a);
+    } else {
+        if (a.positivity)
+            bp_separable_kernel<false, true><<<grid, kBpThreads, 0, s>>>(a);
+        else
+            bp_separable_kernel<false, false><<<grid, kBpThreads, 0, s>>>(a);
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace tomo

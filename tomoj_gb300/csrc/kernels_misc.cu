@@ -1,0 +1,359 @@
+// Supporting kernels: per-tilt alignment resample, WBP row filter (batched FFT),
+// deterministic residual reductions, TV denoise stencils, FISTA momentum, fills
+// and the long-object normalisation.  The library is compiled with -fmad=false,
+// so every a*b+c here rounds twice like the Java reference unless fmaf is used.
+#include <cmath>
+
+#include "device_util.cuh"
+#include "tomo_internal.h"
+
+namespace tomo {
+namespace {
+
+// AffineAlignment.applyTransformOnImage (TomoJ_Base/.../align/AffineAlignment.java:136-259):
+// inverse-map every output pixel through Tinv around (w/2, h/2), Java (int) truncation,
+// bilinear in double with the floor pixel on the last row/column, optional
+// (x - mean) / stdDev, and the TiltSeries fill policy outside the image.
+__global__ void align_kernel(const float* __restrict__ raw, float* __restrict__ out, const double* __restrict__ tinv,
+                             const double* __restrict__ stats, int w, int h, int normalize, int fill,
+                             const unsigned char* __restrict__ identity) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    const int t = blockIdx.z;
+    if (i >= w) return;
+    const float* un = raw + (size_t)t * w * h;
+    const double mean = stats ? stats[2 * t] : 0.0;
+    const double sd = stats ? stats[2 * t + 1] : 1.0;
+    float pix;
+    if (identity[t]) {
+        const float v = un[(size_t)j * w + i];
+        pix = normalize ? __double2float_rn(__ddiv_rn(__dsub_rn((double)v, mean), sd)) : v;
+    } else {
+        const double* T = tinv + 6 * t;  // {i00, i10, i01, i11, i02, i12}
+        const double cx = w / 2.0, cy = h / 2.0;
+        const double px = (double)i - cx, jc = (double)j - cy;
+        const double xx = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(T[0], px), __dmul_rn(T[2], jc)), T[4]), cx);
+        const double yy = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(T[1], px), __dmul_rn(T[3], jc)), T[5]), cy);
+        const int ix0 = __double2int_rz(xx), iy0 = __double2int_rz(yy);
+        const double dx0 = __dsub_rn(xx, (double)ix0), dy0 = __dsub_rn(yy, (double)iy0);
+        if (ix0 >= 0 && ix0 < w && iy0 >= 0 && iy0 < h) {
+            if (ix0 == w - 1 || iy0 == h - 1) {
+                pix = un[ix0 + (size_t)iy0 * w];
+            } else {
+                const double fac4 = __dmul_rn(dx0, dy0);
+                const size_t pos = ix0 + (size_t)iy0 * w;
+                const double v1 = un[pos], v3 = un[pos + w], v2 = un[pos + 1], v4 = un[pos + 1 + w];
+                const double w1 = __dadd_rn(__dsub_rn(__dsub_rn(1.0, dx0), dy0), fac4);
+                const double acc = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v1, w1), __dmul_rn(v2, __dsub_rn(dx0, fac4))),
+                                                       __dmul_rn(v3, __dsub_rn(dy0, fac4))),
+                                             __dmul_rn(v4, fac4));
+                pix = __double2float_rn(acc);
+            }
+            if (normalize) pix = __double2float_rn(__ddiv_rn(__dsub_rn((double)pix, mean), sd));
+        } else if (fill == 1) {
+            pix = normalize ? 0.0f : __double2float_rn(mean);
+        } else if (fill == 2) {
+            pix = __int_as_float(0x7fc00000);
+        } else {
+            pix = 0.0f;
+        }
+    }
+    out[(size_t)t * w * h + (size_t)j * w + i] = pix;
+}
+
+// --- WBP row filter --------------------------------------------------------------
+// FFTWeighting.weighting (FFTWeighting.java:87-112) multiplies the 2-D spectrum by
+// a mask that, for a zero tilt-axis angle, depends on the column frequency only;
+// the 2-D filter is then exactly a filter of every row.  Two real rows are packed
+// into one complex sequence (the mask is real and even, so the packed halves
+// stay separate), transformed by an in-shared-memory radix-2 FFT, multiplied by
+// the mask, transformed back and scaled by 1/w.
+__device__ __forceinline__ unsigned bitrev(unsigned v, int bits) { return __brev(v) >> (32 - bits); }
+
+__device__ void fft_stages(float2* s, const float2* __restrict__ tw, int n, int logn, bool inverse) {
+    for (int len = 2, stage = 0; len <= n; len <<= 1, stage++) {
+        const int half = len >> 1;
+        const int tstride = n / len;
+        __syncthreads();
+        for (int b = threadIdx.x; b < n / 2; b += blockDim.x) {
+            const int grp = b / half, k = b % half;
+            const int ia = grp * len + k, ib = ia + half;
+            float2 wv = tw[k * tstride];
+            if (inverse) wv.y = -wv.y;
+            const float2 xb = s[ib], xa = s[ia];
+            const float2 t = make_float2(xb.x * wv.x - xb.y * wv.y, xb.x * wv.y + xb.y * wv.x);
+            s[ib] = make_float2(xa.x - t.x, xa.y - t.y);
+            s[ia] = make_float2(xa.x + t.x, xa.y + t.y);
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void row_filter_kernel(float* img, const float* __restrict__ mask, const float2* __restrict__ tw, int rows,
+                                  int n, int logn) {
+    extern __shared__ float2 sbuf[];
+    float2* a = sbuf;
+    float2* b = sbuf + n;
+    const int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+    float* row0 = img + (size_t)r0 * n;
+    float* row1 = (r1 < rows) ? img + (size_t)r1 * n : nullptr;
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        a[bitrev(k, logn)] = make_float2(row0[k], row1 ? row1[k] : 0.0f);
+    fft_stages(a, tw, n, logn, false);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float m = mask[k];
+        const float2 v = a[k];
+        b[bitrev(k, logn)] = make_float2(v.x * m, v.y * m);
+    }
+    fft_stages(b, tw, n, logn, true);
+    const float inv = 1.0f / (float)n;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        row0[k] = b[k].x * inv;
+        if (row1) row1[k] = b[k].y * inv;
+    }
+}
+
+// Sum over rows of the per-row residuals, one thread per tilt, fixed order.
+__global__ void reduce_err_kernel(const double* __restrict__ errpart, double* __restrict__ err, int T, int h) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    double s = 0.0;
+    for (int j = 0; j < h; j++) s += errpart[(size_t)t * h + j];
+    err[t] = s;
+}
+
+// TotalVariationDenoising_3D.updateP (Filters/.../TotalVariationDenoising_3D.java:115-156).
+__global__ void tv_p_kernel(const float* __restrict__ u, float* px, float* py, float* pz, int W, int H, int D,
+                            float theta, float g, float dt) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const size_t o = ((size_t)z * H + y) * W + x;
+    const float u0 = u[o];
+    const float duy = (y < H - 1) ? u[o + W] - u0 : 0.0f;
+    const float dux = (x < W - 1) ? u[o + 1] - u0 : 0.0f;
+    const float duz = (z < D - 1) ? u[o + (size_t)W * H] - u0 : 0.0f;
+    const float s = duy * duy + dux * dux + duz * duz;
+    const float dd1 = 1.0f + dt / theta / g * fabsf(__fsqrt_rn(s));
+    const float k = dt / theta;
+    px[o] = __fdiv_rn(px[o] - k * dux, dd1);
+    py[o] = __fdiv_rn(py[o] - k * duy, dd1);
+    pz[o] = __fdiv_rn(pz[o] - k * duz, dd1);
+}
+
+// TotalVariationDenoising_3D.updateU (TotalVariationDenoising_3D.java:158-202).
+__global__ void tv_u_kernel(const float* __restrict__ f, float* __restrict__ u, const float* __restrict__ px,
+                            const float* __restrict__ py, const float* __restrict__ pz, int W, int H, int D,
+                            float theta) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const size_t o = ((size_t)z * H + y) * W + x;
+    float div;
+    if (x == 0) div = px[o];
+    else if (x == W - 1) div = -px[o];
+    else div = px[o] - px[o - 1];
+    if (y == 0) div += py[o];
+    else if (y == H - 1) div += -py[o];
+    else div += py[o] - py[o - W];
+    if (z == 0) div += pz[o];
+    else if (z == D - 1) div += -pz[o];
+    else div += pz[o] - pz[o - (size_t)W * H];
+    u[o] = f[o] - theta * div;
+}
+
+__global__ void fill_kernel(float* p, size_t n, float v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// FistaProjector3D.endOfIteration (FistaProjector3D.java:43-59) with addToPixel's NaN skip.
+__global__ void fista_kernel(float* rec, const float* __restrict__ prev, size_t n, double factor) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double val = __dmul_rn(factor, (double)(rec[i] - prev[i]));
+        if (!isnan(val)) rec[i] = rec[i] + __double2float_rn(val);
+    }
+}
+
+// Long-object compensation: every norm pixel of a projection becomes the projection's maximum.
+__global__ void long_object_kernel(float* norm, int npix) {
+    __shared__ float red[32];
+    float* n = norm + (size_t)blockIdx.x * npix;
+    float m = 0.0f;
+    for (int i = threadIdx.x; i < npix; i += blockDim.x) m = fmaxf(m, n[i]);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = (threadIdx.x < blockDim.x / 32) ? red[threadIdx.x] : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) red[0] = m;
+    }
+    __syncthreads();
+    m = red[0];
+    for (int i = threadIdx.x; i < npix; i += blockDim.x) n[i] = m;
+}
+
+// VoxelProjector3D.difference (VoxelProjector3D.java:414-433) over precomputed projections
+// (used when long-object compensation replaces the norms after projection).
+__global__ void diff_kernel(const float* __restrict__ meas, const int* __restrict__ tilts, const float* __restrict__ th,
+                            const float* __restrict__ norm, float* __restrict__ diff, double* __restrict__ errpart,
+                            int w, int h, int j0, int j1, double factor) {
+    __shared__ double red[32];
+    const int b = blockIdx.y;
+    const int j = blockIdx.x;
+    double e2 = 0.0;
+    if (j >= j0 && j < j1) {
+        const float* e = meas + ((size_t)tilts[b] * h + j) * w;
+        const size_t o = ((size_t)b * h + j) * w;
+        for (int i = threadIdx.x; i < w; i += blockDim.x) {
+            const float ev = e[i], tv = th[o + i];
+            float d = 0.0f;
+            if (!isnan(ev) && !isnan(tv)) {
+                const float q = __fdiv_rn(ev - tv, norm[o + i]);
+                const double v = (double)q * factor;
+                d = __double2float_rn(v);
+                e2 += v * v;
+            }
+            diff[o + i] = d;
+        }
+    } else {
+        const size_t o = ((size_t)b * h + j) * w;
+        for (int i = threadIdx.x; i < w; i += blockDim.x) diff[o + i] = 0.0f;
+    }
+    e2 = warp_sum(e2);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (int)blockDim.x / 32; k++) s += red[k];
+        errpart[(size_t)b * h + j] = s;
+    }
+}
+
+// Copies image tilts[b] of src into slot b of dst (addProjection's fresh copy).
+__global__ void gather_kernel(float* __restrict__ dst, const float* __restrict__ src, const int* __restrict__ tilts,
+                              size_t npix) {
+    const int b = blockIdx.y;
+    const float* s = src + (size_t)tilts[b] * npix;
+    float* d = dst + (size_t)b * npix;
+    if ((npix & 3) == 0) {  // every image starts 16-byte aligned
+        const float4* s4 = reinterpret_cast<const float4*>(s);
+        float4* d4 = reinterpret_cast<float4*>(d);
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix / 4;
+             i += (size_t)gridDim.x * blockDim.x)
+            d4[i] = s4[i];
+    } else {
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x)
+            d[i] = s[i];
+    }
+}
+
+// flags[0] |= 1 if any NaN, flags[0] |= 2 if any +-Inf.
+__global__ void scan_nonfinite_kernel(const float* __restrict__ p, size_t n, int* flags) {
+    int f = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = p[i];
+        if (isnan(v)) f |= 1;
+        else if (isinf(v)) f |= 2;
+    }
+    f = __reduce_or_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && f) atomicOr(flags, f);
+}
+
+}  // namespace
+
+cudaError_t misc_init_attributes() {
+    return cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                2 * 4096 * (int)sizeof(float2));
+}
+
+cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s) {
+    if (T <= 0) return cudaSuccess;
+    dim3 grid((unsigned)std::min<size_t>((npix / 4 + 255) / 256 + 1, 64), T);
+    gather_kernel<<<grid, 256, 0, s>>>(dst, src, tilts, npix);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+    scan_nonfinite_kernel<<<blocks, 256, 0, s>>>(p, n, flags);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_align(const float* raw, float* out, const double* tinv, const double* stats, int N, int w, int h,
+                         int normalize, int fill, const unsigned char* identity, cudaStream_t s) {
+    dim3 grid((w + 127) / 128, h, N);
+    align_kernel<<<grid, 128, 0, s>>>(raw, out, tinv, stats, w, h, normalize, fill, identity);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2* tw, int rows, int w,
+                                 cudaStream_t s) {
+    int logn = 0;
+    while ((1 << logn) < w) logn++;
+    if ((1 << logn) != w) return cudaErrorInvalidValue;
+    const size_t smem = 2 * (size_t)w * sizeof(float2);
+    row_filter_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, mask_row, tw, rows, w, logn);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s) {
+    reduce_err_kernel<<<(T + 127) / 128, 128, 0, s>>>(errpart, err, T, h);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tv_p(const float* u, float* px, float* py, float* pz, int W, int H, int D, float theta, float g,
+                        float dt, cudaStream_t s) {
+    dim3 grid((W + 127) / 128, H, D);
+    tv_p_kernel<<<grid, 128, 0, s>>>(u, px, py, pz, W, H, D, theta, g, dt);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* py, const float* pz, int W, int H,
+                        int D, float theta, cudaStream_t s) {
+    dim3 grid((W + 127) / 128, H, D);
+    tv_u_kernel<<<grid, 128, 0, s>>>(f, u, px, py, pz, W, H, D, theta);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    fill_kernel<<<blocks, 256, 0, s>>>(p, n, v);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    fista_kernel<<<blocks, 256, 0, s>>>(rec, prev, n, factor);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s) {
+    if (T <= 0) return cudaSuccess;
+    long_object_kernel<<<T, 512, 0, s>>>(norm, h * w);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diff(const float* meas, const int* tilts, const float* th, const float* norm, float* diff,
+                        double* errpart, int T, int w, int h, int j0, int j1, double factor, cudaStream_t s) {
+    if (T <= 0) return cudaSuccess;
+    diff_kernel<<<dim3(h, T), 256, 0, s>>>(meas, tilts, th, norm, diff, errpart, w, h, j0, j1, factor);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace tomo

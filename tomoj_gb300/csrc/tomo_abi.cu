@@ -1,0 +1,853 @@
+// C ABI of the engine: handles, admission control, the Projector surface and
+// the TomoReconstruction2 drivers.  See include/tomoj_gb300.h for the contract.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tomoj_gb300.h"
+#include "tomo_internal.h"
+
+namespace tomo {
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(int n) { g_launches += (uint64_t)n; }
+}  // namespace tomo
+
+using namespace tomo;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<uint64_t> g_in_use{0};
+std::atomic<uint64_t> g_limit{0};
+
+tomo_status fail(tomo_status code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(expr)                                                                                      \
+    do {                                                                                              \
+        cudaError_t _e = (expr);                                                                      \
+        if (_e != cudaSuccess)                                                                        \
+            return fail(TOMO_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));           \
+    } while (0)
+
+#define CKS(expr)                     \
+    do {                              \
+        tomo_status _s = (expr);      \
+        if (_s != TOMO_OK) return _s; \
+    } while (0)
+
+}  // namespace
+
+struct tomo_projector {
+    Geometry g{};
+    tomo_params params{};
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int device = 0;
+    size_t npix = 0, nvox = 0;
+    std::vector<void*> allocs;
+    uint64_t bytes = 0;
+
+    float* d_vol = nullptr;
+    float* d_raw = nullptr;
+    float* d_meas = nullptr;
+    float* d_proj = nullptr;
+    float* d_norm = nullptr;
+    float* d_diff = nullptr;
+    float* d_obatch = nullptr;
+    double* d_errpart = nullptr;
+    double* d_err = nullptr;
+    int* d_batch = nullptr;
+    int* d_orders = nullptr;
+    int orders_cap = 0;
+    int* d_status = nullptr;
+    int* d_flags = nullptr;
+    FpTilt* d_ftilt = nullptr;
+    FpRay* d_rays = nullptr;
+    BpTilt* d_btilt = nullptr;
+    int32_t* d_zint = nullptr;
+    double* d_tinv = nullptr;
+    double* d_stats = nullptr;
+    unsigned char* d_identity = nullptr;
+    float* d_mask = nullptr;
+    float2* d_tw = nullptr;
+    float *d_tv_u = nullptr, *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;
+    float* d_prev = nullptr;
+
+    std::vector<double> euler;
+    std::vector<int> batch;
+    bool batch_uploaded = false;
+    bool series_loaded = false;
+    bool diffs_valid = false;
+    bool projected = false;
+    bool obatch_valid = false;
+    bool meas_has_nan = false, meas_has_inf = false;
+    bool vol_nonfinite = false;
+    int weight_kind = TOMO_WEIGHT_NONE;
+    float tv_theta = 25.0f, tv_g = 1.0f, tv_dt = 0.1f;
+    int tv_iters = 0;
+    bool fista = false;
+    double fista_t = 0.0;
+    std::atomic<int> cancel{0};
+    int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+};
+
+namespace {
+
+tomo_status dalloc(tomo_projector* p, void** ptr, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    const uint64_t lim = g_limit.load();
+    if (lim != 0 && g_in_use.load() + bytes > lim)
+        return fail(TOMO_ERR_NOMEM, "admission: " + std::to_string(bytes) + " bytes exceed the memory limit");
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes > free_b)
+        return fail(TOMO_ERR_NOMEM, "admission: " + std::to_string(bytes) + " bytes exceed free HBM");
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(TOMO_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    p->allocs.push_back(*ptr);
+    p->bytes += bytes;
+    g_in_use += bytes;
+    return TOMO_OK;
+}
+
+template <class T>
+tomo_status alloc_n(tomo_projector* p, T** ptr, size_t n) {
+    return dalloc(p, reinterpret_cast<void**>(ptr), n * sizeof(T));
+}
+
+tomo_status check_status(tomo_projector* p) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    if (st != 0) {
+        CK(cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream));
+        return fail(TOMO_ERR_DEVICE, "a kernel reported status " + std::to_string(st) + " (bounded wait expired)");
+    }
+    return TOMO_OK;
+}
+
+tomo_status upload_batch(tomo_projector* p) {
+    if (p->batch_uploaded) return TOMO_OK;
+    if (!p->batch.empty())
+        CK(cudaMemcpyAsync(p->d_batch, p->batch.data(), p->batch.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           p->stream));
+    // the host vector may change after this call: make the copy complete first
+    CK(cudaStreamSynchronize(p->stream));
+    p->batch_uploaded = true;
+    return TOMO_OK;
+}
+
+// Projection row range of project(y0,y1) (VoxelProjector3D.java:338-352): from
+// round((y0 + offset) * scale) to the projection height.
+void fp_rows(const tomo_projector* p, int y0, int* j0, int* j1) {
+    const Geometry& g = p->g;
+    const int offset = (g.h > g.H && g.scale == 1) ? (g.h - g.H) / 2 : 0;
+    int s = (int)std::floor((y0 + offset) * g.scale + 0.5);
+    if (s < 0) s = 0;
+    *j0 = s;
+    *j1 = g.h;
+}
+
+int auto_tilts_per_cta(const tomo_projector* p, int T, int rows) {
+    const int tgmax = fp_max_tilts_per_cta(p->g.w);
+    if (p->tilts_per_cta > 0) return std::min(p->tilts_per_cta, tgmax);
+    // enough CTAs to fill two per SM, else the widest grouping (fewest volume re-reads)
+    int groups = (T + tgmax - 1) / tgmax;
+    int target = 2 * 152;
+    while ((long long)groups * rows < target && groups < T) groups++;
+    return (T + groups - 1) / groups;
+}
+
+// Forward projection of the current batch, with the fused difference when meas is given.
+tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool with_diff, double factor,
+                   int slot0) {
+    const Geometry& g = p->g;
+    int j0, j1;
+    fp_rows(p, y0, &j0, &j1);
+    float* proj = p->d_proj + (size_t)slot0 * p->npix;
+    float* norm = p->d_norm + (size_t)slot0 * p->npix;
+    float* diff = p->d_diff + (size_t)slot0 * p->npix;
+    double* errpart = p->d_errpart + (size_t)slot0 * g.h;
+    if (j0 > 0) {
+        // rows the reference leaves untouched stay zero (fresh FloatProcessors)
+        for (int b = 0; b < T; b++) {
+            CK(cudaMemsetAsync(proj + (size_t)b * p->npix, 0, sizeof(float) * (size_t)std::min(j0, g.h) * g.w,
+                               p->stream));
+            CK(cudaMemsetAsync(norm + (size_t)b * p->npix, 0, sizeof(float) * (size_t)std::min(j0, g.h) * g.w,
+                               p->stream));
+            if (with_diff)
+                CK(cudaMemsetAsync(diff + (size_t)b * p->npix, 0, sizeof(float) * (size_t)std::min(j0, g.h) * g.w,
+                                   p->stream));
+        }
+        if (with_diff) CK(cudaMemsetAsync(errpart, 0, sizeof(double) * (size_t)T * g.h, p->stream));
+    }
+    if (j0 >= j1) return TOMO_OK;
+    FpLaunch a{};
+    a.vol = p->d_vol;
+    a.meas = (with_diff && !p->params.long_object) ? p->d_meas : nullptr;
+    a.tilts = d_tilts;
+    a.T = T;
+    a.ftilt = p->d_ftilt;
+    a.rays = p->d_rays;
+    a.proj = proj;
+    a.norm = norm;
+    a.diff = diff;
+    a.errpart = errpart;
+    a.factor = factor;
+    a.j0 = j0;
+    a.j1 = j1;
+    a.tilts_per_cta = auto_tilts_per_cta(p, T, j1 - j0);
+    a.W = g.W;
+    a.H = g.H;
+    a.D = g.D;
+    a.w = g.w;
+    a.h = g.h;
+    a.row_off = g.fp_row_off;
+    a.status = p->d_status;
+    CK(launch_fp_separable(a, p->stream));
+    if (p->params.long_object) {
+        CK(launch_long_object(norm, T, g.h, g.w, p->stream));
+        if (with_diff)
+            CK(launch_diff(p->d_meas, d_tilts, proj, norm, diff, errpart, T, g.w, g.h, j0, j1, factor, p->stream));
+    }
+    if (with_diff) CK(launch_reduce_err(errpart, p->d_err + slot0, T, g.h, p->stream));
+    return TOMO_OK;
+}
+
+tomo_status apply_weighting(tomo_projector* p, float* imgs, int T) {
+    if (p->weight_kind == TOMO_WEIGHT_NONE || T <= 0) return TOMO_OK;
+    CK(launch_row_filter_tw(imgs, p->d_mask, p->d_tw, T * p->g.h, p->g.w, p->stream));
+    return TOMO_OK;
+}
+
+tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int T, int y0, int y1, bool sanitize) {
+    const Geometry& g = p->g;
+    y0 = std::max(0, y0);
+    y1 = std::min(g.H, y1);
+    if (y1 <= y0 || T <= 0) return TOMO_OK;
+    BpLaunch a{};
+    a.vol = p->d_vol;
+    a.img = imgs;
+    a.tilts = d_tilts;
+    a.T = T;
+    a.btilt = p->d_btilt;
+    a.zint = p->d_zint;
+    a.y0 = y0;
+    a.y1 = y1;
+    a.W = g.W;
+    a.H = g.H;
+    a.D = g.D;
+    a.w = g.w;
+    a.h = g.h;
+    a.row_off = g.bp_row_off;
+    a.positivity = p->params.positivity;
+    a.sanitize = sanitize || p->vol_nonfinite;
+    a.status = p->d_status;
+    CK(launch_bp_separable(a, p->stream));
+    return TOMO_OK;
+}
+
+tomo_status need_series(tomo_projector* p) {
+    if (!p->series_loaded) return fail(TOMO_ERR_STATE, "no tilt-series loaded (tomo_load_series)");
+    if (!p->g.separable)
+        return fail(TOMO_ERR_UNSUPPORTED,
+                    "geometry is not supported on the device: it needs a vertical tilt axis, scale 1 and "
+                    "integral row offsets between projection and volume centres");
+    return TOMO_OK;
+}
+
+tomo_status tv_denoise(tomo_projector* p) {
+    const Geometry& g = p->g;
+    if (p->tv_iters <= 0) return TOMO_OK;
+    const size_t bytes = sizeof(float) * p->nvox;
+    CK(cudaMemcpyAsync(p->d_tv_u, p->d_vol, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    CK(cudaMemsetAsync(p->d_px, 0, bytes, p->stream));
+    CK(cudaMemsetAsync(p->d_py, 0, bytes, p->stream));
+    CK(cudaMemsetAsync(p->d_pz, 0, bytes, p->stream));
+    for (int it = 0; it < p->tv_iters; it++) {
+        CK(launch_tv_p(p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->tv_g, p->tv_dt,
+                       p->stream));
+        CK(launch_tv_u(p->d_vol, p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->stream));
+    }
+    CK(cudaMemcpyAsync(p->d_vol, p->d_tv_u, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    return TOMO_OK;
+}
+
+tomo_status end_iteration(tomo_projector* p) {
+    CKS(tv_denoise(p));
+    if (p->fista) {
+        const double t_1 = p->fista_t;
+        p->fista_t = (1 + std::sqrt(1 + 4 * p->fista_t * p->fista_t)) / 2;
+        const double factor = (t_1 - 1) / p->fista_t;
+        CK(launch_fista(p->d_vol, p->d_prev, p->nvox, factor, p->stream));
+    }
+    return TOMO_OK;
+}
+
+tomo_status start_iteration(tomo_projector* p) {
+    if (p->fista)
+        CK(cudaMemcpyAsync(p->d_prev, p->d_vol, sizeof(float) * p->nvox, cudaMemcpyDeviceToDevice, p->stream));
+    return TOMO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t tomo_abi_version(void) { return TOMO_ABI_VERSION; }
+const char* tomo_last_error(void) { return g_err.c_str(); }
+
+tomo_status tomo_set_memory_limit(uint64_t bytes) {
+    g_limit = bytes;
+    return TOMO_OK;
+}
+uint64_t tomo_memory_in_use(void) { return g_in_use.load(); }
+uint64_t tomo_kernel_launches(void) { return g_launches.load(); }
+
+tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_projector** out) {
+    if (!geom || !out) return fail(TOMO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (geom->W <= 0 || geom->H <= 0 || geom->D <= 0 || geom->w <= 0 || geom->h <= 0 || geom->nproj <= 0)
+        return fail(TOMO_ERR_INVALID, "dimensions must be positive");
+    if (geom->D > 65535 || geom->w > 4096 || geom->W > 65535)
+        return fail(TOMO_ERR_UNSUPPORTED, "D <= 65535, W <= 65535 and w <= 4096 are supported");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(TOMO_ERR_CUDA, "no CUDA device");
+    }
+    tomo_projector* p = new tomo_projector();
+    Geometry& g = p->g;
+    g.W = geom->W;
+    g.H = geom->H;
+    g.D = geom->D;
+    g.w = geom->w;
+    g.h = geom->h;
+    g.N = geom->nproj;
+    const double dvc[3] = {(g.W - 1) / 2.0, (g.H - 1) / 2.0, (g.D - 1) / 2.0};
+    const double dpc[4] = {(g.w - 1.0) / 2, (g.h - 1.0) / 2, (g.w - 1) / 2.0, (g.h - 1) / 2.0};
+    for (int k = 0; k < 3; k++) g.vc[k] = std::isnan(geom->vol_center[k]) ? dvc[k] : geom->vol_center[k];
+    for (int k = 0; k < 4; k++) g.pc[k] = std::isnan(geom->proj_center[k]) ? dpc[k] : geom->proj_center[k];
+    g.scale = geom->scale == 0.0 ? 1.0 : geom->scale;
+    if (params) p->params = *params;
+    cudaGetDevice(&p->device);
+    p->npix = (size_t)g.w * g.h;
+    p->nvox = (size_t)g.W * g.H * g.D;
+    const size_t N = (size_t)g.N;
+    tomo_status st = TOMO_OK;
+    auto A = [&](tomo_status s) {
+        if (st == TOMO_OK) st = s;
+    };
+    A(alloc_n(p, &p->d_vol, p->nvox));
+    A(alloc_n(p, &p->d_raw, N * p->npix));
+    A(alloc_n(p, &p->d_meas, N * p->npix));
+    A(alloc_n(p, &p->d_proj, N * p->npix));
+    A(alloc_n(p, &p->d_norm, N * p->npix));
+    A(alloc_n(p, &p->d_diff, N * p->npix));
+    A(alloc_n(p, &p->d_obatch, N * p->npix));
+    A(alloc_n(p, &p->d_errpart, N * g.h));
+    A(alloc_n(p, &p->d_err, N));
+    A(alloc_n(p, &p->d_batch, N));
+    A(alloc_n(p, &p->d_status, 1));
+    A(alloc_n(p, &p->d_flags, 1));
+    A(alloc_n(p, &p->d_ftilt, N));
+    A(alloc_n(p, &p->d_rays, N * g.w));
+    A(alloc_n(p, &p->d_btilt, N));
+    A(alloc_n(p, &p->d_zint, N * g.W));
+    A(alloc_n(p, &p->d_tinv, N * 6));
+    A(alloc_n(p, &p->d_stats, N * 2));
+    A(alloc_n(p, &p->d_identity, N));
+    A(alloc_n(p, &p->d_mask, (size_t)g.w));
+    A(alloc_n(p, &p->d_tw, (size_t)g.w));
+    if (st == TOMO_OK) {
+        if (cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            st = fail(TOMO_ERR_CUDA, "cudaStreamCreate failed");
+        }
+    }
+    if (st != TOMO_OK) {
+        std::string msg = g_err;
+        tomo_destroy(p);
+        g_err = msg;
+        return st;
+    }
+    p->stream = p->own_stream;
+    if (fp_init_attributes() != cudaSuccess || misc_init_attributes() != cudaSuccess) {
+        tomo_destroy(p);
+        return fail(TOMO_ERR_CUDA, "cannot configure kernel shared memory");
+    }
+    cudaMemsetAsync(p->d_vol, 0, sizeof(float) * p->nvox, p->stream);
+    cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream);
+    cudaMemsetAsync(p->d_err, 0, sizeof(double) * N, p->stream);
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess) {
+        tomo_destroy(p);
+        return fail(TOMO_ERR_CUDA, "initialisation failed");
+    }
+    *out = p;
+    return TOMO_OK;
+}
+
+tomo_status tomo_destroy(tomo_projector* p) {
+    if (!p) return TOMO_OK;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (void* a : p->allocs) cudaFree(a);
+    g_in_use -= p->bytes;
+    if (p->own_stream) cudaStreamDestroy(p->own_stream);
+    delete p;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_stream(tomo_projector* p, void* stream) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CK(cudaStreamSynchronize(p->stream));
+    p->stream = stream ? static_cast<cudaStream_t>(stream) : p->own_stream;
+    return TOMO_OK;
+}
+
+tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pixels_on_device, const double* euler,
+                             const double* transforms, const double* stats) {
+    if (!p || !pixels || !euler) return fail(TOMO_ERR_INVALID, "null argument");
+    Geometry& g = p->g;
+    const int N = g.N;
+    CK(cudaMemcpyAsync(p->d_raw, pixels, sizeof(float) * N * p->npix,
+                       pixels_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, p->stream));
+    p->euler.assign(euler, euler + 9 * (size_t)N);
+    // geometry tables
+    bool sep = true;
+    for (int t = 0; t < N && sep; t++) sep = tilt_is_separable(&p->euler[9 * t], g);
+    g.separable = sep;
+    if (sep) {
+        g.fp_row_off = (int)(g.pc[1] - g.vc[1]);
+        g.bp_row_off = (int)(g.pc[3] - g.vc[1]);
+        std::vector<FpTilt> ft(N);
+        std::vector<FpRay> rays((size_t)N * g.w);
+        std::vector<BpTilt> bt(N);
+        std::vector<int32_t> zint((size_t)N * g.W);
+        for (int t = 0; t < N; t++) {
+            build_fp_tables(g, &p->euler[9 * t], &ft[t], &rays[(size_t)t * g.w]);
+            build_bp_tables(g, &p->euler[9 * t], &bt[t], &zint[(size_t)t * g.W]);
+        }
+        CK(cudaMemcpyAsync(p->d_ftilt, ft.data(), sizeof(FpTilt) * N, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_rays, rays.data(), sizeof(FpRay) * rays.size(), cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_btilt, bt.data(), sizeof(BpTilt) * N, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_zint, zint.data(), sizeof(int32_t) * zint.size(), cudaMemcpyHostToDevice,
+                           p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+    }
+    // alignment: Tinv = AffineTransform.createInverse (general case)
+    std::vector<double> tinv((size_t)N * 6), st((size_t)N * 2);
+    std::vector<unsigned char> ident(N);
+    for (int t = 0; t < N; t++) {
+        double T[6] = {1, 0, 0, 1, 0, 0};
+        if (transforms) std::memcpy(T, transforms + 6 * t, sizeof(T));
+        ident[t] = (T[0] == 1.0 && T[1] == 0.0 && T[2] == 0.0 && T[3] == 1.0 && T[4] == 0.0 && T[5] == 0.0);
+        const double m00 = T[0], m10 = T[1], m01 = T[2], m11 = T[3], m02 = T[4], m12 = T[5];
+        const double det = m00 * m11 - m01 * m10;
+        if (!ident[t] && !(std::fabs(det) > 4.9e-324))
+            return fail(TOMO_ERR_INVALID, "transform " + std::to_string(t) + " is not invertible");
+        double* I = &tinv[6 * (size_t)t];
+        I[0] = m11 / det;
+        I[1] = -m10 / det;
+        I[2] = -m01 / det;
+        I[3] = m00 / det;
+        I[4] = (m01 * m12 - m11 * m02) / det;
+        I[5] = (m10 * m02 - m00 * m12) / det;
+        st[2 * t] = stats ? stats[2 * t] : 0.0;
+        st[2 * t + 1] = stats ? stats[2 * t + 1] : 1.0;
+    }
+    CK(cudaMemcpyAsync(p->d_tinv, tinv.data(), sizeof(double) * tinv.size(), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_stats, st.data(), sizeof(double) * st.size(), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_identity, ident.data(), N, cudaMemcpyHostToDevice, p->stream));
+    CK(launch_align(p->d_raw, p->d_meas, p->d_tinv, p->d_stats, N, g.w, g.h, p->params.normalize, p->params.fill,
+                    p->d_identity, p->stream));
+    int flags = 0;
+    CK(cudaMemsetAsync(p->d_flags, 0, sizeof(int), p->stream));
+    CK(launch_scan_nonfinite(p->d_meas, (size_t)N * p->npix, p->d_flags, p->stream));
+    CK(cudaMemcpyAsync(&flags, p->d_flags, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->meas_has_nan = (flags & 1) != 0;
+    p->meas_has_inf = (flags & 2) != 0;
+    p->series_loaded = true;
+    p->batch.clear();
+    p->batch_uploaded = false;
+    p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_get_aligned(tomo_projector* p, int32_t index, float* out_host) {
+    if (!p || !out_host) return fail(TOMO_ERR_INVALID, "null argument");
+    if (!p->series_loaded) return fail(TOMO_ERR_STATE, "no tilt-series loaded");
+    if (index < 0 || index >= p->g.N) return fail(TOMO_ERR_INVALID, "index out of range");
+    CK(cudaMemcpyAsync(out_host, p->d_meas + (size_t)index * p->npix, sizeof(float) * p->npix,
+                       cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return TOMO_OK;
+}
+
+static tomo_status volume_copy(tomo_projector* p, float* host_or_dev, int on_device, int y0, int y1, bool to_dev) {
+    const Geometry& g = p->g;
+    if (y0 < 0 || y1 > g.H || y1 < y0) return fail(TOMO_ERR_INVALID, "row range outside the volume");
+    if (y1 == y0) return TOMO_OK;
+    const size_t rows = (size_t)(y1 - y0);
+    // [D][rows][W] <-> [D][H][W] rows y0..y1 of every slice
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice
+                                    : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+    float* dev = p->d_vol + (size_t)y0 * g.W;
+    if (to_dev)
+        CK(cudaMemcpy2DAsync(dev, sizeof(float) * g.W * g.H, host_or_dev, sizeof(float) * g.W * rows,
+                             sizeof(float) * g.W * rows, g.D, kind, p->stream));
+    else
+        CK(cudaMemcpy2DAsync(host_or_dev, sizeof(float) * g.W * rows, dev, sizeof(float) * g.W * g.H,
+                             sizeof(float) * g.W * rows, g.D, kind, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_volume(tomo_projector* p, const float* src, int32_t on_device, int32_t y0, int32_t y1) {
+    if (!p || !src) return fail(TOMO_ERR_INVALID, "null argument");
+    CKS(volume_copy(p, const_cast<float*>(src), on_device, y0, y1, true));
+    int flags = 0;
+    CK(cudaMemsetAsync(p->d_flags, 0, sizeof(int), p->stream));
+    CK(launch_scan_nonfinite(p->d_vol, p->nvox, p->d_flags, p->stream));
+    CK(cudaMemcpyAsync(&flags, p->d_flags, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->vol_nonfinite = flags != 0;
+    return TOMO_OK;
+}
+
+tomo_status tomo_get_volume(tomo_projector* p, float* dst, int32_t on_device, int32_t y0, int32_t y1) {
+    if (!p || !dst) return fail(TOMO_ERR_INVALID, "null argument");
+    return volume_copy(p, dst, on_device, y0, y1, false);
+}
+
+tomo_status tomo_fill_volume(tomo_projector* p, float value) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CK(launch_fill(p->d_vol, p->nvox, value, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->vol_nonfinite = !std::isfinite(value);
+    return TOMO_OK;
+}
+
+tomo_status tomo_volume_device_ptr(tomo_projector* p, float** out) {
+    if (!p || !out) return fail(TOMO_ERR_INVALID, "null argument");
+    *out = p->d_vol;
+    return TOMO_OK;
+}
+
+tomo_status tomo_add_projection(tomo_projector* p, int32_t index) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (!p->series_loaded) return fail(TOMO_ERR_STATE, "no tilt-series loaded");
+    if (index < 0 || index >= p->g.N) return fail(TOMO_ERR_INVALID, "projection index out of range");
+    if ((int)p->batch.size() >= p->g.N) return fail(TOMO_ERR_INVALID, "more projections added than slots");
+    p->batch.push_back(index);
+    p->batch_uploaded = false;
+    p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_clear_projections(tomo_projector* p) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    p->batch.clear();
+    p->batch_uploaded = false;
+    p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+int32_t tomo_projection_count(tomo_projector* p) { return p ? (int32_t)p->batch.size() : 0; }
+
+tomo_status tomo_project(tomo_projector* p, int32_t y0, int32_t y1) {
+    (void)y1;
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(need_series(p));
+    CKS(upload_batch(p));
+    CKS(run_fp(p, p->d_batch, (int)p->batch.size(), y0, false, 0.0, 0));
+    CKS(check_status(p));
+    p->projected = true;
+    p->diffs_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_project_and_difference(tomo_projector* p, double factor, int32_t y0, int32_t y1, double* err_out) {
+    (void)y1;
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(need_series(p));
+    CKS(upload_batch(p));
+    const int T = (int)p->batch.size();
+    CKS(run_fp(p, p->d_batch, T, y0, true, factor, 0));
+    if (err_out && T > 0)
+        CK(cudaMemcpyAsync(err_out, p->d_err, sizeof(double) * T, cudaMemcpyDeviceToHost, p->stream));
+    CKS(check_status(p));
+    p->projected = true;
+    p->diffs_valid = true;
+    return TOMO_OK;
+}
+
+tomo_status tomo_backproject(tomo_projector* p, int32_t y0, int32_t y1) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(need_series(p));
+    CKS(upload_batch(p));
+    const int T = (int)p->batch.size();
+    if (T == 0) return TOMO_OK;
+    const float* imgs;
+    bool sanitize;
+    if (p->diffs_valid) {
+        CKS(apply_weighting(p, p->d_diff, T));
+        imgs = p->d_diff;
+        sanitize = p->meas_has_inf;
+    } else {
+        if (!p->obatch_valid) {
+            CK(launch_gather(p->d_obatch, p->d_meas, p->d_batch, T, p->npix, p->stream));
+            p->obatch_valid = true;
+        }
+        CKS(apply_weighting(p, p->d_obatch, T));
+        imgs = p->d_obatch;
+        sanitize = p->meas_has_nan || p->meas_has_inf;
+    }
+    CKS(run_bp(p, imgs, p->d_batch, T, y0, y1, sanitize));
+    CKS(check_status(p));
+    return TOMO_OK;
+}
+
+tomo_status tomo_start_iteration(tomo_projector* p) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(start_iteration(p));
+    return TOMO_OK;
+}
+
+tomo_status tomo_end_iteration(tomo_projector* p) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(end_iteration(p));
+    CK(cudaStreamSynchronize(p->stream));
+    return TOMO_OK;
+}
+
+static tomo_status get_slot(tomo_projector* p, const float* base, int32_t k, float* out, bool need) {
+    if (!p || !out) return fail(TOMO_ERR_INVALID, "null argument");
+    if (!need) return fail(TOMO_ERR_STATE, "nothing projected for the current projections");
+    if (k < 0 || k >= (int)p->batch.size()) return fail(TOMO_ERR_INVALID, "projection slot out of range");
+    CK(cudaMemcpyAsync(out, base + (size_t)k * p->npix, sizeof(float) * p->npix, cudaMemcpyDeviceToHost,
+                       p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return TOMO_OK;
+}
+
+tomo_status tomo_get_projection(tomo_projector* p, int32_t k, float* out_host) {
+    return get_slot(p, p ? p->d_proj : nullptr, k, out_host, p && p->projected);
+}
+tomo_status tomo_get_norm(tomo_projector* p, int32_t k, float* out_host) {
+    return get_slot(p, p ? p->d_norm : nullptr, k, out_host, p && p->projected);
+}
+tomo_status tomo_get_difference(tomo_projector* p, int32_t k, float* out_host) {
+    return get_slot(p, p ? p->d_diff : nullptr, k, out_host, p && p->diffs_valid);
+}
+
+tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, const double* tilt_axes) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (kind < TOMO_WEIGHT_NONE || kind > TOMO_WEIGHT_HAMMING_RAMP) return fail(TOMO_ERR_INVALID, "unknown filter");
+    if (kind == TOMO_WEIGHT_NONE) {
+        p->weight_kind = kind;
+        return TOMO_OK;
+    }
+    if (!p->series_loaded) return fail(TOMO_ERR_STATE, "load the tilt-series before setting the weighting");
+    const Geometry& g = p->g;
+    if (tilt_axes)
+        for (int t = 0; t < g.N; t++)
+            if (tilt_axes[t] != 0.0)
+                return fail(TOMO_ERR_UNSUPPORTED, "weighting with a non-zero tilt-axis angle needs a 2-D filter");
+    if ((g.w & (g.w - 1)) != 0) return fail(TOMO_ERR_UNSUPPORTED, "weighting needs a power-of-two width");
+    if (kind == TOMO_WEIGHT_RADERMACHER && !(radius > 0))
+        return fail(TOMO_ERR_INVALID, "Radermacher weighting needs a positive radius");
+    std::vector<double> sint(g.N), deg(g.N);
+    for (int t = 0; t < g.N; t++) {
+        sint[t] = p->euler[9 * t + 6];  // eulerAngles2Matrix row 2 = (sin(theta) cos(phi), ., .)
+        deg[t] = std::atan2(p->euler[9 * t + 6], p->euler[9 * t + 8]) * (180.0 / M_PI);
+    }
+    std::vector<float> mask(g.w);
+    weighting_row_filter(kind, g.w, g.N, sint.data(), deg.data(), radius * g.w, mask.data());
+    std::vector<float2> tw(g.w);
+    for (int k = 0; k < g.w; k++) {
+        const double a = -2.0 * M_PI * k / g.w;
+        tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    CK(cudaMemcpyAsync(p->d_mask, mask.data(), sizeof(float) * g.w, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_tw, tw.data(), sizeof(float2) * g.w, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->weight_kind = kind;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int32_t iterations) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (iterations < 0) return fail(TOMO_ERR_INVALID, "negative iteration count");
+    if (iterations > 0 && !p->d_tv_u) {
+        CKS(alloc_n(p, &p->d_tv_u, p->nvox));
+        CKS(alloc_n(p, &p->d_px, p->nvox));
+        CKS(alloc_n(p, &p->d_py, p->nvox));
+        CKS(alloc_n(p, &p->d_pz, p->nvox));
+    }
+    p->tv_theta = theta;
+    p->tv_g = g;
+    p->tv_dt = dt;
+    p->tv_iters = iterations;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_fista(tomo_projector* p, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (enabled && !p->d_prev) CKS(alloc_n(p, &p->d_prev, p->nvox));
+    p->fista = enabled != 0;
+    p->fista_t = 0.0;
+    return TOMO_OK;
+}
+
+tomo_status tomo_cancel(tomo_projector* p) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    p->cancel = 1;
+    return TOMO_OK;
+}
+
+int32_t tomo_first_index(uint64_t seed, int32_t iteration, int32_t nproj) {
+    return first_index(seed, iteration, nproj);
+}
+
+tomo_status tomo_order(tomo_projector* p, int32_t first, int32_t* order_out) {
+    if (!p || !order_out) return fail(TOMO_ERR_INVALID, "null argument");
+    if (!p->series_loaded) return fail(TOMO_ERR_STATE, "no tilt-series loaded");
+    if (first < 0 || first >= p->g.N) return fail(TOMO_ERR_INVALID, "first index out of range");
+    order_shuffle(p->g.N, p->euler.data(), first, order_out);
+    return TOMO_OK;
+}
+
+tomo_status tomo_order_shuffle(int32_t nproj, const double* euler, int32_t first, int32_t* order_out) {
+    if (!euler || !order_out || nproj <= 0) return fail(TOMO_ERR_INVALID, "null argument or empty series");
+    if (first < 0 || first >= nproj) return fail(TOMO_ERR_INVALID, "first index out of range");
+    order_shuffle(nproj, euler, first, order_out);
+    return TOMO_OK;
+}
+
+tomo_status tomo_run_wbp(tomo_projector* p, int32_t y0, int32_t y1) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(need_series(p));
+    const int N = p->g.N;
+    std::vector<int> all(N);
+    for (int t = 0; t < N; t++) all[t] = t;
+    CK(cudaMemcpyAsync(p->d_batch, all.data(), sizeof(int) * N, cudaMemcpyHostToDevice, p->stream));
+    CK(launch_gather(p->d_obatch, p->d_meas, p->d_batch, N, p->npix, p->stream));
+    CKS(apply_weighting(p, p->d_obatch, N));
+    CKS(run_bp(p, p->d_obatch, p->d_batch, N, y0, y1, p->meas_has_nan || p->meas_has_inf));
+    CKS(check_status(p));
+    p->batch.clear();
+    p->batch_uploaded = false;
+    p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int32_t update, uint64_t seed,
+                            int32_t y0, int32_t y1, int32_t use_graph, double* err_out) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    CKS(need_series(p));
+    if (n_iter < 0 || update < 0) return fail(TOMO_ERR_INVALID, "negative iteration count or update size");
+    const Geometry& g = p->g;
+    const int N = g.N;
+    const int upd = (update == 0) ? N : std::min(update, N);
+    const double factor = (double)(float)(relax / upd);  // float factorimg (TomoReconstruction2.java:646)
+    if (p->orders_cap < n_iter) {
+        if (p->d_orders) {
+            cudaFree(p->d_orders);
+            for (auto& a : p->allocs)
+                if (a == p->d_orders) a = nullptr;
+            g_in_use -= sizeof(int) * (size_t)p->orders_cap * N;
+            p->bytes -= sizeof(int) * (size_t)p->orders_cap * N;
+            p->d_orders = nullptr;
+        }
+        CKS(alloc_n(p, &p->d_orders, (size_t)std::max(n_iter, 1) * N));
+        p->orders_cap = std::max(n_iter, 1);
+    }
+    std::vector<int> orders((size_t)n_iter * N);
+    for (int it = 0; it < n_iter; it++)
+        order_shuffle(N, p->euler.data(), first_index(seed, it, N), &orders[(size_t)it * N]);
+    if (n_iter > 0)
+        CK(cudaMemcpyAsync(p->d_orders, orders.data(), sizeof(int) * orders.size(), cudaMemcpyHostToDevice,
+                           p->stream));
+    std::vector<double> errs((size_t)N);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto body = [&](const int* d_ord) -> tomo_status {
+        CKS(start_iteration(p));
+        for (int s = 0; s < N; s += upd) {
+            const int T = std::min(upd, N - s);
+            CKS(run_fp(p, d_ord + s, T, y0, true, factor, s));
+            CKS(run_bp(p, p->d_diff + (size_t)s * p->npix, d_ord + s, T, y0, y1, p->meas_has_inf));
+        }
+        CKS(end_iteration(p));
+        return TOMO_OK;
+    };
+    int* d_cur = p->d_batch;  // the graph reads the iteration's order from here
+    tomo_status result = TOMO_OK;
+    for (int it = 0; it < n_iter && result == TOMO_OK; it++) {
+        if (p->cancel.exchange(0)) {
+            result = fail(TOMO_ERR_CANCELLED, "cancelled");
+            break;
+        }
+        CK(cudaMemcpyAsync(d_cur, p->d_orders + (size_t)it * N, sizeof(int) * N, cudaMemcpyDeviceToDevice,
+                           p->stream));
+        if (use_graph && !p->fista) {
+            if (!exec) {
+                CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+                tomo_status bs = body(d_cur);
+                cudaError_t ce = cudaStreamEndCapture(p->stream, &graph);
+                if (bs != TOMO_OK) return bs;
+                CK(ce);
+                CK(cudaGraphInstantiate(&exec, graph, 0));
+            }
+            CK(cudaGraphLaunch(exec, p->stream));
+        } else {
+            CKS(body(d_cur));
+        }
+        CK(cudaMemcpyAsync(errs.data(), p->d_err, sizeof(double) * N, cudaMemcpyDeviceToHost, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        if (err_out) {
+            // osartIteration's error summary (TomoReconstruction2.java:692-730), including its
+            // else-if: a new maximum is never also tested as a minimum.
+            const int* ord = &orders[(size_t)it * N];
+            double som = 0, errmin = 3.4028234663852886e38, errmax = 0;
+            int imin = 0, imax = 0;
+            for (int t = 0; t < N; t++) {
+                const double e = errs[t];
+                som += e;
+                if (e > errmax) {
+                    errmax = e;
+                    imax = ord[t];
+                } else if (e < errmin) {
+                    errmin = e;
+                    imin = ord[t];
+                }
+            }
+            double* o = err_out + 5 * (size_t)it;
+            o[0] = std::sqrt(som / (double)((long long)N * g.W * g.H));
+            o[1] = std::sqrt(errmin / (double)(g.W * g.H));
+            o[2] = imin;
+            o[3] = std::sqrt(errmax / (double)(g.W * g.H));
+            o[4] = imax;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (result != TOMO_OK) return result;
+    CKS(check_status(p));
+    p->batch.clear();
+    p->batch_uploaded = false;
+    p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+// Internal declarations of the GB300 projection / backprojection engine.
+//
+// Geometry convention ("separable" fast path): with the tilt axis vertical
+// (AffineAlignment keeps tiltAxisVertical = true, AffineAlignment.java:18, 389-395)
+// every Euler matrix is [[c,0,-s],[0,1,0],[s,0,c]], so projection row j only
+// sees volume row r = j - (pc1 - vc1) and the forward projector and
+// backprojector work on independent XZ planes.  Positions along a plane are
+// kept in 32.32 fixed point so that interpolation weights match the
+// reference's double-precision geometry to ~1e-7 pixel; which samples are
+// inside the volume / projection is decided on the host with the reference's
+// exact double arithmetic and shipped as per-ray / per-column z intervals.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace tomo {
+
+constexpr double kFix = 4294967296.0;  // 2^32: fixed-point scale of positions
+
+// One forward-projection ray (tilt t, detector column i).  The ray is inside
+// the volume for z in [za, za + cnt); x(z) = X0 + z * step in 32.32 fixed point.
+struct alignas(16) FpRay {
+    int32_t zab;    // za | cnt << 16 (cnt = 0: the ray misses the volume)
+    float norm;     // exact float ray length the reference accumulates (VoxelProjector3D.java:774-783)
+    long long X0;   // fixed-point x at z = 0
+};
+
+struct alignas(16) FpTilt {
+    long long step;  // fixed-point dirX
+    double ninc;     // normIncrement
+};
+
+// Backprojection of tilt t: xx(x, z) = K + x * C + z * S (fixed point, volume
+// indices x, z); voxels of column x are inside the projection for z in
+// [zlo, zlo + cnt) (per-column table).
+struct alignas(8) BpTilt {
+    long long K, C, S;
+};
+
+// Per-handle geometry constants (host-computed).
+struct Geometry {
+    int W, H, D, w, h, N;
+    double vc[3], pc[4], scale;
+    bool separable;  // all tilts have the vertical-axis form, scale 1, integral row offsets
+    int fp_row_off;  // r = j - fp_row_off for the forward projector
+    int bp_row_off;  // j = r + bp_row_off for the backprojector
+};
+
+// Host-side table builders (geometry.cpp).  Return false if the tilt is not separable.
+bool tilt_is_separable(const double* R, const Geometry& g);
+void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays /* w entries */);
+void build_bp_tables(const Geometry& g, const double* R, BpTilt* tilt, int32_t* zint /* W entries */);
+void order_shuffle(int n, const double* euler, int first, int* out);
+int first_index(uint64_t seed, int iteration, int nproj);
+void weighting_row_filter(int kind, int w, int nproj, const double* sint, const double* tilts_deg, double diameter,
+                          float* mask_row);
+
+// Device kernels (launch wrappers in the .cu files).  All return cudaError_t of the launch.
+struct FpLaunch {
+    const float* vol;       // [D][H][W]
+    const float* meas;      // aligned measured [N][h][w] (nullptr: projection only)
+    const int* tilts;       // batch tilt indices [T]
+    int T;                  // projections in the batch
+    const FpTilt* ftilt;    // [N]
+    const FpRay* rays;      // [N][w]
+    float* proj;            // [T][h][w]
+    float* norm;            // [T][h][w]
+    float* diff;            // [T][h][w] (written when meas != nullptr)
+    double* errpart;        // [T][h] per-row sum of squared differences
+    double factor;          // relaxation factor passed to projectAndDifference
+    int j0, j1;             // projection rows to compute
+    int tilts_per_cta;
+    int W, H, D, w, h;
+    int row_off;
+    int* status;            // device error word
+};
+cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s);
+
+struct BpLaunch {
+    float* vol;
+    const float* img;       // [T][h][w] images to backproject, batch order
+    const int* tilts;       // [T] tilt index of each image (for geometry)
+    int T;
+    const BpTilt* btilt;    // [N]
+    const int32_t* zint;    // [N][W]
+    int y0, y1;             // volume rows
+    int W, H, D, w, h;
+    int row_off;
+    int positivity;
+    int sanitize;           // apply NaN/Inf checks of the reference (images may be non-finite)
+    int* status;
+};
+cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
+
+cudaError_t launch_align(const float* raw, float* out, const double* tinv /*[N][6]*/, const double* stats, int N,
+                         int w, int h, int normalize, int fill, const unsigned char* identity, cudaStream_t s);
+cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2* tw, int rows, int w, cudaStream_t s);
+cudaError_t launch_diff(const float* meas, const int* tilts, const float* th, const float* norm, float* diff,
+                        double* errpart, int T, int w, int h, int j0, int j1, double factor, cudaStream_t s);
+cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s);
+cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s);
+int fp_max_tilts_per_cta(int w);
+cudaError_t fp_init_attributes();
+cudaError_t misc_init_attributes();
+cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s);
+cudaError_t launch_tv_p(const float* u, float* px, float* py, float* pz, int W, int H, int D, float theta, float g,
+                        float dt, cudaStream_t s);
+cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* py, const float* pz, int W, int H,
+                        int D, float theta, cudaStream_t s);
+cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s);
+cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s);
+cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s);
+
+// Counts kernels launched by this library (tomo_kernel_launches).
+void count_launch(int n = 1);
+
+}  // namespace tomo

@@ -1,0 +1,207 @@
+"""GB300 drop-in for TomoJ's Projector plug-in surface.
+
+Mirrors Projector (TomoJ_Base/.../projectors/Projector.java:14-159) and the
+VoxelProjector3D setters (VoxelProjector3D.java:69-104) with the same method
+names and argument meanings; every call goes through the C ABI of
+libtomoj_gb300.so (include/tomoj_gb300.h).  The volume and the tilt-series stay
+resident in HBM; `rec` is updated in place on the device and read back with
+TomoReconstruction2.getVolume().
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import check
+
+
+class Projector:
+    """Abstract projector surface (Projector.java:130-156)."""
+
+    def addProjection(self, index: int) -> None:
+        raise NotImplementedError
+
+    def clearAllProjections(self) -> None:
+        raise NotImplementedError
+
+    def project(self, startY: int = 0, endY: int | None = None) -> None:
+        raise NotImplementedError
+
+    def projectAndDifference(self, factor: float, startY: int = 0, endY: int | None = None) -> np.ndarray:
+        raise NotImplementedError
+
+    def backproject(self, startY: int = 0, endY: int | None = None) -> None:
+        raise NotImplementedError
+
+    def startOfIteration(self) -> None:
+        raise NotImplementedError
+
+    def endOfIteration(self) -> None:
+        raise NotImplementedError
+
+    def getProjection(self, index: int) -> np.ndarray:
+        raise NotImplementedError
+
+
+class VoxelProjector3D(Projector):
+    """Ray-driven forward projector / voxel-driven backprojector on the GPU.
+
+    Construction captures dimensions and centres from the tilt-series and the
+    reconstruction (Projector.java:30-40); the tilt-series (aligned by the
+    series' AffineAlignment, TiltSeries.getPixels) is uploaded once.
+    `weighting` is None or a (kind, radius) pair (WBP filter)."""
+
+    def __init__(self, ts, rec, weighting=None, positivity=False, long_object=False, scale=None):
+        self.ts = ts
+        self.rec = rec
+        lib = _abi.load()
+        W, H, D = rec.getWidth(), rec.getHeight(), rec.getSizez()
+        w, h, n = ts.getWidth(), ts.getHeight(), ts.getImageStackSize()
+        if scale is None:
+            scale = w / float(W)  # ReconstructionParameters.rescaleData (ReconstructionParameters.java:328)
+        self._geom = _abi.make_geom(W, H, D, w, h, n, vol_center=rec.centers(),
+                                    proj_center=(ts.getCenterX(), ts.getCenterY(), ts.getProjectionCenterX(),
+                                                 ts.getProjectionCenterY()), scale=scale)
+        self._params = _abi.make_params(positivity=positivity, long_object=long_object, fill=ts.getFillType(),
+                                        normalize=ts.isNormalized())
+        h_ = C.c_void_p()
+        check(lib.tomo_create(C.byref(self._geom), C.byref(self._params), C.byref(h_)))
+        self._h = h_
+        self._lib = lib
+        self._n_added = 0
+        self.weighting = None
+        self._upload_series()
+        rec._attach(self)
+        if weighting is not None:
+            self.setWeighting(*weighting)
+
+    # --- lifetime --------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self.rec._detach(self)
+            self._lib.tomo_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _upload_series(self):
+        ts = self.ts
+        eul = np.ascontiguousarray(ts.eulers(), np.float64)
+        T = np.ascontiguousarray(ts.transforms(), np.float64)
+        need_stats = ts.isNormalized() or ts.getFillType() == _abi.FILL_AVG
+        stats = np.ascontiguousarray(ts.statistics(), np.float64) if need_stats else None
+        pix = np.ascontiguousarray(ts.pixels, np.float32)
+        check(self._lib.tomo_load_series(self._h, pix.ctypes.data, 0, _abi.ptr(eul, C.c_double),
+                                         _abi.ptr(T, C.c_double),
+                                         None if stats is None else _abi.ptr(stats, C.c_double)))
+
+    # --- setters (VoxelProjector3D.java:78-104) ----------------------------------------
+    def setWeighting(self, kind: int, radius: float = 0.0):
+        check(self._lib.tomo_set_weighting(self._h, int(kind), float(radius), None))
+        self.weighting = (kind, radius)
+
+    def isWeighting(self) -> bool:
+        return self.weighting is not None and self.weighting[0] != _abi.WEIGHT_NONE
+
+    def setTVM(self, theta=25.0, g=1.0, dt=0.1, iterations=5):
+        check(self._lib.tomo_set_tvm(self._h, theta, g, dt, int(iterations)))
+
+    def setFista(self, enabled: bool):
+        check(self._lib.tomo_set_fista(self._h, int(bool(enabled))))
+
+    # --- Projector surface --------------------------------------------------------------
+    def _rows(self, startY, endY):
+        return int(startY), int(self.rec.getHeight() if endY is None else endY)
+
+    def addProjection(self, index: int) -> None:
+        check(self._lib.tomo_add_projection(self._h, int(index)))
+        self._n_added += 1
+
+    def clearAllProjections(self) -> None:
+        check(self._lib.tomo_clear_projections(self._h))
+        self._n_added = 0
+
+    def project(self, startY: int = 0, endY: int | None = None) -> None:
+        y0, y1 = self._rows(startY, endY)
+        check(self._lib.tomo_project(self._h, y0, y1))
+
+    def projectAndDifference(self, factor: float, startY: int = 0, endY: int | None = None) -> np.ndarray:
+        y0, y1 = self._rows(startY, endY)
+        n = self._lib.tomo_projection_count(self._h)
+        err = np.zeros(max(n, 1), np.float64)
+        check(self._lib.tomo_project_and_difference(self._h, float(factor), y0, y1, _abi.ptr(err, C.c_double)))
+        return err[:n]
+
+    def backproject(self, startY: int = 0, endY: int | None = None) -> None:
+        y0, y1 = self._rows(startY, endY)
+        check(self._lib.tomo_backproject(self._h, y0, y1))
+
+    def startOfIteration(self) -> None:
+        check(self._lib.tomo_start_iteration(self._h))
+
+    def endOfIteration(self) -> None:
+        check(self._lib.tomo_end_iteration(self._h))
+
+    def _slot(self, fn, index):
+        out = np.empty((self.ts.getHeight(), self.ts.getWidth()), np.float32)
+        check(fn(self._h, int(index), _abi.ptr(out)))
+        return out
+
+    def getProjection(self, index: int) -> np.ndarray:
+        return self._slot(self._lib.tomo_get_projection, index)
+
+    def getNormImage(self, index: int) -> np.ndarray:
+        return self._slot(self._lib.tomo_get_norm, index)
+
+    def getDifferenceImage(self, index: int) -> np.ndarray:
+        return self._slot(self._lib.tomo_get_difference, index)
+
+    def getAlignedProjection(self, index: int) -> np.ndarray:
+        """TiltSeries.getPixels(index) as resident on the device."""
+        return self._slot(self._lib.tomo_get_aligned, index)
+
+    # --- device drivers ---------------------------------------------------------------------
+    def run_wbp(self, startY=0, endY=None):
+        y0, y1 = self._rows(startY, endY)
+        check(self._lib.tomo_run_wbp(self._h, y0, y1))
+
+    def run_ossart(self, n_iter, relax, update, seed=0, startY=0, endY=None, use_graph=True):
+        y0, y1 = self._rows(startY, endY)
+        err = np.zeros((max(n_iter, 1), 5), np.float64)
+        check(self._lib.tomo_run_ossart(self._h, int(n_iter), float(relax), int(update), int(seed), y0, y1,
+                                        int(bool(use_graph)), _abi.ptr(err, C.c_double)))
+        return err[:n_iter]
+
+    def order(self, first: int) -> np.ndarray:
+        out = np.zeros(self.ts.getImageStackSize(), np.int32)
+        check(self._lib.tomo_order(self._h, int(first), _abi.ptr(out, C.c_int32)))
+        return out
+
+    def cancel(self):
+        check(self._lib.tomo_cancel(self._h))
+
+    # volume plumbing used by TomoReconstruction2
+    def _set_volume(self, vol: np.ndarray):
+        vol = np.ascontiguousarray(vol, np.float32)
+        check(self._lib.tomo_set_volume(self._h, vol.ctypes.data, 0, 0, vol.shape[1]))
+
+    def _get_volume(self) -> np.ndarray:
+        D, H, W = self.rec.getSizez(), self.rec.getHeight(), self.rec.getWidth()
+        out = np.empty((D, H, W), np.float32)
+        check(self._lib.tomo_get_volume(self._h, out.ctypes.data, 0, 0, H))
+        return out
+
+
+def first_index(seed: int, iteration: int, nproj: int) -> int:
+    """Deterministic replacement of orderShuffleART's Math.random() first index."""
+    return int(_abi.load().tomo_first_index(int(seed), int(iteration), int(nproj)))

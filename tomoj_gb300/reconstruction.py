@@ -1,0 +1,226 @@
+"""Host-side mirror of TomoReconstruction2's drivers and the parameter factories.
+
+TomoReconstruction2 (TomoJ_Base/.../tomography/TomoReconstruction2.java) is the
+volume container plus the WBP / OSSART / regularization iteration drivers;
+ReconstructionParameters (ReconstructionParameters.java:279-333) and
+AdvancedReconstructionParameters (AdvancedReconstructionParameters.java:112-221)
+build the projector for a method.  Same names and argument meanings; the
+drivers run device-resident through the C ABI (one graph-captured launch
+sequence per iteration) when the projector is the GB300 VoxelProjector3D, and
+through the plain Projector surface otherwise.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _abi
+from .projector import Projector, VoxelProjector3D, first_index
+
+BP, WBP, OSSART, TVM = 0, 1, 2, 10
+
+
+class TomoReconstruction2:
+    """Reconstruction volume float32 (D, H, W) with TomoJ's centre convention."""
+
+    def __init__(self, width: int, height: int, depth: int, data: np.ndarray | None = None):
+        self.W, self.H, self.D = int(width), int(height), int(depth)
+        self._host = np.zeros((self.D, self.H, self.W), np.float32) if data is None else \
+            np.ascontiguousarray(data, np.float32).reshape(self.D, self.H, self.W).copy()
+        self.centerx = (self.W - 1) / 2.0
+        self.centery = (self.H - 1) / 2.0
+        self.centerz = (self.D - 1) / 2.0
+        self._proj = None
+        self.completion = 0.0
+
+    # --- container ------------------------------------------------------------------
+    def getWidth(self):
+        return self.W
+
+    def getHeight(self):
+        return self.H
+
+    def getSizez(self):
+        return self.D
+
+    def centers(self):
+        return (self.centerx, self.centery, self.centerz)
+
+    def setCenter(self, cx, cy, cz):
+        self.centerx, self.centery, self.centerz = float(cx), float(cy), float(cz)
+
+    def _attach(self, projector):
+        self._proj = projector
+        projector._set_volume(self._host)
+
+    def _detach(self, projector):
+        if self._proj is projector:
+            self._host = projector._get_volume()
+            self._proj = None
+
+    def getVolume(self) -> np.ndarray:
+        if self._proj is not None:
+            self._host = self._proj._get_volume()
+        return self._host
+
+    def setVolume(self, data: np.ndarray):
+        self._host = np.ascontiguousarray(data, np.float32).reshape(self.D, self.H, self.W).copy()
+        if self._proj is not None:
+            self._proj._set_volume(self._host)
+
+    def interrupt(self):
+        self.completion = -1000
+        if self._proj is not None:
+            self._proj.cancel()
+
+    # --- drivers ----------------------------------------------------------------------
+    def WBP(self, ts, projector: Projector, params=None, startY=0, endY=None):
+        """WBP with update 0 (TomoReconstruction2.java:499-538)."""
+        endY = self.H if endY is None else endY
+        if isinstance(projector, VoxelProjector3D):
+            projector.run_wbp(startY, endY)
+            return
+        for i in range(ts.getImageStackSize()):
+            projector.addProjection(i)
+            projector.backproject(startY, endY)
+            projector.clearAllProjections()
+
+    def OSSART(self, ts, projector: Projector, params, startY=0, endY=None, seed=0, use_graph=True):
+        """OS-SART / SIRT / ART (TomoReconstruction2.java:548-634).  Returns the per-iteration
+        error rows [average, min, argmin, max, argmax]."""
+        endY = self.H if endY is None else endY
+        if isinstance(projector, VoxelProjector3D):
+            return projector.run_ossart(params.getNbIterations(), params.getRelaxationCoefficient(),
+                                        params.getUpdateNb(), seed, startY, endY, use_graph)
+        return self._ossart_surface(ts, projector, params, startY, endY, seed)
+
+    def regularization(self, ts, projector: Projector, params, startY=0, endY=None, seed=0, use_graph=True):
+        """TomoReconstruction2.regularization (TomoReconstruction2.java:783-878): the same
+        iteration with the projector's endOfIteration regularisation (TVM)."""
+        return self.OSSART(ts, projector, params, startY, endY, seed, use_graph)
+
+    def _ossart_surface(self, ts, projector, params, startY, endY, seed):
+        n = ts.getImageStackSize()
+        eul = ts.eulers()
+        upd = n if params.getUpdateNb() == 0 else params.getUpdateNb()
+        factor = float(np.float32(params.getRelaxationCoefficient() / upd))
+        out = []
+        for it in range(params.getNbIterations()):
+            projector.startOfIteration()
+            order = order_shuffle(eul, first_index(seed, it, n))
+            som, errmin, errmax, imin, imax = 0.0, float(np.finfo(np.float32).max), 0.0, 0, 0
+            batch = []
+            for t in range(n):
+                projector.addProjection(int(order[t]))
+                batch.append(int(order[t]))
+                if len(batch) == upd or t == n - 1:
+                    err = projector.projectAndDifference(factor, startY, endY)
+                    for e, v in enumerate(err):
+                        som += v
+                        if v > errmax:
+                            errmax, imax = v, order[t - len(err) + e + 1]
+                        elif v < errmin:
+                            errmin, imin = v, order[t - len(err) + e + 1]
+                    projector.backproject(startY, endY)
+                    projector.clearAllProjections()
+                    batch = []
+            projector.endOfIteration()
+            wh = self.W * self.H
+            out.append([np.sqrt(som / (n * wh)), np.sqrt(errmin / wh), imin, np.sqrt(errmax / wh), imax])
+        return np.array(out)
+
+
+def order_shuffle(eulers, first: int) -> np.ndarray:
+    """orderShuffleART with a given first index, through the engine's host code."""
+    import ctypes as C
+    e = np.ascontiguousarray(eulers, np.float64)
+    out = np.zeros(e.shape[0], np.int32)
+    _abi.check(_abi.load().tomo_order_shuffle(e.shape[0], _abi.ptr(e, C.c_double), int(first),
+                                              _abi.ptr(out, C.c_int32)))
+    return out
+
+
+class ReconstructionParameters:
+    """ReconstructionParameters (ReconstructionParameters.java:12-333)."""
+
+    def __init__(self, width, height, depth):
+        self.width, self.height, self.depth = width, height, depth
+        self.reconstructionType = OSSART
+        self.nbIterations = 0
+        self.relaxationCoefficient = 1.0
+        self.updateNb = 0
+        self.positivityConstraint = False
+        self.fista = False
+        self.weightingRadius = float("nan")
+        self.weightingType = _abi.WEIGHT_RADERMACHER
+        self.rescaleData = True
+        self.longObjectCompensation = False
+        # TVM (AdvancedReconstructionParameters)
+        self.tvmTheta, self.tvmG, self.tvmDt, self.tvmIterations = 25.0, 1.0, 0.1, 5
+        self.regularizationWeight = 0.1
+
+    @staticmethod
+    def createOSSARTParameters(width, height, depth, nbIterations, relaxationCoefficient, updateNb):
+        p = ReconstructionParameters(width, height, depth)
+        p.reconstructionType = OSSART
+        p.nbIterations = nbIterations
+        p.relaxationCoefficient = relaxationCoefficient
+        p.updateNb = updateNb
+        return p
+
+    @staticmethod
+    def createWBPParameters(width, height, depth, weightingRadius, weightingType=_abi.WEIGHT_RADERMACHER):
+        p = ReconstructionParameters(width, height, depth)
+        radial = weightingType == _abi.WEIGHT_RADERMACHER
+        p.reconstructionType = BP if (radial and (np.isnan(weightingRadius) or weightingRadius <= 0)) else WBP
+        p.weightingRadius = weightingRadius
+        p.weightingType = weightingType
+        p.updateNb = 0
+        p.nbIterations = 0
+        p.relaxationCoefficient = float("nan")
+        return p
+
+    @staticmethod
+    def createTVMParameters(width, height, depth, nbIterations, relaxationCoefficient, tvmTheta, tvmG, tvmDt,
+                            tvmIterations):
+        """AdvancedReconstructionParameters.createTVMParameters (AdvancedReconstructionParameters.java:122-134).
+        TVMProjector3D.endOfIteration uses the regularisation weight (lambda) as dt
+        (TVMProjector3D.java:152); pass lambda as tvmDt."""
+        p = ReconstructionParameters(width, height, depth)
+        p.reconstructionType = TVM
+        p.nbIterations = nbIterations
+        p.relaxationCoefficient = relaxationCoefficient
+        p.tvmTheta, p.tvmG, p.tvmDt, p.tvmIterations = tvmTheta, tvmG, tvmDt, tvmIterations
+        p.updateNb = 0
+        return p
+
+    def getNbIterations(self):
+        return self.nbIterations
+
+    def getRelaxationCoefficient(self):
+        return self.relaxationCoefficient
+
+    def getUpdateNb(self):
+        return self.updateNb
+
+    def setPositivityConstraint(self, v):
+        self.positivityConstraint = bool(v)
+
+    def setFista(self, v):
+        self.fista = bool(v)
+
+    def setLongObjectCompensation(self, v):
+        self.longObjectCompensation = bool(v)
+
+    def getProjector(self, ts, rec) -> VoxelProjector3D:
+        """ReconstructionParameters.getProjector (ReconstructionParameters.java:313-333)."""
+        scale = ts.getWidth() / float(rec.getWidth()) if self.rescaleData else 1.0
+        pos = self.positivityConstraint if self.reconstructionType in (OSSART, TVM) else False
+        proj = VoxelProjector3D(ts, rec, None, positivity=pos, long_object=self.longObjectCompensation, scale=scale)
+        if self.reconstructionType == WBP:
+            proj.setWeighting(self.weightingType, self.weightingRadius if self.weightingRadius == self.weightingRadius
+                              else 0.0)
+        if self.reconstructionType == TVM:
+            proj.setTVM(self.tvmTheta, self.tvmG, self.tvmDt, self.tvmIterations)
+        if self.fista:
+            proj.setFista(True)
+        return proj
