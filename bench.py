@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark of the projection/backprojection hot path (one JSON line on rank 0).
+
+Workload (default "ossart512"): a 512 x 256 x 512 (W x H x D) float32 volume of
+60 seeded ellipsoids; 61 projections of 512 x 256 at -60..+60 deg with seeded
+per-tilt shifts U(-5,5) px and in-plane rotations U(-1,1) deg; one step is one
+whole reconstruction job on the resident tilt-series: Hamming-ramp WBP, then
+OS-SART with update 7 (9 subsets of 61 tilts) for 20 iterations.  The metric
+is voxel-updates/s: one update is one (voxel, tilt) pair of one pass, so a step
+is Nvox * Nproj * (1 + 20) updates.  Inputs are larger than L2 (the volume is
+268 MB), so no flush is needed between steps.
+
+Arms:
+  default            the GB300 engine through its C ABI (device-resident inputs)
+  --impl reference   the reference's CPU algorithm (C restatement, all host
+                     threads) on a bounded sample of the same workload
+Multi-GPU (torchrun): every rank reconstructs its own series (weak scaling, no
+collective on the data path); value = all ranks' updates / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "ossart512": dict(W=512, H=256, D=512, n=61, amax=60.0, ellipsoids=60, shifts=5.0, rot=1.0, noise=0.0,
+                      wbp="hamming_ramp", n_iter=20, update=7, relax=1.0, seed=1235),
+    "sirt256": dict(W=256, H=64, D=256, n=61, amax=60.0, ellipsoids=20, shifts=0.0, rot=0.0, noise=0.01,
+                    wbp="ramp", n_iter=10, update=0, relax=1.0, seed=1234),
+}
+METRIC = "SIRT voxel-updates/s + served recon p50/p99 vs plain FP32 GPU, ≤1e-3 rel-L2"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ----------------------------------------------------------------------------- inputs
+def make_inputs(wl, project_fn):
+    from tomoj_gb300 import phantom as P
+    t0 = time.time()
+    vol = P.ellipsoid_phantom(wl["W"], wl["H"], wl["D"], wl["ellipsoids"], wl["seed"])
+    angles = np.linspace(-wl["amax"], wl["amax"], wl["n"])
+    ideal = project_fn(vol, angles)
+    n = wl["n"]
+    if wl["shifts"] or wl["rot"]:
+        T = P.misalignment(n, wl["seed"] + 1, wl["shifts"], wl["rot"])
+        series = np.array([P.unalign(ideal[i], T[i]) for i in range(n)], np.float32)
+    else:
+        T = np.tile(np.array([1.0, 0, 0, 1, 0, 0]), (n, 1))
+        series = ideal
+    if wl["noise"]:
+        series = P.add_gaussian_noise(series, wl["noise"], wl["seed"] + 2)
+    log(f"[bench] inputs ready in {time.time() - t0:.1f}s")
+    return vol, angles, np.ascontiguousarray(T), np.ascontiguousarray(series, np.float32)
+
+
+def euler_y(angles):
+    from tomoj_gb300.tiltseries import euler_angles_to_matrix
+    return np.ascontiguousarray([euler_angles_to_matrix(0.0, a, -0.0) for a in angles], np.float64)
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU arm
+def cpu_sample(wl, rows, threads, steps=1):
+    """Time the C restatement of the reference's CPU path on `rows` volume rows of the
+    workload (same W, D, tilts, subsets): one WBP pass + one OS-SART iteration per step.
+    Returns (updates/s, seconds, updates)."""
+    from oracle import oracle as O
+    from tomoj_gb300 import phantom as P
+    O.build()
+    O.set_threads(threads)
+    W, D, n = wl["W"], wl["D"], wl["n"]
+    H = rows
+    g = O.Geom(W, H, D, W, H)
+    vol = P.ellipsoid_phantom(W, H, D, max(4, wl["ellipsoids"] // 4), wl["seed"])
+    angles = np.linspace(-wl["amax"], wl["amax"], n)
+    eul = np.array([O.euler_tilt_y(a) for a in angles])
+    meas = np.nan_to_num(np.array([O.project(vol, g, e)[0] for e in eul], np.float32))
+    order = O.order_shuffle(eul, 0)
+    upd = wl["update"]
+    ups = W * H * D * n * 2
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        rec = np.zeros((D, H, W), np.float32)
+        O.wbp(rec, g, eul, meas, None)
+        O.ossart_iteration(rec, g, eul, meas, order, wl["relax"], upd)
+    dt = time.perf_counter() - t0
+    return ups * steps / dt, dt, ups * steps
+
+
+def cpu_rows_for(wl, threads, target_s):
+    """Rows of the workload whose CPU sample takes about target_s seconds."""
+    rate, dt, _ = cpu_sample(wl, 4, threads)
+    per_row = dt / 4
+    return int(max(4, min(wl["H"], round(target_s / max(per_row, 1e-6)))))
+
+
+def run_reference(args, wl):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rows = cpu_rows_for(wl, threads, args.cpu_seconds)
+    for _ in range(args.warmup):
+        cpu_sample(wl, max(4, rows // 4), threads)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        rate, dt, _ = cpu_sample(wl, rows, threads)
+        vals.append(rate)
+        secs += dt
+    value = float(np.mean(vals))
+    sample = (f"{wl['W']}x{rows}x{wl['D']} rows of the workload: 1 WBP pass + 1 OS-SART iteration "
+              f"(update {wl['update']}) per step, {wl['n']} tilts")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, **{k: wl[k] for k in ("W", "H", "D", "n", "n_iter", "update")},
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_engine(args, wl):
+    import torch
+    from tomoj_gb300 import _abi
+    from tomoj_gb300.build import build
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if rank == 0:
+        build()
+    if world > 1:
+        torch.distributed.barrier()
+    lib = _abi.load()
+    stream = torch.cuda.current_stream()
+    W, H, D, n = wl["W"], wl["H"], wl["D"], wl["n"]
+
+    def create(normalize=False):
+        g = _abi.make_geom(W, H, D, W, H, n)
+        p = _abi.make_params(fill=_abi.FILL_NAN, normalize=normalize)
+        h = C.c_void_p()
+        _abi.check(lib.tomo_create(C.byref(g), C.byref(p), C.byref(h)))
+        _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        return h
+
+    eul = euler_y(np.linspace(-wl["amax"], wl["amax"], n))
+
+    def project_fn(vol, angles):
+        h = create()
+        try:
+            zeros = np.zeros((n, H, W), np.float32)
+            _abi.check(lib.tomo_load_series(h, zeros.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+            v = np.ascontiguousarray(vol)
+            _abi.check(lib.tomo_set_volume(h, v.ctypes.data, 0, 0, H))
+            for i in range(n):
+                _abi.check(lib.tomo_add_projection(h, i))
+            _abi.check(lib.tomo_project(h, 0, H))
+            out = np.empty((n, H, W), np.float32)
+            for i in range(n):
+                _abi.check(lib.tomo_get_projection(h, i, _abi.ptr(out[i])))
+            return np.nan_to_num(out)
+        finally:
+            lib.tomo_destroy(h)
+
+    _, angles, T, series = make_inputs(wl, project_fn)
+    wkind = {"ramp": _abi.WEIGHT_RAMP, "hamming_ramp": _abi.WEIGHT_HAMMING_RAMP}[wl["wbp"]]
+
+    # per-tilt ROI statistics (TiltSeries.getImageStatistics) for the FILL_AVG of the WBP pass
+    from tomoj_gb300.tiltseries import TiltSeries
+    ts = TiltSeries(series, angles)
+    for i in range(n):
+        ts.getAlignment().setTransform(i, T[i])
+    ts.getAlignment().setCombineTransforms(False)
+    stats = np.ascontiguousarray(ts.statistics(), np.float64)
+
+    h = create()
+
+    def load(pixels):
+        _abi.check(lib.tomo_load_series(h, pixels.ctypes.data, 0, _abi.ptr(eul, C.c_double),
+                                        _abi.ptr(T, C.c_double), _abi.ptr(stats, C.c_double)))
+        _abi.check(lib.tomo_set_weighting(h, wkind, 0.0, None))
+
+    load(series)
+    nvox = W * H * D
+    updates_per_step = nvox * n * (1 + wl["n_iter"])
+
+    def step(errs=None):
+        # WBP on FILL_AVG projections, then OS-SART on FILL_NAN projections, as the
+        # reference's WBP and iterative applications set them
+        _abi.check(lib.tomo_fill_volume(h, 0.0))
+        _abi.check(lib.tomo_set_fill(h, _abi.FILL_AVG))
+        _abi.check(lib.tomo_run_wbp(h, 0, H))
+        _abi.check(lib.tomo_set_fill(h, _abi.FILL_NAN))
+        _abi.check(lib.tomo_run_ossart(h, wl["n_iter"], wl["relax"], wl["update"], wl["seed"], 0, H, 1,
+                                       None if errs is None else _abi.ptr(errs, C.c_double)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    # ---- timed region: device-resident inputs ----
+    _abi.check(lib.tomo_set_profiling(h, 1))
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.tomo_kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    errs = np.zeros((wl["n_iter"], 5))
+    for _ in range(args.steps):
+        step(errs)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.tomo_kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    prof = np.zeros(4)
+    _abi.check(lib.tomo_profile_read(h, _abi.ptr(prof, C.c_double)))
+    _abi.check(lib.tomo_set_profiling(h, 0))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = updates_per_step * args.steps * world / (ms / 1000.0)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    series_pin = torch.empty(series.shape, dtype=torch.float32, pin_memory=True).numpy()
+    series_pin[...] = series
+    vol_pin = torch.empty((D, H, W), dtype=torch.float32, pin_memory=True).numpy()
+    h2d = series_pin.nbytes + eul.nbytes + T.nbytes + stats.nbytes
+    d2h = vol_pin.nbytes
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        load(series_pin)
+        step()
+        _abi.check(lib.tomo_get_volume(h, vol_pin.ctypes.data, 0, 0, H))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = updates_per_step * e2e_steps * world / e2e_s
+
+    # ---- roofline of the dominant kernel ----
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = FALLBACK_HBM_GBS, "fallback"
+    fp_ms, fp_n, bp_ms, bp_n = prof
+    upd = n if wl["update"] == 0 else wl["update"]
+    nsub = (n + upd - 1) // upd
+    tilts_per_launch = n / nsub
+    npix = W * H
+    fp_bytes = 4 * nvox + tilts_per_launch * npix * 4 * 4       # volume read + meas read, proj/norm/diff writes
+    bp_bytes = 8 * nvox + tilts_per_launch * npix * 4           # volume read+write + difference read
+    kernels = {
+        "fp_separable": {"avg_ms": fp_ms / max(fp_n, 1), "bytes": fp_bytes, "launches": int(fp_n)},
+        "bp_separable": {"avg_ms": bp_ms / max(bp_n, 1), "bytes": bp_bytes, "launches": int(bp_n)},
+    }
+    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+    kd = kernels[dom]
+    achieved = kd["bytes"] / (kd["avg_ms"] / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_ossart512.json")
+    if os.path.exists(tpath) and args.workload == "ossart512":
+        traffic = json.load(open(tpath)).get(dom)
+    updates_per_launch = nvox * tilts_per_launch
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+        "algorithmic_bytes_per_launch": kd["bytes"], "avg_launch_ms": kd["avg_ms"],
+        "updates_per_launch": updates_per_launch,
+        "per_update_equiv_GBs": 12.0 * updates_per_launch / (kd["avg_ms"] / 1000.0) / 1e9,
+        "kernels": {k: {"avg_ms": v["avg_ms"], "launches": v["launches"],
+                        "GBs": v["bytes"] / (v["avg_ms"] / 1000.0) / 1e9} for k, v in kernels.items()},
+    }
+
+    # ---- CPU baseline (rank 0, N=1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rows = cpu_rows_for(wl, threads, args.cpu_seconds)
+        rate, dt, ups = cpu_sample(wl, rows, threads)
+        cpu = {"value": rate, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{W}x{rows}x{D} rows of the workload, 1 WBP pass + 1 OS-SART iteration, {dt:.1f} s"}
+
+    lib.tomo_destroy(h)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "W": W, "H": H, "D": D, "nproj": n, "proj": f"{W}x{H}",
+                       "wbp": wl["wbp"], "n_iter": wl["n_iter"], "update": wl["update"],
+                       "updates_per_step": updates_per_step, "l2": "inputs larger than L2 (volume 268 MB)",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+            "sirt_error_last_iteration": float(errs[-1, 0]),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="ossart512", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_engine(args, wl)
+
+
+if __name__ == "__main__":
+    main()

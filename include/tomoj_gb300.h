@@ -107,6 +107,10 @@ tomo_status tomo_set_stream(tomo_projector* p, void* stream);
  * `pixels` is a device pointer. */
 tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pixels_on_device, const double* euler,
                              const double* transforms, const double* stats);
+/* TiltSeries.setFillType: re-aligns the resident series with another fill policy
+ * (WBP uses FILL_AVG, iterative methods FILL_NAN; WBPReconstructionApplication.java:52,
+ * IterativeReconstructionApplication.java:196). */
+tomo_status tomo_set_fill(tomo_projector* p, int32_t fill);
 /* The aligned projection `index` as the projector sees it (host copy). */
 tomo_status tomo_get_aligned(tomo_projector* p, int32_t index, float* out_host);
 /* Volume rows [y0,y1) from/to a host or device buffer laid out [D][y1-y0][W]. */
@@ -163,6 +167,16 @@ tomo_status tomo_order(tomo_projector* p, int32_t first, int32_t* order_out);
 tomo_status tomo_order_shuffle(int32_t nproj, const double* euler, int32_t first, int32_t* order_out);
 /* Cooperative cancel, polled between updates (TomoReconstruction2.interrupt). */
 tomo_status tomo_cancel(tomo_projector* p);
+
+/* ---- measurement (no counterpart in the reference; Chrono-style timing) ----
+ * When enabled, tomo_run_ossart records CUDA events around every forward
+ * projection (+ residual reduction) and backprojection launch on the handle's
+ * stream; tomo_profile_read returns {fp_ms, fp_launches, bp_ms, bp_launches}
+ * accumulated since profiling was enabled. */
+tomo_status tomo_set_profiling(tomo_projector* p, int32_t enabled);
+tomo_status tomo_profile_read(tomo_projector* p, double* out4);
+/* Tilts per forward-projection CTA (0 = automatic; tuning knob). */
+tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n);
 
 #ifdef __cplusplus
 }

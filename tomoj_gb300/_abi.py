@@ -71,6 +71,7 @@ SIGNATURES = {
     "tomo_set_stream": (C.c_int32, [_P, C.c_void_p]),
     "tomo_load_series": (C.c_int32, [_P, C.c_void_p, C.c_int32, _f64p, _f64p, _f64p]),
     "tomo_get_aligned": (C.c_int32, [_P, C.c_int32, _f32p]),
+    "tomo_set_fill": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_volume": (C.c_int32, [_P, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "tomo_get_volume": (C.c_int32, [_P, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "tomo_fill_volume": (C.c_int32, [_P, C.c_float]),
@@ -96,6 +97,9 @@ SIGNATURES = {
     "tomo_order": (C.c_int32, [_P, C.c_int32, _i32p]),
     "tomo_order_shuffle": (C.c_int32, [C.c_int32, _f64p, C.c_int32, _i32p]),
     "tomo_cancel": (C.c_int32, [_P]),
+    "tomo_set_profiling": (C.c_int32, [_P, C.c_int32]),
+    "tomo_profile_read": (C.c_int32, [_P, _f64p]),
+    "tomo_set_tilts_per_cta": (C.c_int32, [_P, C.c_int32]),
 }
 
 

@@ -12,7 +12,7 @@
 #include "tomo_internal.h"
 
 namespace tomo {
-static std::atomic<uint64_t> g_launches{0};
+std::atomic<uint64_t> g_launches{0};
 void count_launch(int n) { g_launches += (uint64_t)n; }
 }  // namespace tomo
 
@@ -96,6 +96,11 @@ struct tomo_projector {
     double fista_t = 0.0;
     std::atomic<int> cancel{0};
     int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+    // per-kernel timing of the OS-SART driver (tomo_set_profiling)
+    bool profile = false;
+    std::vector<cudaEvent_t> ev;
+    double prof_ms[2] = {0, 0};  // forward projection (+ residual reduction), backprojection
+    long long prof_n[2] = {0, 0};
 };
 
 namespace {
@@ -399,6 +404,7 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
 tomo_status tomo_destroy(tomo_projector* p) {
     if (!p) return TOMO_OK;
     if (p->stream) cudaStreamSynchronize(p->stream);
+    for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
     for (void* a : p->allocs) cudaFree(a);
     g_in_use -= p->bytes;
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
@@ -480,6 +486,25 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
     p->batch.clear();
     p->batch_uploaded = false;
     p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_fill(tomo_projector* p, int32_t fill) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (fill < TOMO_FILL_NONE || fill > TOMO_FILL_NAN) return fail(TOMO_ERR_INVALID, "unknown fill type");
+    p->params.fill = fill;
+    if (!p->series_loaded) return TOMO_OK;
+    const Geometry& g = p->g;
+    CK(launch_align(p->d_raw, p->d_meas, p->d_tinv, p->d_stats, g.N, g.w, g.h, p->params.normalize, fill,
+                    p->d_identity, p->stream));
+    int flags = 0;
+    CK(cudaMemsetAsync(p->d_flags, 0, sizeof(int), p->stream));
+    CK(launch_scan_nonfinite(p->d_meas, (size_t)g.N * p->npix, p->d_flags, p->stream));
+    CK(cudaMemcpyAsync(&flags, p->d_flags, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->meas_has_nan = (flags & 1) != 0;
+    p->meas_has_inf = (flags & 2) != 0;
+    p->obatch_valid = false;
     return TOMO_OK;
 }
 
@@ -709,6 +734,29 @@ tomo_status tomo_set_fista(tomo_projector* p, int32_t enabled) {
     return TOMO_OK;
 }
 
+tomo_status tomo_set_profiling(tomo_projector* p, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    p->profile = enabled != 0;
+    p->prof_ms[0] = p->prof_ms[1] = 0;
+    p->prof_n[0] = p->prof_n[1] = 0;
+    return TOMO_OK;
+}
+
+tomo_status tomo_profile_read(tomo_projector* p, double* out4) {
+    if (!p || !out4) return fail(TOMO_ERR_INVALID, "null argument");
+    out4[0] = p->prof_ms[0];
+    out4[1] = (double)p->prof_n[0];
+    out4[2] = p->prof_ms[1];
+    out4[3] = (double)p->prof_n[1];
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n) {
+    if (!p || n < 0) return fail(TOMO_ERR_INVALID, "bad argument");
+    p->tilts_per_cta = n;
+    return TOMO_OK;
+}
+
 tomo_status tomo_cancel(tomo_projector* p) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
     p->cancel = 1;
@@ -781,16 +829,28 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
     std::vector<double> errs((size_t)N);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    const int nsub = (N + upd - 1) / upd;
+    if (p->profile && (int)p->ev.size() < 4 * nsub) {
+        while ((int)p->ev.size() < 4 * nsub) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            p->ev.push_back(e);
+        }
+    }
     auto body = [&](const int* d_ord) -> tomo_status {
         CKS(start_iteration(p));
-        for (int s = 0; s < N; s += upd) {
+        for (int s = 0, k = 0; s < N; s += upd, k++) {
             const int T = std::min(upd, N - s);
+            if (p->profile) CK(cudaEventRecordWithFlags(p->ev[4 * k + 0], p->stream, cudaEventRecordExternal));
             CKS(run_fp(p, d_ord + s, T, y0, true, factor, s));
+            if (p->profile) CK(cudaEventRecordWithFlags(p->ev[4 * k + 1], p->stream, cudaEventRecordExternal));
             CKS(run_bp(p, p->d_diff + (size_t)s * p->npix, d_ord + s, T, y0, y1, p->meas_has_inf));
+            if (p->profile) CK(cudaEventRecordWithFlags(p->ev[4 * k + 2], p->stream, cudaEventRecordExternal));
         }
         CKS(end_iteration(p));
         return TOMO_OK;
     };
+    uint64_t graph_kernels = 0;
     int* d_cur = p->d_batch;  // the graph reads the iteration's order from here
     tomo_status result = TOMO_OK;
     for (int it = 0; it < n_iter && result == TOMO_OK; it++) {
@@ -802,19 +862,35 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
                            p->stream));
         if (use_graph && !p->fista) {
             if (!exec) {
+                const uint64_t before = tomo::g_launches.load();
                 CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
                 tomo_status bs = body(d_cur);
                 cudaError_t ce = cudaStreamEndCapture(p->stream, &graph);
+                // kernels are counted when the graph runs, not when it is captured
+                graph_kernels = tomo::g_launches.load() - before;
+                tomo::g_launches -= graph_kernels;
                 if (bs != TOMO_OK) return bs;
                 CK(ce);
                 CK(cudaGraphInstantiate(&exec, graph, 0));
             }
             CK(cudaGraphLaunch(exec, p->stream));
+            tomo::count_launch((int)graph_kernels);
         } else {
             CKS(body(d_cur));
         }
         CK(cudaMemcpyAsync(errs.data(), p->d_err, sizeof(double) * N, cudaMemcpyDeviceToHost, p->stream));
         CK(cudaStreamSynchronize(p->stream));
+        if (p->profile) {
+            for (int k = 0; k < nsub; k++) {
+                float a = 0, b = 0;
+                CK(cudaEventElapsedTime(&a, p->ev[4 * k + 0], p->ev[4 * k + 1]));
+                CK(cudaEventElapsedTime(&b, p->ev[4 * k + 1], p->ev[4 * k + 2]));
+                p->prof_ms[0] += a;
+                p->prof_ms[1] += b;
+                p->prof_n[0]++;
+                p->prof_n[1]++;
+            }
+        }
         if (err_out) {
             // osartIteration's error summary (TomoReconstruction2.java:692-730), including its
             // else-if: a new maximum is never also tested as a minimum.

@@ -10,6 +10,7 @@
 // inside the volume / projection is decided on the host with the reference's
 // exact double arithmetic and shipped as per-ray / per-column z intervals.
 #pragma once
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 
@@ -115,5 +116,6 @@ cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s)
 
 // Counts kernels launched by this library (tomo_kernel_launches).
 void count_launch(int n = 1);
+extern std::atomic<uint64_t> g_launches;
 
 }  // namespace tomo
