@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libtomoj_gb300.so")
-SOURCES = ["tomo_abi.cu", "kernels_fp.cu", "kernels_bp.cu", "kernels_misc.cu", "geometry.cpp"]
+SOURCES = ["tomo_abi.cu", "kernels_fp.cu", "fp_kernel_q1.cu", "fp_kernel_q2.cu", "fp_kernel_q4.cu", "fp_kernel_q8.cu",
+           "fp_kernel_q16.cu", "kernels_bp.cu", "kernels_misc.cu", "geometry.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -45,18 +46,20 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile (if stale) and return the path of the shared library."""
-    if not force and not _stale():
+def build(force: bool = False, verbose: bool = False, out: str | None = None, defines=()) -> str:
+    """Compile (if stale) and return the path of the shared library.
+    `out` and `defines` (e.g. ["TOMO_BP_MIN_BLOCKS=2"]) build a tuning variant elsewhere."""
+    lib = out or LIB
+    if not force and out is None and not _stale():
         return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
-    obj_dir = os.path.join(OUT_DIR, "obj")
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
+    obj_dir = os.path.join(os.path.dirname(lib), "obj_" + os.path.basename(lib))
     os.makedirs(obj_dir, exist_ok=True)
     cc = nvcc()
 
     def compile_one(src: str) -> str:
         obj = os.path.join(obj_dir, src + ".o")
-        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + _flags(verbose)
+        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + _flags(verbose) + [f"-D{d}" for d in defines]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
@@ -66,13 +69,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["--cudart", "static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -66,6 +66,10 @@ __device__ __forceinline__ float fix_frac(uint32_t lo) {
     return __uint_as_float((lo >> 9) | 0x3F800000u) - 1.0f;
 }
 
+// 1 + fraction in [1,2) from the low 32 bits of a 32.32 fixed-point position; used with
+// (v - d, d) pairs: v + f d == fma(1 + f, d, v - d).
+__device__ __forceinline__ float fix_one_plus_frac(uint32_t lo) { return __uint_as_float((lo >> 9) | 0x3F800000u); }
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

@@ -1,0 +1,333 @@
+// Forward projection fused with the residual (separable geometry).
+//
+// Reference: VoxelProjector3D.projectJosephPartial + difference
+// (TomoJ_Base/.../projectors/VoxelProjector3D.java:671-821, 414-433) and the
+// sampler TomoReconstruction2.getPixel(double,double,int) (TomoReconstruction2.java:154-190).
+//
+// One CTA owns one projection row j (= volume row r = j - row_off) for a group
+// of TG tilts.  It walks the row's XZ plane in chunks of ZC planes: one thread
+// stages each chunk with bulk TMA copies (one per plane row, completing on an
+// mbarrier), all threads turn it into (v - d, d) pairs so that a bilinear
+// sample is one 64-bit shared load and one FMA, and every thread advances its
+// 16 rays (TG tilts x QP detector columns) through the chunk.  A ray position is
+// 32.32 fixed point whose per-plane step also carries the pair-row pitch, so its
+// integer part is directly the shared-memory pair index.  Ray sums accumulate in
+// FP32 along z (two interleaved sub-chains per chunk), matching the reference's
+// float ray_sum to rounding.  The epilogue writes proj/norm and, when the
+// aligned measurement is given, diff = (float)(((e - th) / norm) * factor) and
+// the per-row FP64 sum of squared differences.
+//
+// This header is compiled once per detector-column count per thread (QP) by the
+// fp_kernel_q*.cu translation units.
+#pragma once
+#include <cmath>
+
+#include "device_util.cuh"
+#include "tomo_internal.h"
+
+namespace tomo {
+namespace fpk {
+
+constexpr int kThreads = 256;
+constexpr uint32_t kWaitTries = 1u << 24;
+constexpr size_t kMaxSmem = 112 * 1024;  // two CTAs per SM
+
+struct Smem {
+    int PW;
+    size_t raw_off, pair_off, red_off, step_off, total;
+};
+
+// Shared memory: mbarrier | raw chunk [ZC][W] | pairs [ZC][W+4] | reduction scratch | steps.
+__host__ __device__ inline Smem layout(int ZC, int W, int tgmax) {
+    Smem L;
+    L.PW = W + 4;
+    size_t o = 16;
+    L.raw_off = o;
+    o += (size_t)ZC * W * sizeof(float);
+    o = (o + 15) & ~(size_t)15;
+    L.pair_off = o;
+    o += (size_t)ZC * L.PW * sizeof(float2);
+    o = (o + 15) & ~(size_t)15;
+    L.red_off = o;
+    o += (kThreads / 32) * sizeof(double);
+    L.step_off = o;
+    o += (size_t)tgmax * sizeof(long long);
+    L.total = o;
+    return L;
+}
+
+// Pairs of one plane row: slot k+2 holds the sample at floor(x) = k for k in [-2, W+1]
+// as (v_k - d_k, d_k), d_k = v_{k+1} - v_k, so that a bilinear sample with fraction f is
+// fma(1 + f, d_k, v_k - d_k).  d = 0 where the reference returns the raw floor voxel
+// (last column, last row, last plane) and outside [0, W-1].
+__device__ __forceinline__ void build_pairs_row(const float* __restrict__ src, float2* __restrict__ dst, int W,
+                                                bool flat) {
+    const int tid = threadIdx.x;
+    if ((W & 3) == 0) {
+        for (int m = tid; m < W / 4; m += kThreads) {
+            const float4 v = *reinterpret_cast<const float4*>(src + 4 * m);
+            const float nx = (4 * m + 4 < W) ? src[4 * m + 4] : v.w;
+            float d0 = v.y - v.x, d1 = v.z - v.y, d2 = v.w - v.z, d3 = nx - v.w;
+            if (flat) d0 = d1 = d2 = d3 = 0.0f;
+            float4* o = reinterpret_cast<float4*>(dst + 4 * m + 2);
+            o[0] = make_float4(v.x - d0, d0, v.y - d1, d1);
+            o[1] = make_float4(v.z - d2, d2, v.w - d3, d3);
+        }
+    } else {
+        for (int k = tid; k < W; k += kThreads) {
+            const float v = src[k];
+            float d = (k + 1 < W) ? src[k + 1] - v : 0.0f;
+            if (flat) d = 0.0f;
+            dst[k + 2] = make_float2(v - d, d);
+        }
+    }
+    if (tid < 4) {
+        const int k = (tid < 2) ? tid - 2 : W + tid - 2;  // -2, -1, W, W+1
+        const float v = src[(tid < 2) ? 0 : W - 1];
+        dst[k + 2] = make_float2(v, 0.0f);
+    }
+}
+
+__device__ __forceinline__ float sample(const float2* __restrict__ P, long long x) {
+    const float2 p = P[(int)(x >> 32)];
+    return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
+}
+
+template <int QP, int ZC>
+__global__ void __launch_bounds__(kThreads, 2) fp_kernel(FpLaunch a, int use_tma) {
+    constexpr int TGMAX = 16 / QP;
+    constexpr int NR = TGMAX * QP;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Smem L = layout(ZC, a.W, TGMAX);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+    float* raw = reinterpret_cast<float*>(smem + L.raw_off);
+    float2* pairs = reinterpret_cast<float2*>(smem + L.pair_off);
+    double* red = reinterpret_cast<double*>(smem + L.red_off);
+    long long* s_step = reinterpret_cast<long long*>(smem + L.step_off);
+
+    const int tid = threadIdx.x;
+    const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
+    const int PW = L.PW;
+    const int j = a.j0 + blockIdx.y;
+    const int g0 = blockIdx.x * a.tilts_per_cta;
+    const int TG = min(a.tilts_per_cta, a.T - g0);
+    const int r = j - a.row_off;
+    const bool row_in = (r >= 0 && r < H);
+
+    // ray k = t * QP + q: tilt g0 + t, detector column tid + q * kThreads
+    long long X[NR];
+    float acc[NR];
+    int zab[NR];
+#pragma unroll
+    for (int k = 0; k < NR; k++) {
+        const int t = k / QP, q = k % QP;
+        const int i = tid + q * kThreads;
+        acc[k] = 0.0f;
+        X[k] = 0;
+        zab[k] = 0;
+        if (t < TG) {
+            const int tilt = a.tilts[g0 + t];
+            if (tid == 0 && q == 0) s_step[t] = a.ftilt[tilt].step;
+            if (i < w && row_in) {
+                const FpRay ray = a.rays[(size_t)tilt * w + i];
+                X[k] = ray.X0;
+                zab[k] = ray.zab;
+            }
+        } else if (tid == 0 && q == 0) {
+            s_step[t] = 0;
+        }
+    }
+
+    if (row_in) {
+        const int nchunks = (D + ZC - 1) / ZC;
+        const bool last_row = (r == H - 1);
+        const long long pitch = (long long)PW << 32;  // one pair row in position units
+        auto stage = [&](int c) {                     // chunk c -> raw
+            const int z0 = c * ZC, zn = min(ZC, D - z0);
+            if (use_tma) {
+                if (tid == 0) {
+                    fence_proxy_async();
+                    mbar_arrive_expect_tx(bar, (uint32_t)(zn * W * sizeof(float)));
+                    for (int zz = 0; zz < zn; zz++)
+                        tma_load_1d(raw + (size_t)zz * W, a.vol + ((size_t)(z0 + zz) * H + r) * W,
+                                    W * sizeof(float), bar);
+                }
+            } else {
+                for (int zz = 0; zz < zn; zz++) {
+                    const float* src = a.vol + ((size_t)(z0 + zz) * H + r) * W;
+                    for (int k = tid; k < W; k += kThreads) raw[(size_t)zz * W + k] = src[k];
+                }
+            }
+        };
+        if (use_tma && tid == 0) {
+            mbar_init(bar, 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        stage(0);
+        for (int c = 0; c < nchunks; c++) {
+            const int z0 = c * ZC;
+            const int zc = min(ZC, D - z0);
+            if (use_tma) {
+                const bool ok = mbar_wait_bounded(bar, (uint32_t)(c & 1), kWaitTries);
+                if (__syncthreads_or(!ok)) {
+                    if (tid == 0) atomicOr(a.status, kStatusTimeout);
+                    // let any copy still in flight land before the CTA's shared memory is released
+                    mbar_wait_bounded(bar, (uint32_t)(c & 1), kWaitTries);
+                    return;
+                }
+            } else {
+                __syncthreads();
+            }
+            for (int zz = 0; zz < zc; zz++) {
+                const bool flat = last_row || (z0 + zz == D - 1);  // raw floor voxel on the last row / plane
+                build_pairs_row(raw + (size_t)zz * W, pairs + (size_t)zz * PW, W, flat);
+            }
+            __syncthreads();
+            if (c + 1 < nchunks && use_tma) stage(c + 1);
+            const float2* P = pairs + 2;
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
+                const long long st = s_step[k / QP];
+                const int za = zab[k] & 0xFFFF;
+                const int cnt = (int)((uint32_t)zab[k] >> 16);
+                const bool full = (za <= z0) && (za + cnt >= z0 + zc);
+                const bool none = (cnt == 0) || (za + cnt <= z0) || (za >= z0 + zc);
+                if (__all_sync(0xffffffffu, full) && zc == ZC) {
+                    if (ZC >= 2) {
+                        // two interleaved sub-chains (even / odd planes)
+                        const long long s2 = 2 * (st + pitch);
+                        long long x0 = X[k], x1 = x0 + st + pitch;
+                        float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+                        for (int zz = 0; zz < ZC; zz += 2) {
+                            a0 += sample(P, x0);
+                            a1 += sample(P, x1);
+                            x0 += s2;
+                            x1 += s2;
+                        }
+                        X[k] = x0 - (long long)ZC * pitch;
+                        acc[k] += a0 + a1;
+                    } else {
+                        acc[k] += sample(P, X[k]);
+                        X[k] += st;
+                    }
+                } else if (__all_sync(0xffffffffu, none)) {
+                    X[k] += (long long)zc * st;
+                } else {
+                    const int lo = za - z0;
+                    long long x = X[k];
+                    float s = 0.0f;
+                    for (int zz = 0; zz < zc; zz++) {
+                        if ((unsigned)(zz - lo) < (unsigned)cnt) s += sample(P, x);
+                        x += st + pitch;
+                    }
+                    X[k] = x - (long long)zc * pitch;
+                    acc[k] += s;
+                }
+            }
+            __syncthreads();
+            if (c + 1 < nchunks && !use_tma) stage(c + 1);
+        }
+    }
+
+    // Epilogue: projection, norm, residual.
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int t = 0; t < TGMAX; t++) {
+        if (t >= TG) break;
+        const int tilt = a.tilts[g0 + t];
+        const double ninc = a.ftilt[tilt].ninc;
+        double e2 = 0.0;
+#pragma unroll
+        for (int q = 0; q < QP; q++) {
+            const int i = tid + q * kThreads;
+            if (i >= w) continue;
+            const int cnt = (int)((uint32_t)zab[t * QP + q] >> 16);
+            float th, nrm;
+            if (cnt == 0) {
+                th = __int_as_float(0x7fc00000);
+                nrm = 0.0f;
+            } else {
+                th = __double2float_rn((double)acc[t * QP + q] * ninc);
+                nrm = a.rays[(size_t)tilt * w + i].norm;
+            }
+            const size_t o = ((size_t)(g0 + t) * h + j) * w + i;
+            a.proj[o] = th;
+            a.norm[o] = nrm;
+            if (a.meas != nullptr) {
+                const float e = a.meas[((size_t)tilt * h + j) * w + i];
+                float d = 0.0f;
+                if (!isnan(e) && !isnan(th)) {
+                    const float qv = __fdiv_rn(__fsub_rn(e, th), nrm);
+                    const double v = (double)qv * a.factor;
+                    d = __double2float_rn(v);
+                    e2 += v * v;
+                }
+                a.diff[o] = d;
+            }
+        }
+        if (a.meas != nullptr) {
+            e2 = warp_sum(e2);
+            if (lane == 0) red[warp] = e2;
+            __syncthreads();
+            if (tid == 0) {
+                double sum = 0.0;
+                for (int k = 0; k < kThreads / 32; k++) sum += red[k];
+                a.errpart[(size_t)(g0 + t) * h + j] = sum;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <int QP, int ZC>
+cudaError_t set_attr_one() {
+    return cudaFuncSetAttribute(fp_kernel<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+}
+
+template <int QP>
+cudaError_t set_attr_qp() {
+    cudaError_t e;
+    if ((e = set_attr_one<QP, 16>()) != cudaSuccess) return e;
+    if ((e = set_attr_one<QP, 8>()) != cudaSuccess) return e;
+    if ((e = set_attr_one<QP, 4>()) != cudaSuccess) return e;
+    if ((e = set_attr_one<QP, 2>()) != cudaSuccess) return e;
+    return set_attr_one<QP, 1>();
+}
+
+// Largest chunk (planes per stage) whose shared memory fits two CTAs per SM.
+inline int choose_zc(int W) {
+    for (int zc = 16; zc > 1; zc >>= 1)
+        if (layout(zc, W, 16).total <= kMaxSmem) return zc;
+    return 1;
+}
+
+template <int QP>
+cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
+    const int ZC = choose_zc(a.W);
+    const Smem L = layout(ZC, a.W, 16 / QP);
+    if (L.total > kMaxSmem) return cudaErrorInvalidValue;
+    const int use_tma = (a.W % 4 == 0) && ((reinterpret_cast<uintptr_t>(a.vol) & 15) == 0);
+    dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0);
+    switch (ZC) {
+        case 16: fp_kernel<QP, 16><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
+        case 8: fp_kernel<QP, 8><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
+        case 4: fp_kernel<QP, 4><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
+        case 2: fp_kernel<QP, 2><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
+        default: fp_kernel<QP, 1><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace fpk
+}  // namespace tomo
+
+// One translation unit per QP defines these two entry points.
+#define TOMO_FP_INSTANTIATE(QP)                                                                          \
+    namespace tomo {                                                                                     \
+    cudaError_t fp_launch_q##QP(const FpLaunch& a, cudaStream_t s) { return fpk::launch_qp<QP>(a, s); } \
+    cudaError_t fp_attr_q##QP() { return fpk::set_attr_qp<QP>(); }                                     \
+    }

@@ -1,0 +1,4 @@
+// Forward-projection kernels for QP = 16 detector columns per thread (see fp_kernel.cuh).
+#include "fp_kernel.cuh"
+
+TOMO_FP_INSTANTIATE(16)

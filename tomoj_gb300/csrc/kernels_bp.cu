@@ -12,7 +12,7 @@
 // CTA tile: 64 x-columns x 64 z-planes of one volume row.  Thread (tx, tzg)
 // owns the 16 voxels z = z0 + 16*tzg + k of column x0 + tx.  Per chunk of 32
 // tilts the CTA stages, for each tilt, the segment of the image row the tile
-// projects onto as (value, slope) pairs read with 128-bit loads, plus each
+// projects onto as (v - slope, slope) pairs read with 128-bit loads, plus each
 // column's exact z-interval of voxels that fall inside the projection.
 #include <cmath>
 
@@ -22,6 +22,9 @@
 namespace tomo {
 namespace {
 
+#ifndef TOMO_BP_MIN_BLOCKS
+#define TOMO_BP_MIN_BLOCKS 3
+#endif
 constexpr int kBpThreads = 256;
 constexpr int kTX = 64;
 constexpr int kTZ = 64;
@@ -31,7 +34,7 @@ constexpr int kSeg = 96;     // >= 63 * (|cos| + |sin|) + 3 pairs per tilt segme
 constexpr int kRawSeg = 104; // floats staged per tilt (kSeg + 1 rounded up to float4, + alignment slack)
 
 struct BpShared {
-    float2 seg[kTC][kSeg];
+    float2 seg[kTC * kSeg];  // tilt t's pairs at [t * kSeg, (t + 1) * kSeg)
     float raw[kTC][kRawSeg];
     int seg_start[kTC];
     int raw_start[kTC];
@@ -56,7 +59,7 @@ __device__ __forceinline__ void bp_add(float& vox, float val) {
 }
 
 template <bool SANITIZE, bool POS>
-__global__ void __launch_bounds__(kBpThreads) bp_separable_kernel(BpLaunch a) {
+__global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_kernel(BpLaunch a) {
     __shared__ __align__(16) BpShared sh;
     const int tid = threadIdx.x;
     const int tx = tid & (kTX - 1);
@@ -147,31 +150,38 @@ __global__ void __launch_bounds__(kBpThreads) bp_separable_kernel(BpLaunch a) {
                 const float* up = (jp < h - 1) ? row + w : row;
                 if (!isfinite(up[k0]) || !isfinite(up[k1])) v0 = __int_as_float(0x7fc00000);
             }
-            sh.seg[t][m] = make_float2(v0, d);
+            sh.seg[t * kSeg + m] = make_float2(v0 - d, d);  // sample = fma(1 + f, d, v0 - d)
         }
         __syncthreads();
         // --- accumulate the chunk's tilts in update order ----------------------------------
         for (int t = 0; t < tc; t++) {
-            long long X = sh.K[t] + (long long)x * sh.C[t] + (long long)zs * sh.S[t];
+            // the tilt's segment base rides in the high word, so (X >> 32) is the flat pair index
+            const long long base = (long long)(t * kSeg - sh.seg_start[t]) << 32;
+            long long X = sh.K[t] + (long long)x * sh.C[t] + (long long)zs * sh.S[t] + base;
             const long long S = sh.S[t];
             const int zi = sh.zint[t][tx];
             const int kl = (zi & 0xFFFF) - zs;
             const int cnt = (int)((uint32_t)zi >> 16);
-            const float2* seg = &sh.seg[t][0] - sh.seg_start[t];
             const bool full = xin && kl <= 0 && kl + cnt >= kKZ;
             if (__all_sync(0xffffffffu, full)) {
+                // two independent position chains (even / odd z)
+                long long X1 = X + S;
+                const long long S2 = 2 * S;
 #pragma unroll
-                for (int k = 0; k < kKZ; k++) {
-                    const float2 p = seg[(int)(X >> 32)];
-                    bp_add<SANITIZE, POS>(vox[k], fmaf(fix_frac((uint32_t)X), p.y, p.x));
-                    X += S;
+                for (int k = 0; k < kKZ; k += 2) {
+                    const float2 p0 = sh.seg[(int)(X >> 32)];
+                    const float2 p1 = sh.seg[(int)(X1 >> 32)];
+                    bp_add<SANITIZE, POS>(vox[k], fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x));
+                    bp_add<SANITIZE, POS>(vox[k + 1], fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x));
+                    X += S2;
+                    X1 += S2;
                 }
             } else {
 #pragma unroll
                 for (int k = 0; k < kKZ; k++) {
                     if ((unsigned)(k - kl) < (unsigned)cnt) {
-                        const float2 p = seg[(int)(X >> 32)];
-                        bp_add<SANITIZE, POS>(vox[k], fmaf(fix_frac((uint32_t)X), p.y, p.x));
+                        const float2 p = sh.seg[(int)(X >> 32)];
+                        bp_add<SANITIZE, POS>(vox[k], fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x));
                     }
                     X += S;
                 }
