@@ -216,11 +216,17 @@ __global__ void __launch_bounds__(kThreads, 2) fp_kernel(FpLaunch a, int use_tma
                 } else if (__all_sync(0xffffffffu, none)) {
                     X[k] += (long long)zc * st;
                 } else {
+                    // partial chunk: branch-free, the load is predicated and an
+                    // out-of-range sample adds fma(F, 0, 0) = 0
                     const int lo = za - z0;
                     long long x = X[k];
                     float s = 0.0f;
+#pragma unroll 4
                     for (int zz = 0; zz < zc; zz++) {
-                        if ((unsigned)(zz - lo) < (unsigned)cnt) s += sample(P, x);
+                        const bool in = (unsigned)(zz - lo) < (unsigned)cnt;
+                        float2 p = make_float2(0.0f, 0.0f);
+                        if (in) p = P[(int)(x >> 32)];
+                        s += fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
                         x += st + pitch;
                     }
                     X[k] = x - (long long)zc * pitch;

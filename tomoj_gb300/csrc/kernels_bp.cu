@@ -74,12 +74,12 @@ __global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_k
     const int zs = z0 + tzg * kKZ;
     const bool xin = x < W;
 
+    const size_t plane = (size_t)H * W;
+    float* vb = a.vol + ((size_t)zs * H + r) * W + x;  // voxel (x, r, zs); voxel k is vb[k * plane]
+    const int nk = xin ? min(kKZ, D - zs) : 0;
     float vox[kKZ];
 #pragma unroll
-    for (int k = 0; k < kKZ; k++) {
-        const int z = zs + k;
-        vox[k] = (xin && z < D) ? a.vol[((size_t)z * H + r) * W + x] : 0.0f;
-    }
+    for (int k = 0; k < kKZ; k++) vox[k] = (k < nk) ? vb[k * plane] : 0.0f;
 
     const int xa = x0, xb = min(x0 + kTX - 1, W - 1);
     const int za = z0, zb = min(z0 + kTZ - 1, D - 1);
@@ -103,15 +103,16 @@ __global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_k
             sh.seg_start[tid] = s;
             sh.raw_start[tid] = s & ~3;
         }
-        for (int e = tid; e < tc * kTX; e += kBpThreads) {
-            const int t = e / kTX, xx = e % kTX;
-            const int xc = x0 + xx;
-            sh.zint[t][xx] = (xc < W) ? a.zint[(size_t)a.tilts[c0 + t] * W + xc] : 0;
+        for (int t = tid >> 6; t < tc; t += kBpThreads / kTX) {
+            const int xc = x0 + tx;
+            sh.zint[t][tx] = (xc < W) ? a.zint[(size_t)a.tilts[c0 + t] * W + xc] : 0;
         }
         __syncthreads();
         // --- stage image segments: 128-bit loads of the row, then (value, slope) pairs --
-        for (int e = tid; e < tc * (kRawSeg / 4); e += kBpThreads) {
-            const int t = e / (kRawSeg / 4), v = e % (kRawSeg / 4);
+        // one warp per tilt, lane v < 26 loads 4 floats
+        for (int t = tid >> 5; t < tc; t += kBpThreads / 32) {
+            const int v = tid & 31;
+            if (v >= kRawSeg / 4) continue;
             const float* row = a.img + ((size_t)(c0 + t) * h + jp) * w;
             const int k0 = sh.raw_start[t] + 4 * v;
             float4 q;
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_k
         }
         __syncthreads();
         for (int e = tid; e < tc * kSeg; e += kBpThreads) {
-            const int t = e / kSeg, m = e % kSeg;
+            const int t = e / kSeg, m = e - t * kSeg;
             const int k = sh.seg_start[t] + m;       // image column of this pair
             const int o = k - sh.raw_start[t];        // offset in the staged floats
             const float* row = a.img + ((size_t)(c0 + t) * h + jp) * w;
@@ -191,10 +192,8 @@ __global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_k
     }
 
 #pragma unroll
-    for (int k = 0; k < kKZ; k++) {
-        const int z = zs + k;
-        if (xin && z < D) a.vol[((size_t)z * H + r) * W + x] = vox[k];
-    }
+    for (int k = 0; k < kKZ; k++)
+        if (k < nk) vb[k * plane] = vox[k];
 }
 
 }  // namespace
