@@ -216,6 +216,8 @@ def ossart_iteration(vol, g: Geom, eulers, meas, order, relax, update, y0=0, y1=
     meas = np.ascontiguousarray(meas, np.float32)
     order = np.ascontiguousarray(order, np.int32)
     n = e.shape[0]
+    if order.shape != (n,) or meas.shape[0] != n:
+        raise ValueError("order must list every projection once (use update_step for one update)")
     err5 = np.zeros(5, np.float64)
     errs = np.zeros(n, np.float64)
     gc = g.c()
@@ -223,6 +225,22 @@ def ossart_iteration(vol, g: Geom, eulers, meas, order, relax, update, y0=0, y1=
                               _p(order, C.c_int), float(relax), int(update), y0, y1, _p(err5, C.c_double),
                               _p(errs, C.c_double))
     return err5, errs
+
+
+def update_step(vol, g: Geom, eulers, meas, batch, factor, y0=0, y1=None):
+    """One update of osartIteration (TomoReconstruction2.java:678-719): forward project and
+    difference every projection of `batch` against the current volume, then backproject
+    the differences in batch order.  Returns the per-projection sums of squares."""
+    _vol(vol)
+    errs = np.zeros(len(batch))
+    diffs = []
+    for k, p in enumerate(batch):
+        th, nm = project(vol, g, eulers[p], y0, y1)
+        d, errs[k] = difference(meas[p], th, nm, factor)
+        diffs.append(d)
+    for k, p in enumerate(batch):
+        backproject(vol, g, eulers[p], diffs[k], y0, y1)
+    return errs
 
 
 def wbp(vol, g: Geom, eulers, meas, mask=None, y0=0, y1=None):
