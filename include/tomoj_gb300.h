@@ -178,6 +178,26 @@ tomo_status tomo_profile_read(tomo_projector* p, double* out4);
 /* Tilts per forward-projection CTA (0 = automatic; tuning knob). */
 tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n);
 
+/* ---- projection + difference without allocation ----------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a JVM that keeps all device memory in its own pre-sized pool, a serving loop
+ * that may not take cudaMalloc's implicit synchronisation mid-request, code held
+ * to a fixed memory budget): the forward projection + difference of one update
+ * (projectAndDifference) on the caller's device buffers, with no handle.
+ *   volume  device float32 [D][H][W]      meas  device float32 [nproj][h][w] (aligned)
+ *   proj, norm, diff  device float32 [T][h][w] outputs (slot b = tilts[b])
+ *   err_out host double [T]               euler host double [nproj][9]
+ * Its scratch lives in one static device array of about 5 MiB that every GPU
+ * loading the library keeps until exit.  Limits: nproj <= 128, T <= 64,
+ * w, h <= 2048, vertical tilt axis.  The first call on a device sets up the
+ * scratch address (make it before any stream capture).  Calls share the
+ * scratch: calls that overlap on the GPU, or run concurrently, race.
+ * Synchronous on `stream` (cudaStream_t as void*, NULL = default stream). */
+tomo_status tomo_project_and_difference_noalloc(const tomo_geom* geom, const double* euler, const int32_t* tilts,
+                                                int32_t T, double factor, const float* volume, const float* meas,
+                                                float* proj, float* norm, float* diff, double* err_out,
+                                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif

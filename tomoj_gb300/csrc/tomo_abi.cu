@@ -44,6 +44,8 @@ tomo_status fail(tomo_status code, const std::string& msg) {
 
 }  // namespace
 
+void tomo::set_last_error(const char* msg) { g_err = msg; }
+
 struct tomo_projector {
     Geometry g{};
     tomo_params params{};

@@ -114,6 +114,9 @@ cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s);
 cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s);
 cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s);
 
+// Sets the calling thread's message for tomo_last_error.
+void set_last_error(const char* msg);
+
 // Counts kernels launched by this library (tomo_kernel_launches).
 void count_launch(int n = 1);
 extern std::atomic<uint64_t> g_launches;
