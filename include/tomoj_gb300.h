@@ -168,6 +168,26 @@ tomo_status tomo_order_shuffle(int32_t nproj, const double* euler, int32_t first
 /* Cooperative cancel, polled between updates (TomoReconstruction2.interrupt). */
 tomo_status tomo_cancel(tomo_projector* p);
 
+/* ---- batching (no counterpart in the reference) ------------------------------
+ * A batch runs iterations of many handles together (heterogeneous tilt-series:
+ * sizes, tilt counts and schemes may differ): for every update index one
+ * forward-projection launch per kernel variant covers that update of every
+ * member, then one residual reduction and one backprojection launch.  Members
+ * keep their own volumes, series and options (TVM, positivity...); the batch
+ * only references them, so destroy the batch before its handles.  A step's
+ * launches are captured as one CUDA graph and replayed while the membership
+ * and update sizes are unchanged.  Members must live on one device. */
+typedef struct tomo_batch tomo_batch;
+tomo_status tomo_batch_create(tomo_batch** out);
+tomo_status tomo_batch_destroy(tomo_batch* b);
+/* Replaces the membership (n handles). */
+tomo_status tomo_batch_set(tomo_batch* b, tomo_projector* const* members, int32_t n);
+/* One OS-SART iteration of every member (osartIteration, TomoReconstruction2.java:636-733):
+ * relax[m], update[m] (0 = SIRT) and the ordering's first index first[m] per member;
+ * err_out (n*5, may be NULL) receives each member's {average, min, argmin, max, argmax}. */
+tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32_t* update, const int32_t* first,
+                                 int32_t use_graph, double* err_out);
+
 /* ---- measurement (no counterpart in the reference; Chrono-style timing) ----
  * When enabled, tomo_run_ossart records CUDA events around every forward
  * projection (+ residual reduction) and backprojection launch on the handle's

@@ -1,0 +1,410 @@
+// Batched execution of many handles (heterogeneous tilt-series).
+//
+// A batch references existing handles (each keeps its own volume, series,
+// tables and options) and runs one OS-SART iteration of all of them together:
+// for every update index s, one forward-projection launch per kernel variant
+// covers update s of every member that has one (each CTA reads its
+// {descriptor, tilt group, row} work item), one batched residual reduction
+// follows, and one backprojection launch covers all members' tiles.  The
+// per-member descriptors and work lists are rebuilt only when the membership
+// or the update sizes change, and the step's launches are captured once as a
+// CUDA graph and replayed while they stay valid; every iteration only uploads
+// the members' new orderings (orderShuffleART with the given first index) and
+// reads their residuals back.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "tomo_handle.h"
+
+using namespace tomo;
+
+struct tomo_batch {
+    std::vector<tomo_projector*> members;
+    std::vector<int> upd;        // update size of each member in the cached plan
+    std::vector<double> factor;  // relaxation factor of each member in the cached plan
+    bool plan_valid = false;
+    cudaStream_t stream = nullptr;
+    // device plan
+    FpLaunch* d_fp = nullptr;
+    BpLaunch* d_bp = nullptr;
+    ErrReduce* d_red = nullptr;
+    int4* d_fp_items = nullptr;
+    int4* d_bp_items = nullptr;
+    size_t cap_fp = 0, cap_bp = 0, cap_fpi = 0, cap_bpi = 0, cap_red = 0;
+    struct FpSeg {
+        int s, qp, zc;
+        size_t smem;
+        int off, n;
+    };
+    struct BpSeg {
+        int s;
+        bool sanitize, pos;
+        int off, n;
+    };
+    struct RedSeg {
+        int s, off, n, maxT;
+    };
+    std::vector<FpSeg> fp_segs;
+    std::vector<BpSeg> bp_segs;
+    std::vector<RedSeg> red_segs;
+    int max_nsub = 0;
+    bool has_fista = false;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    uint64_t graph_kernels = 0;
+    std::vector<int> host_orders;
+    std::vector<double> host_err;
+};
+
+namespace {
+
+#define BCK(expr)                                                                              \
+    do {                                                                                       \
+        cudaError_t _e = (expr);                                                               \
+        if (_e != cudaSuccess) {                                                               \
+            cudaGetLastError();                                                                \
+            return handle_fail(TOMO_ERR_CUDA, (std::string(#expr) + ": " + cudaGetErrorString(_e)).c_str()); \
+        }                                                                                      \
+    } while (0)
+
+#define BCKS(expr)                    \
+    do {                              \
+        tomo_status _s = (expr);      \
+        if (_s != TOMO_OK) return _s; \
+    } while (0)
+
+template <class T>
+tomo_status ensure(T** ptr, size_t* cap, size_t n) {
+    if (n <= *cap && *ptr) return TOMO_OK;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    size_t c = std::max<size_t>(n, 16);
+    if (cudaMalloc(reinterpret_cast<void**>(ptr), c * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        *cap = 0;
+        return handle_fail(TOMO_ERR_NOMEM, "batch plan allocation failed");
+    }
+    *cap = c;
+    return TOMO_OK;
+}
+
+void drop_graph(tomo_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// Descriptors and work lists of one iteration for the current membership.
+tomo_status build_plan(tomo_batch* b) {
+    std::vector<FpLaunch> fp;
+    std::vector<BpLaunch> bp;
+    std::vector<ErrReduce> red;
+    // work items grouped by (s, qp, zc) for FP and (s, sanitize, pos) for BP
+    std::map<std::tuple<int, int, int>, std::vector<int4>> fpi;
+    std::map<std::tuple<int, int, int>, size_t> fpsmem;
+    std::map<std::tuple<int, int, int>, std::vector<int4>> bpi;
+    std::map<int, std::vector<ErrReduce>> reds;
+    b->max_nsub = 0;
+    b->has_fista = false;
+    const int tx = bp_tile_x(), tz = bp_tile_z();
+    for (size_t m = 0; m < b->members.size(); m++) {
+        tomo_projector* p = b->members[m];
+        const Geometry& g = p->g;
+        const int N = g.N, upd = b->upd[m];
+        const int nsub = (N + upd - 1) / upd;
+        b->max_nsub = std::max(b->max_nsub, nsub);
+        b->has_fista = b->has_fista || p->fista;
+        // rows the forward projector never writes must read as zero residual
+        BCK(cudaMemsetAsync(p->d_errpart, 0, sizeof(double) * (size_t)N * g.h, b->stream));
+        const int qp = fp_qp(g.w);
+        const int zc = fp_choose_zc(g.W);
+        const int use_tma = (g.W % 4 == 0) && ((reinterpret_cast<uintptr_t>(p->d_vol) & 15) == 0);
+        const int offset = (g.h > g.H && g.scale == 1) ? (g.h - g.H) / 2 : 0;
+        const int j0 = std::max(0, (int)std::floor(offset * g.scale + 0.5));
+        for (int s = 0; s < nsub; s++) {
+            const int T = std::min(upd, N - s * upd);
+            const int slot = s * upd;
+            FpLaunch a{};
+            a.vol = p->d_vol;
+            a.meas = p->d_meas;
+            a.tilts = p->d_batch + slot;
+            a.T = T;
+            a.ftilt = p->d_ftilt;
+            a.rays = p->d_rays;
+            a.proj = p->d_proj + (size_t)slot * p->npix;
+            a.norm = p->d_norm + (size_t)slot * p->npix;
+            a.diff = p->d_diff + (size_t)slot * p->npix;
+            a.errpart = p->d_errpart + (size_t)slot * g.h;
+            a.factor = b->factor[m];
+            a.j0 = j0;
+            a.j1 = g.h;
+            a.tilts_per_cta = handle_tilts_per_cta(p, T);
+            a.W = g.W;
+            a.H = g.H;
+            a.D = g.D;
+            a.w = g.w;
+            a.h = g.h;
+            a.row_off = g.fp_row_off;
+            a.status = p->d_status;
+            const int di = (int)fp.size();
+            fp.push_back(a);
+            const auto key = std::make_tuple(s, qp, zc);
+            fpsmem[key] = std::max(fpsmem[key], fp_smem_bytes(zc, g.W, qp));
+            auto& items = fpi[key];
+            for (int g0 = 0; g0 < T; g0 += a.tilts_per_cta)
+                for (int j = j0; j < g.h; j++) items.push_back(make_int4(di, g0, j, use_tma));
+            reds[s].push_back(ErrReduce{a.errpart, p->d_err + slot, T, g.h});
+            BpLaunch c{};
+            c.vol = p->d_vol;
+            c.img = a.diff;
+            c.tilts = a.tilts;
+            c.T = T;
+            c.btilt = p->d_btilt;
+            c.zint = p->d_zint;
+            c.y0 = 0;
+            c.y1 = g.H;
+            c.W = g.W;
+            c.H = g.H;
+            c.D = g.D;
+            c.w = g.w;
+            c.h = g.h;
+            c.row_off = g.bp_row_off;
+            c.positivity = p->params.positivity;
+            c.sanitize = p->meas_has_inf || p->vol_nonfinite;
+            c.status = p->d_status;
+            const int bi = (int)bp.size();
+            bp.push_back(c);
+            auto& bitems = bpi[std::make_tuple(s, c.sanitize, c.positivity)];
+            for (int r = 0; r < g.H; r++) {
+                const int jp = r + g.bp_row_off;
+                if (jp < 0 || jp >= g.h) continue;
+                for (int zt = 0; zt < (g.D + tz - 1) / tz; zt++)
+                    for (int xt = 0; xt < (g.W + tx - 1) / tx; xt++) bitems.push_back(make_int4(bi, xt, zt, r));
+            }
+        }
+    }
+    // flatten
+    std::vector<int4> fp_all, bp_all;
+    b->fp_segs.clear();
+    b->bp_segs.clear();
+    b->red_segs.clear();
+    for (auto& kv : fpi) {
+        tomo_batch::FpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first), fpsmem[kv.first],
+                             (int)fp_all.size(), (int)kv.second.size()};
+        fp_all.insert(fp_all.end(), kv.second.begin(), kv.second.end());
+        b->fp_segs.push_back(sg);
+    }
+    for (auto& kv : bpi) {
+        tomo_batch::BpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first) != 0, std::get<2>(kv.first) != 0,
+                             (int)bp_all.size(), (int)kv.second.size()};
+        bp_all.insert(bp_all.end(), kv.second.begin(), kv.second.end());
+        b->bp_segs.push_back(sg);
+    }
+    for (auto& kv : reds) {
+        int maxT = 0;
+        for (auto& r : kv.second) maxT = std::max(maxT, r.T);
+        b->red_segs.push_back(tomo_batch::RedSeg{kv.first, (int)red.size(), (int)kv.second.size(), maxT});
+        red.insert(red.end(), kv.second.begin(), kv.second.end());
+    }
+    BCKS(ensure(&b->d_fp, &b->cap_fp, fp.size()));
+    BCKS(ensure(&b->d_bp, &b->cap_bp, bp.size()));
+    BCKS(ensure(&b->d_red, &b->cap_red, red.size()));
+    BCKS(ensure(&b->d_fp_items, &b->cap_fpi, fp_all.size()));
+    BCKS(ensure(&b->d_bp_items, &b->cap_bpi, bp_all.size()));
+    BCK(cudaMemcpyAsync(b->d_fp, fp.data(), sizeof(FpLaunch) * fp.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->d_bp, bp.data(), sizeof(BpLaunch) * bp.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->d_red, red.data(), sizeof(ErrReduce) * red.size(), cudaMemcpyHostToDevice, b->stream));
+    if (!fp_all.empty())
+        BCK(cudaMemcpyAsync(b->d_fp_items, fp_all.data(), sizeof(int4) * fp_all.size(), cudaMemcpyHostToDevice,
+                            b->stream));
+    if (!bp_all.empty())
+        BCK(cudaMemcpyAsync(b->d_bp_items, bp_all.data(), sizeof(int4) * bp_all.size(), cudaMemcpyHostToDevice,
+                            b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    b->plan_valid = true;
+    drop_graph(b);
+    return TOMO_OK;
+}
+
+tomo_status launch_step(tomo_batch* b) {
+    for (tomo_projector* p : b->members) BCKS(handle_start_iteration(p));
+    for (int s = 0; s < b->max_nsub; s++) {
+        for (auto& sg : b->fp_segs)
+            if (sg.s == s)
+                BCK(launch_fp_batch(sg.qp, b->d_fp, b->d_fp_items + sg.off, sg.n, sg.zc, sg.smem, b->stream));
+        for (auto& sg : b->red_segs)
+            if (sg.s == s) BCK(launch_reduce_err_batch(b->d_red + sg.off, sg.n, sg.maxT, b->stream));
+        for (auto& sg : b->bp_segs)
+            if (sg.s == s) BCK(launch_bp_batch(sg.sanitize, sg.pos, b->d_bp, b->d_bp_items + sg.off, sg.n, b->stream));
+    }
+    for (tomo_projector* p : b->members) BCKS(handle_end_iteration(p));
+    return TOMO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tomo_status tomo_batch_create(tomo_batch** out) {
+    if (!out) return handle_fail(TOMO_ERR_INVALID, "null argument");
+    tomo_batch* b = new tomo_batch();
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return handle_fail(TOMO_ERR_CUDA, "cannot create the batch stream");
+    }
+    *out = b;
+    return TOMO_OK;
+}
+
+tomo_status tomo_batch_destroy(tomo_batch* b) {
+    if (!b) return TOMO_OK;
+    cudaStreamSynchronize(b->stream);
+    drop_graph(b);
+    cudaFree(b->d_fp);
+    cudaFree(b->d_bp);
+    cudaFree(b->d_red);
+    cudaFree(b->d_fp_items);
+    cudaFree(b->d_bp_items);
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return TOMO_OK;
+}
+
+tomo_status tomo_batch_set(tomo_batch* b, tomo_projector* const* members, int32_t n) {
+    if (!b || (n > 0 && !members) || n < 0) return handle_fail(TOMO_ERR_INVALID, "bad argument");
+    for (int i = 0; i < n; i++) {
+        if (!members[i]) return handle_fail(TOMO_ERR_INVALID, "null member");
+        BCKS(handle_need_series(members[i]));
+        for (int k = 0; k < i; k++)
+            if (members[k] == members[i]) return handle_fail(TOMO_ERR_INVALID, "a handle appears twice");
+    }
+    BCK(cudaStreamSynchronize(b->stream));
+    b->members.assign(members, members + n);
+    b->plan_valid = false;
+    drop_graph(b);
+    return TOMO_OK;
+}
+
+tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32_t* update, const int32_t* first,
+                                 int32_t use_graph, double* err_out) {
+    if (!b || !relax || !update || !first) return handle_fail(TOMO_ERR_INVALID, "null argument");
+    const size_t M = b->members.size();
+    if (M == 0) return TOMO_OK;
+    // the members' own streams must be idle: their buffers are used on the batch stream
+    for (tomo_projector* p : b->members) BCK(cudaStreamSynchronize(p->stream));
+    std::vector<int> upd(M);
+    std::vector<double> fac(M);
+    for (size_t m = 0; m < M; m++) {
+        const int N = b->members[m]->g.N;
+        if (update[m] < 0) return handle_fail(TOMO_ERR_INVALID, "negative update size");
+        if (first[m] < 0 || first[m] >= N) return handle_fail(TOMO_ERR_INVALID, "first index out of range");
+        upd[m] = update[m] == 0 ? N : std::min(update[m], N);
+        fac[m] = (double)(float)(relax[m] / upd[m]);  // float factorimg (TomoReconstruction2.java:646)
+    }
+    if (!b->plan_valid || upd != b->upd || fac != b->factor) {
+        b->upd = upd;
+        b->factor = fac;
+        BCKS(build_plan(b));
+    }
+    // orderings of this iteration into each member's batch buffer
+    size_t total = 0;
+    for (size_t m = 0; m < M; m++) total += b->members[m]->g.N;
+    b->host_orders.resize(total);
+    size_t o = 0;
+    for (size_t m = 0; m < M; m++) {
+        tomo_projector* p = b->members[m];
+        order_shuffle(p->g.N, p->euler.data(), first[m], &b->host_orders[o]);
+        BCK(cudaMemcpyAsync(p->d_batch, &b->host_orders[o], sizeof(int) * p->g.N, cudaMemcpyHostToDevice,
+                            b->stream));
+        o += p->g.N;
+    }
+    // the members' start/end-of-iteration work (TVM, FISTA) joins the batch stream
+    std::vector<cudaStream_t> saved(M);
+    for (size_t m = 0; m < M; m++) {
+        saved[m] = b->members[m]->stream;
+        b->members[m]->stream = b->stream;
+    }
+    struct Restore {
+        tomo_batch* b;
+        std::vector<cudaStream_t>& s;
+        ~Restore() {
+            for (size_t m = 0; m < b->members.size(); m++) b->members[m]->stream = s[m];
+        }
+    } restore{b, saved};
+    if (use_graph && !b->has_fista) {
+        if (!b->exec) {
+            const uint64_t before = g_launches.load();
+            BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            tomo_status st = launch_step(b);
+            cudaError_t ce = cudaStreamEndCapture(b->stream, &b->graph);
+            b->graph_kernels = g_launches.load() - before;
+            g_launches -= b->graph_kernels;
+            if (st != TOMO_OK) {
+                drop_graph(b);
+                return st;
+            }
+            BCK(ce);
+            BCK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+        }
+        BCK(cudaGraphLaunch(b->exec, b->stream));
+        count_launch((int)b->graph_kernels);
+    } else {
+        BCKS(launch_step(b));
+    }
+    b->host_err.resize(total);
+    o = 0;
+    for (size_t m = 0; m < M; m++) {
+        tomo_projector* p = b->members[m];
+        BCK(cudaMemcpyAsync(&b->host_err[o], p->d_err, sizeof(double) * p->g.N, cudaMemcpyDeviceToHost, b->stream));
+        o += p->g.N;
+    }
+    BCK(cudaStreamSynchronize(b->stream));
+    o = 0;
+    for (size_t m = 0; m < M; m++) {
+        tomo_projector* p = b->members[m];
+        int st = 0;
+        BCK(cudaMemcpy(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (st != 0) {
+            cudaMemset(p->d_status, 0, sizeof(int));
+            return handle_fail(TOMO_ERR_DEVICE, "a kernel reported a bounded-wait timeout");
+        }
+        if (err_out) {
+            const int N = p->g.N;
+            const int* ord = &b->host_orders[o];
+            double som = 0, errmin = 3.4028234663852886e38, errmax = 0;
+            int imin = 0, imax = 0;
+            for (int t = 0; t < N; t++) {
+                const double e = b->host_err[o + t];
+                som += e;
+                if (e > errmax) {
+                    errmax = e;
+                    imax = ord[t];
+                } else if (e < errmin) {
+                    errmin = e;
+                    imin = ord[t];
+                }
+            }
+            const double wh = (double)p->g.W * p->g.H;
+            double* e5 = err_out + 5 * m;
+            e5[0] = std::sqrt(som / ((double)N * wh));
+            e5[1] = std::sqrt(errmin / wh);
+            e5[2] = imin;
+            e5[3] = std::sqrt(errmax / wh);
+            e5[4] = imax;
+        }
+        o += p->g.N;
+    }
+    for (tomo_projector* p : b->members) {
+        p->batch.clear();
+        p->batch_uploaded = false;
+        p->diffs_valid = p->projected = p->obatch_valid = false;
+    }
+    return TOMO_OK;
+}
+
+}  // extern "C"

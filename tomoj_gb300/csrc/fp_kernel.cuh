@@ -93,8 +93,9 @@ __device__ __forceinline__ float sample(const float2* __restrict__ P, long long 
     return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
 }
 
+// One CTA's work: projection row j, tilts [g0, g0 + tilts_per_cta) of problem `a`.
 template <int QP, int ZC>
-__global__ void __launch_bounds__(kThreads, 2) fp_kernel(FpLaunch a, int use_tma) {
+__device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma) {
     constexpr int TGMAX = 16 / QP;
     constexpr int NR = TGMAX * QP;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -108,8 +109,6 @@ __global__ void __launch_bounds__(kThreads, 2) fp_kernel(FpLaunch a, int use_tma
     const int tid = threadIdx.x;
     const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
     const int PW = L.PW;
-    const int j = a.j0 + blockIdx.y;
-    const int g0 = blockIdx.x * a.tilts_per_cta;
     const int TG = min(a.tilts_per_cta, a.T - g0);
     const int r = j - a.row_off;
     const bool row_in = (r >= 0 && r < H);
@@ -289,8 +288,24 @@ __global__ void __launch_bounds__(kThreads, 2) fp_kernel(FpLaunch a, int use_tma
 }
 
 template <int QP, int ZC>
+__global__ void __launch_bounds__(kThreads, 2) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
+    fp_body<QP, ZC>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma);
+}
+
+// Batched form: CTA b works on item {problem, first tilt, row, use_tma} of many problems.
+template <int QP, int ZC>
+__global__ void __launch_bounds__(kThreads, 2)
+    fp_kernel_batch(const FpLaunch* __restrict__ descs, const int4* __restrict__ items) {
+    const int4 it = items[blockIdx.x];
+    fp_body<QP, ZC>(descs[it.x], it.y, it.z, it.w);
+}
+
+template <int QP, int ZC>
 cudaError_t set_attr_one() {
-    return cudaFuncSetAttribute(fp_kernel<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaError_t e = cudaFuncSetAttribute(fp_kernel<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fp_kernel_batch<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kMaxSmem);
 }
 
 template <int QP>
@@ -328,12 +343,32 @@ cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int QP>
+cudaError_t launch_batch_qp(const FpLaunch* descs, const int4* items, int n_items, int ZC, size_t smem,
+                            cudaStream_t s) {
+    if (n_items <= 0) return cudaSuccess;
+    if (smem > kMaxSmem) return cudaErrorInvalidValue;
+    switch (ZC) {
+        case 16: fp_kernel_batch<QP, 16><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 8: fp_kernel_batch<QP, 8><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 4: fp_kernel_batch<QP, 4><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 2: fp_kernel_batch<QP, 2><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        default: fp_kernel_batch<QP, 1><<<n_items, kThreads, smem, s>>>(descs, items); break;
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace fpk
 }  // namespace tomo
 
-// One translation unit per QP defines these two entry points.
+// One translation unit per QP defines these entry points.
 #define TOMO_FP_INSTANTIATE(QP)                                                                          \
     namespace tomo {                                                                                     \
     cudaError_t fp_launch_q##QP(const FpLaunch& a, cudaStream_t s) { return fpk::launch_qp<QP>(a, s); } \
     cudaError_t fp_attr_q##QP() { return fpk::set_attr_qp<QP>(); }                                     \
+    cudaError_t fp_batch_q##QP(const FpLaunch* d, const int4* it, int n, int zc, size_t smem,            \
+                               cudaStream_t s) {                                                         \
+        return fpk::launch_batch_qp<QP>(d, it, n, zc, smem, s);                                          \
+    }                                                                                                    \
     }

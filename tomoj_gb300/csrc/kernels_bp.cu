@@ -58,16 +58,14 @@ __device__ __forceinline__ void bp_add(float& vox, float val) {
     }
 }
 
+// One CTA's work: tile (x0, z0) of volume row r of problem `a`.
 template <bool SANITIZE, bool POS>
-__global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_kernel(BpLaunch a) {
+__device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const int z0, const int r) {
     __shared__ __align__(16) BpShared sh;
     const int tid = threadIdx.x;
     const int tx = tid & (kTX - 1);
     const int tzg = tid >> 6;
     const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
-    const int x0 = blockIdx.x * kTX;
-    const int z0 = blockIdx.y * kTZ;
-    const int r = a.y0 + blockIdx.z;
     const int jp = r + a.row_off;  // projection row seen by this volume row
     if (jp < 0 || jp >= h) return;  // no tilt reaches this row (yy outside [0,h))
     const int x = x0 + tx;
@@ -196,7 +194,37 @@ __global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_k
         if (k < nk) vb[k * plane] = vox[k];
 }
 
+template <bool SANITIZE, bool POS>
+__global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_kernel(const __grid_constant__ BpLaunch a) {
+    bp_body<SANITIZE, POS>(a, blockIdx.x * kTX, blockIdx.y * kTZ, a.y0 + blockIdx.z);
+}
+
+// Batched form: CTA b works on item {problem, x tile, z tile, row} of many problems.
+template <bool SANITIZE, bool POS>
+__global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS)
+    bp_kernel_batch(const BpLaunch* __restrict__ descs, const int4* __restrict__ items) {
+    const int4 it = items[blockIdx.x];
+    bp_body<SANITIZE, POS>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
+}
+
 }  // namespace
+
+int bp_tile_x() { return kTX; }
+int bp_tile_z() { return kTZ; }
+
+cudaError_t launch_bp_batch(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n_items,
+                            cudaStream_t s) {
+    if (n_items <= 0) return cudaSuccess;
+    if (sanitize) {
+        if (positivity) bp_kernel_batch<true, true><<<n_items, kBpThreads, 0, s>>>(descs, items);
+        else bp_kernel_batch<true, false><<<n_items, kBpThreads, 0, s>>>(descs, items);
+    } else {
+        if (positivity) bp_kernel_batch<false, true><<<n_items, kBpThreads, 0, s>>>(descs, items);
+        else bp_kernel_batch<false, false><<<n_items, kBpThreads, 0, s>>>(descs, items);
+    }
+    count_launch();
+    return cudaGetLastError();
+}
 
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s) {
     if (a.T <= 0 || a.y1 <= a.y0) return cudaSuccess;

@@ -15,6 +15,11 @@ cudaError_t fp_attr_q2();
 cudaError_t fp_attr_q4();
 cudaError_t fp_attr_q8();
 cudaError_t fp_attr_q16();
+cudaError_t fp_batch_q1(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
+cudaError_t fp_batch_q2(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
+cudaError_t fp_batch_q4(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
+cudaError_t fp_batch_q8(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
+cudaError_t fp_batch_q16(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
 
 namespace {
 constexpr int kFpThreads = 256;
@@ -39,6 +44,39 @@ int fp_max_tilts_per_cta(int w) {
     if (qp <= 8) return 2;
     if (qp <= 16) return 1;
     return 0;
+}
+
+int fp_qp(int w) {
+    const int qp = (w + kFpThreads - 1) / kFpThreads;
+    return qp <= 1 ? 1 : qp <= 2 ? 2 : qp <= 4 ? 4 : qp <= 8 ? 8 : qp <= 16 ? 16 : 0;
+}
+
+// Shared-memory bytes of a CTA for width W and planes per chunk ZC (matches fpk::layout).
+size_t fp_smem_bytes(int ZC, int W, int qp) {
+    size_t o = 16 + (size_t)ZC * W * sizeof(float);
+    o = (o + 15) & ~(size_t)15;
+    o += (size_t)ZC * (W + 4) * sizeof(float2);
+    o = (o + 15) & ~(size_t)15;
+    o += (kFpThreads / 32) * sizeof(double) + (size_t)(16 / qp) * sizeof(long long);
+    return o;
+}
+
+int fp_choose_zc(int W) {
+    for (int zc = 16; zc > 1; zc >>= 1)
+        if (fp_smem_bytes(zc, W, 1) <= 112 * 1024) return zc;
+    return 1;
+}
+
+cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,
+                            cudaStream_t s) {
+    switch (qp) {
+        case 1: return fp_batch_q1(descs, items, n_items, zc, smem, s);
+        case 2: return fp_batch_q2(descs, items, n_items, zc, smem, s);
+        case 4: return fp_batch_q4(descs, items, n_items, zc, smem, s);
+        case 8: return fp_batch_q8(descs, items, n_items, zc, smem, s);
+        case 16: return fp_batch_q16(descs, items, n_items, zc, smem, s);
+    }
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s) {

@@ -122,6 +122,15 @@ __global__ void reduce_err_kernel(const double* __restrict__ errpart, double* __
     err[t] = s;
 }
 
+__global__ void reduce_err_batch_kernel(const ErrReduce* __restrict__ jobs) {
+    const ErrReduce j = jobs[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= j.T) return;
+    double s = 0.0;
+    for (int r = 0; r < j.h; r++) s += j.errpart[(size_t)t * j.h + r];
+    j.err[t] = s;
+}
+
 // TotalVariationDenoising_3D.updateP (Filters/.../TotalVariationDenoising_3D.java:115-156).
 __global__ void tv_p_kernel(const float* __restrict__ u, float* px, float* py, float* pz, int W, int H, int D,
                             float theta, float g, float dt) {
@@ -305,6 +314,13 @@ cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2
 
 cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s) {
     reduce_err_kernel<<<(T + 127) / 128, 128, 0, s>>>(errpart, err, T, h);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_err_batch(const ErrReduce* jobs, int n_jobs, int max_T, cudaStream_t s) {
+    if (n_jobs <= 0) return cudaSuccess;
+    reduce_err_batch_kernel<<<dim3((max_T + 127) / 128, n_jobs), 128, 0, s>>>(jobs);
     count_launch();
     return cudaGetLastError();
 }

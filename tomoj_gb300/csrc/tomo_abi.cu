@@ -10,6 +10,7 @@
 
 #include "../../include/tomoj_gb300.h"
 #include "tomo_internal.h"
+#include "tomo_handle.h"
 
 namespace tomo {
 std::atomic<uint64_t> g_launches{0};
@@ -46,64 +47,6 @@ tomo_status fail(tomo_status code, const std::string& msg) {
 
 void tomo::set_last_error(const char* msg) { g_err = msg; }
 
-struct tomo_projector {
-    Geometry g{};
-    tomo_params params{};
-    cudaStream_t stream = nullptr;
-    cudaStream_t own_stream = nullptr;
-    int device = 0;
-    size_t npix = 0, nvox = 0;
-    std::vector<void*> allocs;
-    uint64_t bytes = 0;
-
-    float* d_vol = nullptr;
-    float* d_raw = nullptr;
-    float* d_meas = nullptr;
-    float* d_proj = nullptr;
-    float* d_norm = nullptr;
-    float* d_diff = nullptr;
-    float* d_obatch = nullptr;
-    double* d_errpart = nullptr;
-    double* d_err = nullptr;
-    int* d_batch = nullptr;
-    int* d_orders = nullptr;
-    int orders_cap = 0;
-    int* d_status = nullptr;
-    int* d_flags = nullptr;
-    FpTilt* d_ftilt = nullptr;
-    FpRay* d_rays = nullptr;
-    BpTilt* d_btilt = nullptr;
-    int32_t* d_zint = nullptr;
-    double* d_tinv = nullptr;
-    double* d_stats = nullptr;
-    unsigned char* d_identity = nullptr;
-    float* d_mask = nullptr;
-    float2* d_tw = nullptr;
-    float *d_tv_u = nullptr, *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;
-    float* d_prev = nullptr;
-
-    std::vector<double> euler;
-    std::vector<int> batch;
-    bool batch_uploaded = false;
-    bool series_loaded = false;
-    bool diffs_valid = false;
-    bool projected = false;
-    bool obatch_valid = false;
-    bool meas_has_nan = false, meas_has_inf = false;
-    bool vol_nonfinite = false;
-    int weight_kind = TOMO_WEIGHT_NONE;
-    float tv_theta = 25.0f, tv_g = 1.0f, tv_dt = 0.1f;
-    int tv_iters = 0;
-    bool fista = false;
-    double fista_t = 0.0;
-    std::atomic<int> cancel{0};
-    int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
-    // per-kernel timing of the OS-SART driver (tomo_set_profiling)
-    bool profile = false;
-    std::vector<cudaEvent_t> ev;
-    double prof_ms[2] = {0, 0};  // forward projection (+ residual reduction), backprojection
-    long long prof_n[2] = {0, 0};
-};
 
 namespace {
 
@@ -308,6 +251,14 @@ tomo_status start_iteration(tomo_projector* p) {
 }
 
 }  // namespace
+
+namespace tomo {
+tomo_status handle_fail(tomo_status code, const char* msg) { return fail(code, msg); }
+tomo_status handle_need_series(tomo_projector* p) { return need_series(p); }
+tomo_status handle_start_iteration(tomo_projector* p) { return start_iteration(p); }
+tomo_status handle_end_iteration(tomo_projector* p) { return end_iteration(p); }
+int handle_tilts_per_cta(const tomo_projector* p, int T) { return auto_tilts_per_cta(p, T, 0); }
+}  // namespace tomo
 
 extern "C" {
 

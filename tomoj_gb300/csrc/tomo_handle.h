@@ -1,0 +1,75 @@
+// The projector handle (shared by the C-ABI translation units).
+#pragma once
+#include <atomic>
+#include <vector>
+
+#include "../../include/tomoj_gb300.h"
+#include "tomo_internal.h"
+
+struct tomo_projector {
+    tomo::Geometry g{};
+    tomo_params params{};
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int device = 0;
+    size_t npix = 0, nvox = 0;
+    std::vector<void*> allocs;
+    uint64_t bytes = 0;
+
+    float* d_vol = nullptr;
+    float* d_raw = nullptr;
+    float* d_meas = nullptr;
+    float* d_proj = nullptr;
+    float* d_norm = nullptr;
+    float* d_diff = nullptr;
+    float* d_obatch = nullptr;
+    double* d_errpart = nullptr;
+    double* d_err = nullptr;
+    int* d_batch = nullptr;
+    int* d_orders = nullptr;
+    int orders_cap = 0;
+    int* d_status = nullptr;
+    int* d_flags = nullptr;
+    tomo::FpTilt* d_ftilt = nullptr;
+    tomo::FpRay* d_rays = nullptr;
+    tomo::BpTilt* d_btilt = nullptr;
+    int32_t* d_zint = nullptr;
+    double* d_tinv = nullptr;
+    double* d_stats = nullptr;
+    unsigned char* d_identity = nullptr;
+    float* d_mask = nullptr;
+    float2* d_tw = nullptr;
+    float *d_tv_u = nullptr, *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;
+    float* d_prev = nullptr;
+
+    std::vector<double> euler;
+    std::vector<int> batch;
+    bool batch_uploaded = false;
+    bool series_loaded = false;
+    bool diffs_valid = false;
+    bool projected = false;
+    bool obatch_valid = false;
+    bool meas_has_nan = false, meas_has_inf = false;
+    bool vol_nonfinite = false;
+    int weight_kind = TOMO_WEIGHT_NONE;
+    float tv_theta = 25.0f, tv_g = 1.0f, tv_dt = 0.1f;
+    int tv_iters = 0;
+    bool fista = false;
+    double fista_t = 0.0;
+    std::atomic<int> cancel{0};
+    int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+    // per-kernel timing of the OS-SART driver (tomo_set_profiling)
+    bool profile = false;
+    std::vector<cudaEvent_t> ev;
+    double prof_ms[2] = {0, 0};  // forward projection (+ residual reduction), backprojection
+    long long prof_n[2] = {0, 0};
+};
+
+namespace tomo {
+// Helpers of tomo_abi.cu used by the batch driver.
+tomo_status handle_fail(tomo_status code, const char* msg);
+tomo_status handle_need_series(tomo_projector* p);
+tomo_status handle_start_iteration(tomo_projector* p);
+tomo_status handle_end_iteration(tomo_projector* p);
+int handle_tilts_per_cta(const tomo_projector* p, int T);
+}  // namespace tomo

@@ -94,6 +94,11 @@ struct BpLaunch {
     int* status;
 };
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
+// Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row}.
+cudaError_t launch_bp_batch(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n_items,
+                            cudaStream_t s);
+int bp_tile_x();
+int bp_tile_z();
 
 cudaError_t launch_align(const float* raw, float* out, const double* tinv /*[N][6]*/, const double* stats, int N,
                          int w, int h, int normalize, int fill, const unsigned char* identity, cudaStream_t s);
@@ -103,9 +108,22 @@ cudaError_t launch_diff(const float* meas, const int* tilts, const float* th, co
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s);
 cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s);
 int fp_max_tilts_per_cta(int w);
+int fp_qp(int w);
+int fp_choose_zc(int W);
+size_t fp_smem_bytes(int ZC, int W, int qp);
+// Batched forward projection: CTA b runs items[b] = {descriptor, first tilt, row, use_tma}.
+cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,
+                            cudaStream_t s);
 cudaError_t fp_init_attributes();
 cudaError_t misc_init_attributes();
 cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s);
+// Batched residual sums: problem b sums errpart[b][T_b][h_b] into err[b][T_b].
+struct ErrReduce {
+    const double* errpart;
+    double* err;
+    int T, h;
+};
+cudaError_t launch_reduce_err_batch(const ErrReduce* jobs, int n_jobs, int max_T, cudaStream_t s);
 cudaError_t launch_tv_p(const float* u, float* px, float* py, float* pz, int W, int H, int D, float theta, float g,
                         float dt, cudaStream_t s);
 cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* py, const float* pz, int W, int H,
