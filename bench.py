@@ -366,6 +366,8 @@ def run_engine(args, wl):
                "sample": f"{W}x{rows}x{D} rows of the workload, 1 WBP pass + 1 OS-SART iteration, {dt:.1f} s"}
 
     lib.tomo_destroy(h)
+    batched = None if args.no_extra else run_batched_leg(lib, args)
+    serving = None if args.no_extra else run_serving_leg(args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
@@ -378,11 +380,96 @@ def run_engine(args, wl):
             "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+            "batched": batched, "serving": serving,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batched_leg(lib, args):
+    """BASELINE config 3, bounded: 64 independent series (W in {256,384,512,768,1024}, H 64,
+    D in [64,256], 41/61/81/121 tilts over +/-50..70 deg in uniform, Saxton or dose-symmetric
+    order), SIRT iterations in one batched launch sequence per iteration (graph), against the
+    same handles run one by one."""
+    from tomoj_gb300 import phantom as P
+    g = np.random.Generator(np.random.PCG64(3))
+    handles, Ns, ups = [], [], 0
+    for m in range(64):
+        W = int(g.choice([256, 384, 512, 768, 1024]))
+        H, D, n = 64, int(g.integers(64, 257)), int(g.choice([41, 61, 81, 121]))
+        amax = float(g.uniform(50, 70))
+        scheme = int(g.integers(0, 3))
+        angles = (np.linspace(-amax, amax, n) if scheme == 0 else
+                  P.saxton_tilts(amax, n) if scheme == 1 else P.dose_symmetric_tilts(amax, n))
+        eul = euler_y(angles)
+        geo = _abi_mod().make_geom(W, H, D, W, H, n)
+        prm = _abi_mod().make_params()
+        h = C.c_void_p()
+        _abi_mod().check(lib.tomo_create(C.byref(geo), C.byref(prm), C.byref(h)))
+        yy, xx = np.mgrid[0:H, 0:W].astype(np.float32)
+        base = np.exp(-((xx - W / 2) ** 2) / (2 * (0.2 * W) ** 2)).astype(np.float32) * np.float32(0.3 * D)
+        ser = np.ascontiguousarray(np.broadcast_to(base, (n, H, W)), np.float32)
+        _abi_mod().check(lib.tomo_load_series(h, ser.ctypes.data, 0, _abi_mod().ptr(eul, C.c_double), None, None))
+        handles.append(h)
+        Ns.append(n)
+        ups += W * H * D * n
+    n_iter = 30
+    import torch
+    torch.cuda.synchronize()
+    for h in handles[:2]:
+        _abi_mod().check(lib.tomo_run_ossart(h, 1, 1.0, 0, 1, 0, 64, 1, None))
+    t0 = time.perf_counter()
+    for h in handles:
+        _abi_mod().check(lib.tomo_run_ossart(h, n_iter, 1.0, 0, 1, 0, 64, 1, None))
+    one = ups * n_iter / (time.perf_counter() - t0)
+    b = C.c_void_p()
+    _abi_mod().check(lib.tomo_batch_create(C.byref(b)))
+    arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
+    _abi_mod().check(lib.tomo_batch_set(b, arr, len(handles)))
+    rel = np.ones(len(handles))
+    upd = np.zeros(len(handles), np.int32)
+
+    def it(k):
+        first = np.array([lib.tomo_first_index(1, k, n) for n in Ns], np.int32)
+        _abi_mod().check(lib.tomo_batch_iteration(b, _abi_mod().ptr(rel, C.c_double), _abi_mod().ptr(upd, C.c_int32),
+                                                  _abi_mod().ptr(first, C.c_int32), 1, None))
+    it(0)
+    t0 = time.perf_counter()
+    for k in range(n_iter):
+        it(k)
+    bat = ups * n_iter / (time.perf_counter() - t0)
+    lib.tomo_batch_destroy(b)
+    for h in handles:
+        lib.tomo_destroy(h)
+    return {"workload": "64 heterogeneous series, SIRT, FP32", "iterations": n_iter,
+            "updates_per_iteration": ups, "voxel_updates_per_s": bat, "one_by_one_voxel_updates_per_s": one,
+            "speedup_vs_one_by_one": bat / one}
+
+
+def run_serving_leg(args):
+    """BASELINE config 5, bounded to args.serve_requests requests: Poisson arrivals (4/s) of
+    series of {512,1024,2048}^2 x {128,256,512} with {41,61,121} tilts, WBP 30 % / SIRT 40 % /
+    OS-SART 20 % / TVM 10 %, 5-50 iterations; continuous batching with HBM admission."""
+    from tomoj_gb300.serving import EngineAdapter, Server, summarize, synthetic_requests
+    reqs = synthetic_requests(args.serve_requests, seed=42)
+    eng = EngineAdapter()
+    try:
+        t0 = time.perf_counter()
+        res = Server(eng, max_active=64).run(reqs)
+        wall = time.perf_counter() - t0
+    finally:
+        eng.close()
+    s = summarize(res)
+    s["wall_s"] = wall
+    s["unit"] = "seconds (time to reconstruction)"
+    return s
+
+
+def _abi_mod():
+    from tomoj_gb300 import _abi
+    return _abi
 
 
 def main():
@@ -394,6 +481,8 @@ def main():
     ap.add_argument("--workload", default="ossart512", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving legs")
+    ap.add_argument("--serve-requests", type=int, default=16)
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
