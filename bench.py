@@ -159,11 +159,16 @@ def cpu_sample(wl, rows, threads, steps=1):
     return ups * steps / dt, dt, ups * steps
 
 
-def cpu_rows_for(wl, threads, target_s):
-    """Rows of the workload whose CPU sample takes about target_s seconds."""
-    rate, dt, _ = cpu_sample(wl, 4, threads)
-    per_row = dt / 4
-    return int(max(4, min(wl["H"], round(target_s / max(per_row, 1e-6)))))
+def cpu_plan(wl, threads, target_s):
+    """(rows, passes) of the workload whose CPU sample takes about target_s seconds:
+    calibrated on 16 rows (the per-tilt barriers make smaller samples unrepresentative),
+    capped at the whole volume, with repeated passes when the whole volume is faster."""
+    rows0 = min(16, wl["H"])
+    _, dt, _ = cpu_sample(wl, rows0, threads)
+    per_row = dt / rows0
+    rows = int(max(rows0, min(wl["H"], round(target_s / max(per_row, 1e-6)))))
+    passes = int(max(1, round(target_s / max(per_row * rows, 1e-6))))
+    return rows, passes
 
 
 def run_reference(args, wl):
@@ -171,17 +176,18 @@ def run_reference(args, wl):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    rows = cpu_rows_for(wl, threads, args.cpu_seconds)
+    # steps are bounded samples: about cpu_seconds / steps of CPU work each
+    rows, passes = cpu_plan(wl, threads, max(2.0, args.cpu_seconds / max(args.steps, 1)))
     for _ in range(args.warmup):
-        cpu_sample(wl, max(4, rows // 4), threads)
+        cpu_sample(wl, min(rows, 16), threads)
     vals, secs = [], 0.0
     for _ in range(args.steps):
-        rate, dt, _ = cpu_sample(wl, rows, threads)
+        rate, dt, _ = cpu_sample(wl, rows, threads, passes)
         vals.append(rate)
         secs += dt
     value = float(np.mean(vals))
-    sample = (f"{wl['W']}x{rows}x{wl['D']} rows of the workload: 1 WBP pass + 1 OS-SART iteration "
-              f"(update {wl['update']}) per step, {wl['n']} tilts")
+    sample = (f"{wl['W']}x{rows}x{wl['D']} rows of the workload: {passes} x (1 WBP pass + 1 OS-SART iteration "
+              f"(update {wl['update']})) per step, {wl['n']} tilts")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(args.steps, 1),
@@ -360,14 +366,16 @@ def run_engine(args, wl):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rows = cpu_rows_for(wl, threads, args.cpu_seconds)
-        rate, dt, ups = cpu_sample(wl, rows, threads)
+        rows, passes = cpu_plan(wl, threads, args.cpu_seconds)
+        rate, dt, ups = cpu_sample(wl, rows, threads, passes)
         cpu = {"value": rate, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
-               "sample": f"{W}x{rows}x{D} rows of the workload, 1 WBP pass + 1 OS-SART iteration, {dt:.1f} s"}
+               "sample": f"{W}x{rows}x{D} rows of the workload, {passes} x (1 WBP pass + 1 OS-SART iteration), "
+                         f"{dt:.1f} s"}
 
     lib.tomo_destroy(h)
     batched = None if args.no_extra else run_batched_leg(lib, args)
     serving = None if args.no_extra else run_serving_leg(args)
+    precision = None if args.no_extra else run_precision_leg(lib, args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
@@ -380,7 +388,7 @@ def run_engine(args, wl):
             "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-            "batched": batched, "serving": serving,
+            "batched": batched, "serving": serving, "precision": precision,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)
@@ -467,6 +475,117 @@ def run_serving_leg(args):
     return s
 
 
+def phantom_on_device(W, H, D, n_ell, seed, device):
+    """The seeded ellipsoid phantom of tomoj_gb300.phantom (same parameter draws),
+    evaluated on the GPU for volumes too large for the host generator."""
+    import math
+    import torch
+    from tomoj_gb300 import phantom as P
+    g = P.rng(seed)
+    vol = torch.zeros((D, H, W), dtype=torch.float32, device=device)
+    dims = np.array([W, H, D], np.float64)
+    for _ in range(n_ell):
+        axes = g.uniform(0.05, 0.25, 3) * dims
+        centre = np.clip(g.uniform(0.0, 1.0, 3) * (dims - 2 * axes) + axes, 0, dims - 1)
+        a, b, c = g.uniform(0, 2 * np.pi, 3)
+        ca, sa, cb, sb, cc, sc = math.cos(a), math.sin(a), math.cos(b), math.sin(b), math.cos(c), math.sin(c)
+        Rm = (np.array([[ca, -sa, 0], [sa, ca, 0], [0, 0, 1]]) @ np.array([[cb, 0, sb], [0, 1, 0], [-sb, 0, cb]])
+              @ np.array([[cc, -sc, 0], [sc, cc, 0], [0, 0, 1]])).astype(np.float32)
+        dens = float(g.uniform(0.0, 1.0))
+        r = float(np.max(axes)) + 1
+        x0, x1 = int(max(0, centre[0] - r)), int(min(W, centre[0] + r + 1))
+        y0, y1 = int(max(0, centre[1] - r)), int(min(H, centre[1] + r + 1))
+        z0, z1 = int(max(0, centre[2] - r)), int(min(D, centre[2] + r + 1))
+        if x0 >= x1 or y0 >= y1 or z0 >= z1:
+            continue
+        px = (torch.arange(x0, x1, device=device, dtype=torch.float32) - float(centre[0]))[None, None, :]
+        py = (torch.arange(y0, y1, device=device, dtype=torch.float32) - float(centre[1]))[None, :, None]
+        pz = (torch.arange(z0, z1, device=device, dtype=torch.float32) - float(centre[2]))[:, None, None]
+        q = 0
+        for k in range(3):
+            t = (float(Rm[0, k]) * px + float(Rm[1, k]) * py + float(Rm[2, k]) * pz) / float(axes[k])
+            q = q + t * t
+        vol[z0:z1, y0:y1, x0:x1] += (q <= 1.0).to(torch.float32) * dens
+    return vol
+
+
+def run_precision_leg(lib, args):
+    """BASELINE config 4, bounded: a 2048 x 512 x 2048 (W x H x D) phantom, 121 projections
+    of 2048 x 512 at -60..+60 deg in 1 deg steps with Poisson noise at 50 e-/px; SIRT
+    iterations with the volume stored in FP32, BF16 and FP16 (per-row slab scales,
+    Kahan-compensated FP32 backprojection sums, FP64 residual norms).  Reports each
+    form's voxel-updates/s and the reduced forms' relative L2 against the FP32 form
+    after the same iterations (against the FP64 oracle: tests/test_precision_gpu.py)."""
+    import torch
+    from tomoj_gb300 import _abi
+    from tomoj_gb300 import phantom as P
+    W, H, D = args.prec_size
+    n = 121
+    angles = np.linspace(-60.0, 60.0, n)
+    eul = euler_y(angles)
+    stream = torch.cuda.current_stream()
+    t0 = time.time()
+    vol = phantom_on_device(W, H, D, P.n_ellipsoids_for(W, H, D), 1238, "cuda")
+
+    def create(prec):
+        g = _abi.make_geom(W, H, D, W, H, n)
+        p = _abi.make_params(fill=_abi.FILL_NAN, precision=prec)
+        h = C.c_void_p()
+        _abi.check(lib.tomo_create(C.byref(g), C.byref(p), C.byref(h)))
+        _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        return h
+
+    # tilt-series: the engine's FP32 forward projection of the phantom, then Poisson noise
+    h = create(_abi.PREC_FP32)
+    series = np.empty((n, H, W), np.float32)
+    try:
+        _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+        torch.cuda.synchronize()
+        _abi.check(lib.tomo_set_volume(h, C.c_void_p(vol.data_ptr()), 1, 0, H))
+        for i in range(n):
+            _abi.check(lib.tomo_add_projection(h, i))
+        _abi.check(lib.tomo_project(h, 0, H))
+        for i in range(n):
+            _abi.check(lib.tomo_get_projection(h, i, _abi.ptr(series[i])))
+    finally:
+        lib.tomo_destroy(h)
+    del vol
+    torch.cuda.empty_cache()
+    series = P.add_poisson_noise(np.nan_to_num(series), 50.0, 1239)
+    log(f"[bench] precision inputs ready in {time.time() - t0:.1f}s")
+    nvox = W * H * D
+    iters = args.prec_iters
+    out, vols = {}, {}
+    for name, prec in (("fp32", _abi.PREC_FP32), ("bf16", _abi.PREC_BF16), ("fp16", _abi.PREC_FP16)):
+        h = create(prec)
+        try:
+            _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+            _abi.check(lib.tomo_run_ossart(h, 1, 1.0, 0, 5, 0, H, 1, None))  # warm-up (graph, tables)
+            _abi.check(lib.tomo_fill_volume(h, 0.0))
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            _abi.check(lib.tomo_run_ossart(h, iters, 1.0, 0, 5, 0, H, 1, None))
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            v = np.empty((D, H, W), np.float32)
+            _abi.check(lib.tomo_get_volume(h, v.ctypes.data, 0, 0, H))
+            vols[name] = v
+            out[name] = {"voxel_updates_per_s": nvox * n * iters / (ms / 1000.0), "ms_per_iteration": ms / iters,
+                         "volume_bytes": nvox * (4 if prec == _abi.PREC_FP32 else 2)}
+        finally:
+            lib.tomo_destroy(h)
+    ref = vols["fp32"].astype(np.float64)
+    den = float(np.linalg.norm(ref))
+    for name in ("bf16", "fp16"):
+        out[name]["rel_l2_vs_fp32"] = float(np.linalg.norm(vols[name] - ref) / den)
+        out[name]["speedup_vs_fp32"] = out[name]["voxel_updates_per_s"] / out["fp32"]["voxel_updates_per_s"]
+    out["workload"] = f"{W}x{H}x{D} phantom, {n} tilts of {W}x{H}, Poisson 50 e-/px, SIRT"
+    out["iterations"] = iters
+    return out
+
+
 def _abi_mod():
     from tomoj_gb300 import _abi
     return _abi
@@ -481,8 +600,11 @@ def main():
     ap.add_argument("--workload", default="ossart512", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving legs")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched, serving and precision legs")
     ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--prec-size", type=int, nargs=3, default=[2048, 512, 2048], metavar=("W", "H", "D"),
+                    help="volume of the reduced-precision leg")
+    ap.add_argument("--prec-iters", type=int, default=3)
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -55,8 +55,13 @@ typedef int32_t tomo_status;
 #define TOMO_WEIGHT_RAMP 2
 #define TOMO_WEIGHT_HAMMING_RAMP 3
 
-/* Storage precision of the volume (accumulation is always FP32). */
+/* Storage precision of the volume (accumulation is always FP32).  BF16 and FP16
+ * keep each volume row (an XZ slab) as value / scale in 16 bits with a per-row
+ * power-of-two scale; backprojection sums are Kahan-compensated FP32 and residual
+ * norms FP64.  These modes have no counterpart in the reference (float volumes). */
 #define TOMO_PREC_FP32 0
+#define TOMO_PREC_BF16 1
+#define TOMO_PREC_FP16 2
 
 typedef struct tomo_geom {
     int32_t W, H, D;        /* volume width (x), height (y: tilt-axis rows), depth (z) */

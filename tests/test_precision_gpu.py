@@ -1,0 +1,229 @@
+"""Reduced-precision volume storage (BF16 / FP16 with per-row slab scales).
+
+The volume is stored in 16 bits as value / scale[r] per volume row r; every
+arithmetic step stays FP32 (Kahan-compensated backprojection sums) and residual
+norms FP64.  Tolerances:
+
+* FP16 storage: <= 1e-3 relative L2 against the FP64 oracle after 10 SIRT
+  iterations (the format keeps 11 significant bits: rounding alone is ~1.4e-4).
+* BF16 storage: 8 significant bits, so rounding a volume once already costs
+  ~1.1e-3 to 1.6e-3 relative L2, and every iteration re-rounds it (measured on a
+  GB300: 4.0e-3 after 10 SIRT iterations).  BF16 therefore does not meet the
+  1e-3 target; its bound here is 6e-3 and FP16 is the storage that meets it.
+* A forward projection of a reduced volume is bit-identical to the FP32 forward
+  projection of the same values (power-of-two scales commute with rounding).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import np_oracle as N
+from oracle import oracle as O
+from tests.cases import rel_l2, series_case
+from tomoj_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+PRECS = {"bf16": _abi.PREC_BF16, "fp16": _abi.PREC_FP16}
+ULP_REL = {"bf16": 2.0 ** -8, "fp16": 2.0 ** -11}  # bound on |x - round(x)| / |x| (half an ulp, doubled)
+TOL_SIRT10 = {"bf16": 6e-3, "fp16": 1e-3}
+
+
+class RHandle:
+    def __init__(self, lib, case, precision):
+        self.lib, self.c = lib, case
+        g = _abi.make_geom(case["W"], case["H"], case["D"], case["w"], case["h"], case["n"])
+        p = _abi.make_params(precision=precision)
+        h = C.c_void_p()
+        _abi.check(lib.tomo_create(C.byref(g), C.byref(p), C.byref(h)))
+        self.h = h
+        eul = np.ascontiguousarray(case["eul"], np.float64)
+        T = np.ascontiguousarray(case["T"], np.float64)
+        series = np.ascontiguousarray(case["series"], np.float32)
+        _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double),
+                                        _abi.ptr(T, C.c_double), None))
+
+    def set_volume(self, vol):
+        v = np.ascontiguousarray(vol, np.float32)
+        _abi.check(self.lib.tomo_set_volume(self.h, v.ctypes.data, 0, 0, v.shape[1]))
+
+    def volume(self):
+        c = self.c
+        out = np.empty((c["D"], c["H"], c["W"]), np.float32)
+        _abi.check(self.lib.tomo_get_volume(self.h, out.ctypes.data, 0, 0, c["H"]))
+        return out
+
+    def sirt(self, n_iter, seed, update=0, graph=1):
+        err = np.zeros((n_iter, 5))
+        _abi.check(self.lib.tomo_run_ossart(self.h, n_iter, 1.0, update, seed, 0, self.c["H"], graph,
+                                            _abi.ptr(err, C.c_double)))
+        return err
+
+    def close(self):
+        self.lib.tomo_destroy(self.h)
+
+
+def _aligned(case):
+    return np.array([O.align(case["series"][i], case["T"][i], fill=O.FILL_NAN) for i in range(case["n"])],
+                    np.float32)
+
+
+@pytest.mark.parametrize("name", sorted(PRECS))
+def test_reduced_volume_roundtrip_uses_slab_scales(engine, name):
+    c = series_case(W=40, H=9, D=24, n=5, seed=3, noise=0.0)
+    rng = np.random.default_rng(11)
+    vol = rng.uniform(-1.0, 1.0, (c["D"], c["H"], c["W"])).astype(np.float32)
+    # rows far outside FP16's native range (1e-7 .. 1e6) must survive through their scales
+    mags = np.array([1e-7, 1e-4, 1e-2, 1.0, 3.0, 1e2, 1e4, 1e6, 0.0], np.float32)
+    vol *= mags[None, :, None]
+    hd = RHandle(engine, c, PRECS[name])
+    try:
+        hd.set_volume(vol)
+        got = hd.volume()
+        nz = vol != 0
+        rel = np.abs(got[nz] - vol[nz]) / np.abs(vol[nz])
+        assert np.all(got[~nz] == 0)
+        assert rel.max() <= ULP_REL[name], rel.max()
+        # the volume pointer is not exposed for 16-bit storage
+        ptr = C.c_void_p()
+        assert engine.tomo_volume_device_ptr(hd.h, C.byref(ptr)) == _abi.ERR_UNSUPPORTED
+    finally:
+        hd.close()
+
+
+@pytest.mark.parametrize("name", sorted(PRECS))
+def test_reduced_forward_projection_is_bitwise_fp32_of_stored_values(engine, name):
+    c = series_case(W=64, H=8, D=40, n=9, seed=5)
+    red = RHandle(engine, c, PRECS[name])
+    ref = RHandle(engine, c, _abi.PREC_FP32)
+    try:
+        red.set_volume(c["vol"] * 3.7)
+        stored = red.volume()  # the values the reduced volume holds
+        ref.set_volume(stored)
+        for hd in (red, ref):
+            _abi.check(engine.tomo_clear_projections(hd.h))
+            for i in range(c["n"]):
+                _abi.check(engine.tomo_add_projection(hd.h, i))
+            _abi.check(engine.tomo_project(hd.h, 0, c["H"]))
+        for i in range(c["n"]):
+            a = np.empty((c["h"], c["w"]), np.float32)
+            b = np.empty_like(a)
+            _abi.check(engine.tomo_get_projection(red.h, i, _abi.ptr(a)))
+            _abi.check(engine.tomo_get_projection(ref.h, i, _abi.ptr(b)))
+            assert np.array_equal(a, b, equal_nan=True)
+    finally:
+        red.close()
+        ref.close()
+
+
+@pytest.mark.parametrize("name", sorted(PRECS))
+def test_reduced_sirt_10_against_fp64_oracle(engine, name):
+    c = series_case(W=64, H=8, D=48, n=21, seed=21)
+    n_iter, seed = 10, 99
+    hd = RHandle(engine, c, PRECS[name])
+    f32 = RHandle(engine, c, _abi.PREC_FP32)
+    try:
+        err = hd.sirt(n_iter, seed)
+        got = hd.volume()
+        f32.sirt(n_iter, seed)
+        got32 = f32.volume()
+        meas = _aligned(c)
+        ref = np.zeros(c["vol"].shape, np.float64)
+        errs = []
+        for it in range(n_iter):
+            order = O.order_shuffle(c["eul"], int(engine.tomo_first_index(seed, it, c["n"])))
+            errs.append(N.ossart_iteration(ref, c["g"], c["eul"], meas, order, 1.0, 0))
+        errs = np.array(errs)
+        e64 = rel_l2(got, ref)
+        e32 = rel_l2(got, got32)
+        print(f"{name}: rel-L2 vs FP64 oracle {e64:.3e}, vs FP32 engine {e32:.3e}, "
+              f"FP32 engine vs FP64 {rel_l2(got32, ref):.3e}")
+        assert e64 <= TOL_SIRT10[name], e64
+        # residual norms (FP64 reductions) follow the oracle's
+        assert np.allclose(err[:, 0], errs[:, 0], rtol=10 * TOL_SIRT10[name])
+    finally:
+        hd.close()
+        f32.close()
+
+
+def test_fp16_overflow_of_a_slab_is_reported(engine):
+    # rows hold ~1e-3 (slab scale 2^-14); measurements of ~1e6 push one update past
+    # 65504 * 2^-14 = 4.0, which the backprojector must report (the slab saturates)
+    c = series_case(W=32, H=4, D=16, n=5, seed=9, noise=0.0)
+    c = dict(c)
+    c["series"] = np.full_like(c["series"], 1.0e6)
+    hd = RHandle(engine, c, _abi.PREC_FP16)
+    try:
+        hd.set_volume(np.full(c["vol"].shape, 1.0e-3, np.float32))
+        st = engine.tomo_run_ossart(hd.h, 1, 1.0, 0, 1, 0, c["H"], 0, None)
+        assert st == _abi.ERR_DEVICE
+        assert b"FP16" in engine.tomo_last_error()
+        # the handle stays usable: BF16 has the range, and a fresh FP16 volume of the
+        # right magnitude iterates without error
+        hd.set_volume(np.full(c["vol"].shape, 1.0e3, np.float32))
+        _abi.check(engine.tomo_run_ossart(hd.h, 1, 1.0, 0, 1, 0, c["H"], 0, None))
+    finally:
+        hd.close()
+    hb = RHandle(engine, c, _abi.PREC_BF16)
+    try:
+        hb.set_volume(np.full(c["vol"].shape, 1.0e-3, np.float32))
+        _abi.check(engine.tomo_run_ossart(hb.h, 1, 1.0, 0, 1, 0, c["H"], 0, None))
+        assert np.all(np.isfinite(hb.volume()))
+    finally:
+        hb.close()
+
+
+def test_reduced_tvm_against_fp64_oracle(engine):
+    c = series_case(W=40, H=8, D=24, n=11, seed=8)
+    hd = RHandle(engine, c, _abi.PREC_FP16)
+    try:
+        _abi.check(engine.tomo_set_tvm(hd.h, 25.0, 1.0, 0.01, 5))
+        hd.sirt(2, 3)
+        got = hd.volume()
+        meas = _aligned(c)
+        ref = np.zeros(c["vol"].shape, np.float64)
+        for it in range(2):
+            order = O.order_shuffle(c["eul"], int(engine.tomo_first_index(3, it, c["n"])))
+            N.ossart_iteration(ref, c["g"], c["eul"], meas, order, 1.0, 0)
+            ref[...] = N.tv_denoise(ref, 25.0, 1.0, 0.01, 5)
+        assert rel_l2(got, ref) <= 1e-3, rel_l2(got, ref)
+        # FISTA momentum needs the FP32 volume
+        assert engine.tomo_set_fista(hd.h, 1) == _abi.ERR_UNSUPPORTED
+    finally:
+        hd.close()
+
+
+def test_reduced_batch_matches_one_by_one(engine):
+    cases = [series_case(W=48, H=6, D=32, n=11, seed=31), series_case(W=64, H=5, D=40, n=13, seed=32)]
+    precs = (_abi.PREC_FP16, _abi.PREC_BF16)
+    seeds = (7, 8)
+    n_iter = 3
+    solo = []
+    for c, prec, sd in zip(cases, precs, seeds):
+        hd = RHandle(engine, c, prec)
+        try:
+            hd.sirt(n_iter, sd)
+            solo.append(hd.volume())
+        finally:
+            hd.close()
+    hs = [RHandle(engine, c, prec) for c, prec in zip(cases, precs)]
+    b = C.c_void_p()
+    _abi.check(engine.tomo_batch_create(C.byref(b)))
+    try:
+        arr = (C.c_void_p * len(hs))(*[x.h.value for x in hs])
+        _abi.check(engine.tomo_batch_set(b, arr, len(hs)))
+        rel = np.ones(len(hs))
+        upd = np.zeros(len(hs), np.int32)
+        for it in range(n_iter):
+            first = np.array([engine.tomo_first_index(sd, it, c["n"]) for sd, c in zip(seeds, cases)], np.int32)
+            _abi.check(engine.tomo_batch_iteration(b, _abi.ptr(rel, C.c_double), _abi.ptr(upd, C.c_int32),
+                                                   _abi.ptr(first, C.c_int32), 1, None))
+        for x, ref in zip(hs, solo):
+            assert np.array_equal(x.volume(), ref)
+    finally:
+        engine.tomo_batch_destroy(b)
+        for x in hs:
+            x.close()

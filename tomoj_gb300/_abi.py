@@ -22,6 +22,8 @@ ERRORS = {
 FILL_NONE, FILL_AVG, FILL_NAN = 0, 1, 2
 WEIGHT_NONE, WEIGHT_RADERMACHER, WEIGHT_RAMP, WEIGHT_HAMMING_RAMP = 0, 1, 2, 3
 PREC_FP32 = 0
+PREC_BF16 = 1
+PREC_FP16 = 2
 
 
 class TomoError(RuntimeError):
@@ -125,6 +127,10 @@ def load():
     return _lib
 
 
+OK = 0
+ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED, ERR_CANCELLED, ERR_DEVICE = -1, -2, -3, -4, -5, -6, -7
+
+
 def check(rc: int) -> None:
     if rc != TOMO_OK:
         msg = load().tomo_last_error().decode(errors="replace")
@@ -145,6 +151,16 @@ def make_geom(W, H, D, w, h, nproj, vol_center=None, proj_center=None, scale=1.0
     g.proj_center = (C.c_double * 4)(*pc)
     g.scale = scale
     return g
+
+
+def precision_code(v) -> int:
+    """PREC_* value of "fp32" / "bf16" / "fp16" (or of an int)."""
+    if isinstance(v, str):
+        names = {"fp32": PREC_FP32, "f32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16, "f16": PREC_FP16}
+        if v.lower() not in names:
+            raise ValueError(f"unknown precision {v!r}")
+        return names[v.lower()]
+    return int(v)
 
 
 def make_params(positivity=False, long_object=False, fill=FILL_NAN, normalize=False, precision=PREC_FP32) -> Params:

@@ -42,6 +42,7 @@ struct tomo_batch {
     struct BpSeg {
         int s;
         bool sanitize, pos;
+        int vt;
         int off, n;
     };
     struct RedSeg {
@@ -103,10 +104,10 @@ tomo_status build_plan(tomo_batch* b) {
     std::vector<FpLaunch> fp;
     std::vector<BpLaunch> bp;
     std::vector<ErrReduce> red;
-    // work items grouped by (s, qp, zc) for FP and (s, sanitize, pos) for BP
+    // work items grouped by (s, qp, zc) for FP and (s, sanitize, pos, storage type) for BP
     std::map<std::tuple<int, int, int>, std::vector<int4>> fpi;
     std::map<std::tuple<int, int, int>, size_t> fpsmem;
-    std::map<std::tuple<int, int, int>, std::vector<int4>> bpi;
+    std::map<std::tuple<int, int, int, int>, std::vector<int4>> bpi;
     std::map<int, std::vector<ErrReduce>> reds;
     b->max_nsub = 0;
     b->has_fista = false;
@@ -122,14 +123,16 @@ tomo_status build_plan(tomo_batch* b) {
         BCK(cudaMemsetAsync(p->d_errpart, 0, sizeof(double) * (size_t)N * g.h, b->stream));
         const int qp = fp_qp(g.w);
         const int zc = fp_choose_zc(g.W);
-        const int use_tma = (g.W % 4 == 0) && ((reinterpret_cast<uintptr_t>(p->d_vol) & 15) == 0);
+        const int use_tma = fp_use_tma(g.W, p->vtype, p->vol());
         const int offset = (g.h > g.H && g.scale == 1) ? (g.h - g.H) / 2 : 0;
         const int j0 = std::max(0, (int)std::floor(offset * g.scale + 0.5));
         for (int s = 0; s < nsub; s++) {
             const int T = std::min(upd, N - s * upd);
             const int slot = s * upd;
             FpLaunch a{};
-            a.vol = p->d_vol;
+            a.vol = p->vol();
+            a.vtype = p->vtype;
+            a.vscale = p->vtype == kVolF32 ? nullptr : p->d_vscale;
             a.meas = p->d_meas;
             a.tilts = p->d_batch + slot;
             a.T = T;
@@ -159,7 +162,10 @@ tomo_status build_plan(tomo_batch* b) {
                 for (int j = j0; j < g.h; j++) items.push_back(make_int4(di, g0, j, use_tma));
             reds[s].push_back(ErrReduce{a.errpart, p->d_err + slot, T, g.h});
             BpLaunch c{};
-            c.vol = p->d_vol;
+            c.vol = p->vol();
+            c.vtype = p->vtype;
+            c.vscale = p->d_vscale;
+            c.vmax = p->d_vmax;
             c.img = a.diff;
             c.tilts = a.tilts;
             c.T = T;
@@ -178,7 +184,7 @@ tomo_status build_plan(tomo_batch* b) {
             c.status = p->d_status;
             const int bi = (int)bp.size();
             bp.push_back(c);
-            auto& bitems = bpi[std::make_tuple(s, c.sanitize, c.positivity)];
+            auto& bitems = bpi[std::make_tuple(s, c.sanitize, c.positivity, c.vtype)];
             for (int r = 0; r < g.H; r++) {
                 const int jp = r + g.bp_row_off;
                 if (jp < 0 || jp >= g.h) continue;
@@ -200,7 +206,7 @@ tomo_status build_plan(tomo_batch* b) {
     }
     for (auto& kv : bpi) {
         tomo_batch::BpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first) != 0, std::get<2>(kv.first) != 0,
-                             (int)bp_all.size(), (int)kv.second.size()};
+                             std::get<3>(kv.first), (int)bp_all.size(), (int)kv.second.size()};
         bp_all.insert(bp_all.end(), kv.second.begin(), kv.second.end());
         b->bp_segs.push_back(sg);
     }
@@ -238,8 +244,11 @@ tomo_status launch_step(tomo_batch* b) {
                 BCK(launch_fp_batch(sg.qp, b->d_fp, b->d_fp_items + sg.off, sg.n, sg.zc, sg.smem, b->stream));
         for (auto& sg : b->red_segs)
             if (sg.s == s) BCK(launch_reduce_err_batch(b->d_red + sg.off, sg.n, sg.maxT, b->stream));
+        for (tomo_projector* p : b->members) BCKS(handle_bp_pre(p, b->stream));
         for (auto& sg : b->bp_segs)
-            if (sg.s == s) BCK(launch_bp_batch(sg.sanitize, sg.pos, b->d_bp, b->d_bp_items + sg.off, sg.n, b->stream));
+            if (sg.s == s)
+                BCK(launch_bp_batch(sg.sanitize, sg.pos, sg.vt, b->d_bp, b->d_bp_items + sg.off, sg.n, b->stream));
+        for (tomo_projector* p : b->members) BCKS(handle_bp_post(p, b->stream));
     }
     for (tomo_projector* p : b->members) BCKS(handle_end_iteration(p));
     return TOMO_OK;

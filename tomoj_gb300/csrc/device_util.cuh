@@ -5,10 +5,9 @@
 
 #include <cuda_runtime.h>
 
-namespace tomo {
+#include "tomo_internal.h"
 
-// Device status word bits written by kernels (never trap: the host reads them).
-constexpr int kStatusTimeout = 1;  // an mbarrier wait exceeded its iteration budget
+namespace tomo {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));

@@ -24,6 +24,7 @@
 
 #include "device_util.cuh"
 #include "tomo_internal.h"
+#include "vol_storage.cuh"
 
 namespace tomo {
 namespace fpk {
@@ -88,6 +89,39 @@ __device__ __forceinline__ void build_pairs_row(const float* __restrict__ src, f
     }
 }
 
+// The same pairs from a row stored in 16 bits (reduced-precision volume; the slab
+// scale is applied to the finished ray sum).
+template <int VT>
+__device__ __forceinline__ void build_pairs_row16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W,
+                                                  bool flat) {
+    const int tid = threadIdx.x;
+    if ((W & 3) == 0) {
+        for (int m = tid; m < W / 4; m += kThreads) {
+            const uint2 u = *reinterpret_cast<const uint2*>(src + 4 * m);
+            const float vx = vol_load16<VT>((uint16_t)(u.x & 0xFFFFu)), vy = vol_load16<VT>((uint16_t)(u.x >> 16));
+            const float vz = vol_load16<VT>((uint16_t)(u.y & 0xFFFFu)), vw = vol_load16<VT>((uint16_t)(u.y >> 16));
+            const float nx = (4 * m + 4 < W) ? vol_load16<VT>(src[4 * m + 4]) : vw;
+            float d0 = vy - vx, d1 = vz - vy, d2 = vw - vz, d3 = nx - vw;
+            if (flat) d0 = d1 = d2 = d3 = 0.0f;
+            float4* o = reinterpret_cast<float4*>(dst + 4 * m + 2);
+            o[0] = make_float4(vx - d0, d0, vy - d1, d1);
+            o[1] = make_float4(vz - d2, d2, vw - d3, d3);
+        }
+    } else {
+        for (int k = tid; k < W; k += kThreads) {
+            const float v = vol_load16<VT>(src[k]);
+            float d = (k + 1 < W) ? vol_load16<VT>(src[k + 1]) - v : 0.0f;
+            if (flat) d = 0.0f;
+            dst[k + 2] = make_float2(v - d, d);
+        }
+    }
+    if (tid < 4) {
+        const int k = (tid < 2) ? tid - 2 : W + tid - 2;  // -2, -1, W, W+1
+        const float v = vol_load16<VT>(src[(tid < 2) ? 0 : W - 1]);
+        dst[k + 2] = make_float2(v, 0.0f);
+    }
+}
+
 __device__ __forceinline__ float sample(const float2* __restrict__ P, long long x) {
     const float2 p = P[(int)(x >> 32)];
     return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
@@ -141,20 +175,29 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
         const int nchunks = (D + ZC - 1) / ZC;
         const bool last_row = (r == H - 1);
         const long long pitch = (long long)PW << 32;  // one pair row in position units
-        auto stage = [&](int c) {                     // chunk c -> raw
+        const int vt = a.vtype;
+        const uint32_t rowb = (uint32_t)(W * vol_elem_bytes(vt));  // bytes of one plane row
+        const unsigned char* volb = static_cast<const unsigned char*>(a.vol);
+        unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
+        auto stage = [&](int c) {  // chunk c -> raw
             const int z0 = c * ZC, zn = min(ZC, D - z0);
             if (use_tma) {
                 if (tid == 0) {
                     fence_proxy_async();
-                    mbar_arrive_expect_tx(bar, (uint32_t)(zn * W * sizeof(float)));
+                    mbar_arrive_expect_tx(bar, (uint32_t)zn * rowb);
                     for (int zz = 0; zz < zn; zz++)
-                        tma_load_1d(raw + (size_t)zz * W, a.vol + ((size_t)(z0 + zz) * H + r) * W,
-                                    W * sizeof(float), bar);
+                        tma_load_1d(rawb + (size_t)zz * rowb, volb + ((size_t)(z0 + zz) * H + r) * rowb, rowb, bar);
+                }
+            } else if (vt == kVolF32) {
+                for (int zz = 0; zz < zn; zz++) {
+                    const float* src = reinterpret_cast<const float*>(volb + ((size_t)(z0 + zz) * H + r) * rowb);
+                    for (int k = tid; k < W; k += kThreads) raw[(size_t)zz * W + k] = src[k];
                 }
             } else {
+                uint16_t* raw16 = reinterpret_cast<uint16_t*>(raw);
                 for (int zz = 0; zz < zn; zz++) {
-                    const float* src = a.vol + ((size_t)(z0 + zz) * H + r) * W;
-                    for (int k = tid; k < W; k += kThreads) raw[(size_t)zz * W + k] = src[k];
+                    const uint16_t* src = reinterpret_cast<const uint16_t*>(volb + ((size_t)(z0 + zz) * H + r) * rowb);
+                    for (int k = tid; k < W; k += kThreads) raw16[(size_t)zz * W + k] = src[k];
                 }
             }
         };
@@ -180,7 +223,14 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             }
             for (int zz = 0; zz < zc; zz++) {
                 const bool flat = last_row || (z0 + zz == D - 1);  // raw floor voxel on the last row / plane
-                build_pairs_row(raw + (size_t)zz * W, pairs + (size_t)zz * PW, W, flat);
+                if (vt == kVolF32)
+                    build_pairs_row(raw + (size_t)zz * W, pairs + (size_t)zz * PW, W, flat);
+                else if (vt == kVolBF16)
+                    build_pairs_row16<kVolBF16>(reinterpret_cast<const uint16_t*>(raw) + (size_t)zz * W,
+                                                pairs + (size_t)zz * PW, W, flat);
+                else
+                    build_pairs_row16<kVolF16>(reinterpret_cast<const uint16_t*>(raw) + (size_t)zz * W,
+                                               pairs + (size_t)zz * PW, W, flat);
             }
             __syncthreads();
             if (c + 1 < nchunks && use_tma) stage(c + 1);
@@ -239,6 +289,8 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
 
     // Epilogue: projection, norm, residual.
     const int lane = tid & 31, warp = tid >> 5;
+    // reduced storage: ray sums are in units of the row's slab scale (a power of two)
+    const double vsc = (a.vscale != nullptr && row_in) ? (double)a.vscale[r] : 1.0;
 #pragma unroll
     for (int t = 0; t < TGMAX; t++) {
         if (t >= TG) break;
@@ -255,7 +307,8 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 th = __int_as_float(0x7fc00000);
                 nrm = 0.0f;
             } else {
-                th = __double2float_rn((double)acc[t * QP + q] * ninc);
+                th = (a.vscale != nullptr) ? __double2float_rn((double)acc[t * QP + q] * vsc * ninc)
+                                           : __double2float_rn((double)acc[t * QP + q] * ninc);
                 nrm = a.rays[(size_t)tilt * w + i].norm;
             }
             const size_t o = ((size_t)(g0 + t) * h + j) * w + i;
@@ -330,7 +383,7 @@ cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     const int ZC = choose_zc(a.W);
     const Smem L = layout(ZC, a.W, 16 / QP);
     if (L.total > kMaxSmem) return cudaErrorInvalidValue;
-    const int use_tma = (a.W % 4 == 0) && ((reinterpret_cast<uintptr_t>(a.vol) & 15) == 0);
+    const int use_tma = fp_use_tma(a.W, a.vtype, a.vol);
     dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0);
     switch (ZC) {
         case 16: fp_kernel<QP, 16><<<grid, kThreads, L.total, s>>>(a, use_tma); break;

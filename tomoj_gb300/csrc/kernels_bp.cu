@@ -18,6 +18,7 @@
 
 #include "device_util.cuh"
 #include "tomo_internal.h"
+#include "vol_storage.cuh"
 
 namespace tomo {
 namespace {
@@ -58,8 +59,36 @@ __device__ __forceinline__ void bp_add(float& vox, float val) {
     }
 }
 
-// One CTA's work: tile (x0, z0) of volume row r of problem `a`.
+// Reduced-precision storage: Kahan-compensated FP32 sum (comp carries the
+// running rounding error); the reference's per-add NaN/Inf and positivity rules
+// act on the compensated sum and reset the compensation.
 template <bool SANITIZE, bool POS>
+__device__ __forceinline__ void bp_add_kahan(float& vox, float& comp, float val) {
+    if (SANITIZE && isnan(val)) return;
+    const float y = val - comp;
+    float t = vox + y;
+    comp = (t - vox) - y;
+    if (SANITIZE && (isnan(t) || isinf(t))) {
+        t = 0.0f;
+        comp = 0.0f;
+    }
+    if (POS && t < 0.0f) {
+        t = 0.0f;
+        comp = 0.0f;
+    }
+    vox = t;
+}
+
+template <bool SANITIZE, bool POS, int VT>
+__device__ __forceinline__ void bp_acc(float& vox, float& comp, float val) {
+    if (VT == kVolF32)
+        bp_add<SANITIZE, POS>(vox, val);
+    else
+        bp_add_kahan<SANITIZE, POS>(vox, comp, val);
+}
+
+// One CTA's work: tile (x0, z0) of volume row r of problem `a`.
+template <bool SANITIZE, bool POS, int VT>
 __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const int z0, const int r) {
     __shared__ __align__(16) BpShared sh;
     const int tid = threadIdx.x;
@@ -73,11 +102,21 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
     const bool xin = x < W;
 
     const size_t plane = (size_t)H * W;
-    float* vb = a.vol + ((size_t)zs * H + r) * W + x;  // voxel (x, r, zs); voxel k is vb[k * plane]
+    const size_t v0 = ((size_t)zs * H + r) * W + x;  // voxel (x, r, zs); voxel k is at v0 + k * plane
     const int nk = xin ? min(kKZ, D - zs) : 0;
-    float vox[kKZ];
+    float vox[kKZ], comp[kKZ];
+    const float vsc = (VT == kVolF32) ? 1.0f : a.vscale[r];
+    if (VT == kVolF32) {
+        const float* vb = static_cast<const float*>(a.vol) + v0;
 #pragma unroll
-    for (int k = 0; k < kKZ; k++) vox[k] = (k < nk) ? vb[k * plane] : 0.0f;
+        for (int k = 0; k < kKZ; k++) vox[k] = (k < nk) ? vb[k * plane] : 0.0f;
+    } else {
+        const uint16_t* vb = static_cast<const uint16_t*>(a.vol) + v0;
+#pragma unroll
+        for (int k = 0; k < kKZ; k++) vox[k] = (k < nk) ? vol_load16<VT>(vb[k * plane]) * vsc : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < kKZ; k++) comp[k] = 0.0f;
 
     const int xa = x0, xb = min(x0 + kTX - 1, W - 1);
     const int za = z0, zb = min(z0 + kTZ - 1, D - 1);
@@ -170,8 +209,9 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
                 for (int k = 0; k < kKZ; k += 2) {
                     const float2 p0 = sh.seg[(int)(X >> 32)];
                     const float2 p1 = sh.seg[(int)(X1 >> 32)];
-                    bp_add<SANITIZE, POS>(vox[k], fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x));
-                    bp_add<SANITIZE, POS>(vox[k + 1], fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x));
+                    bp_acc<SANITIZE, POS, VT>(vox[k], comp[k], fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x));
+                    bp_acc<SANITIZE, POS, VT>(vox[k + 1], comp[k + 1],
+                                              fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x));
                     X += S2;
                     X1 += S2;
                 }
@@ -180,7 +220,7 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
                 for (int k = 0; k < kKZ; k++) {
                     if ((unsigned)(k - kl) < (unsigned)cnt) {
                         const float2 p = sh.seg[(int)(X >> 32)];
-                        bp_add<SANITIZE, POS>(vox[k], fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x));
+                        bp_acc<SANITIZE, POS, VT>(vox[k], comp[k], fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x));
                     }
                     X += S;
                 }
@@ -189,22 +229,76 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
         __syncthreads();
     }
 
+    if (VT == kVolF32) {
+        float* vb = static_cast<float*>(a.vol) + v0;
 #pragma unroll
-    for (int k = 0; k < kKZ; k++)
-        if (k < nk) vb[k * plane] = vox[k];
+        for (int k = 0; k < kKZ; k++)
+            if (k < nk) vb[k * plane] = vox[k];
+    } else {
+        // store value / scale (exact: power of two) and feed the row maximum for re-scaling
+        uint16_t* vb = static_cast<uint16_t*>(a.vol) + v0;
+        const float inv = 1.0f / vsc;
+        float m = 0.0f;
+        bool range = false;
+#pragma unroll
+        for (int k = 0; k < kKZ; k++) {
+            if (k < nk) {
+                const float v = vox[k] - comp[k];
+                m = fmaxf(m, fabsf(v));
+                float q = v * inv;
+                if (VT == kVolF16 && fabsf(q) > kF16Max && isfinite(q)) {
+                    range = true;  // reported through the status word; the slab saturates
+                    q = copysignf(kF16Max, q);
+                }
+                vb[k * plane] = vol_store16<VT>(q);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((tid & 31) == 0 && m > 0.0f) atomicMax(a.vmax + r, __float_as_uint(m));
+        if (range) atomicOr(a.status, (int)kStatusRange);
+    }
 }
 
-template <bool SANITIZE, bool POS>
-__global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS) bp_separable_kernel(const __grid_constant__ BpLaunch a) {
-    bp_body<SANITIZE, POS>(a, blockIdx.x * kTX, blockIdx.y * kTZ, a.y0 + blockIdx.z);
+// Reduced storage carries a compensation register per voxel: two CTAs per SM.
+template <int VT>
+struct BpOcc {
+    static constexpr int value = VT == kVolF32 ? TOMO_BP_MIN_BLOCKS : 2;
+};
+
+template <bool SANITIZE, bool POS, int VT>
+__global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value) bp_separable_kernel(const __grid_constant__ BpLaunch a) {
+    bp_body<SANITIZE, POS, VT>(a, blockIdx.x * kTX, blockIdx.y * kTZ, a.y0 + blockIdx.z);
 }
 
 // Batched form: CTA b works on item {problem, x tile, z tile, row} of many problems.
-template <bool SANITIZE, bool POS>
-__global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS)
+template <bool SANITIZE, bool POS, int VT>
+__global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value)
     bp_kernel_batch(const BpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
-    bp_body<SANITIZE, POS>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
+    bp_body<SANITIZE, POS, VT>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
+}
+
+template <int VT>
+void bp_batch_vt(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n, cudaStream_t s) {
+    if (sanitize) {
+        if (positivity) bp_kernel_batch<true, true, VT><<<n, kBpThreads, 0, s>>>(descs, items);
+        else bp_kernel_batch<true, false, VT><<<n, kBpThreads, 0, s>>>(descs, items);
+    } else {
+        if (positivity) bp_kernel_batch<false, true, VT><<<n, kBpThreads, 0, s>>>(descs, items);
+        else bp_kernel_batch<false, false, VT><<<n, kBpThreads, 0, s>>>(descs, items);
+    }
+}
+
+template <int VT>
+void bp_separable_vt(const BpLaunch& a, dim3 grid, cudaStream_t s) {
+    if (a.sanitize) {
+        if (a.positivity) bp_separable_kernel<true, true, VT><<<grid, kBpThreads, 0, s>>>(a);
+        else bp_separable_kernel<true, false, VT><<<grid, kBpThreads, 0, s>>>(a);
+    } else {
+        if (a.positivity) bp_separable_kernel<false, true, VT><<<grid, kBpThreads, 0, s>>>(a);
+        else bp_separable_kernel<false, false, VT><<<grid, kBpThreads, 0, s>>>(a);
+    }
 }
 
 }  // namespace
@@ -212,16 +306,13 @@ __global__ void __launch_bounds__(kBpThreads, TOMO_BP_MIN_BLOCKS)
 int bp_tile_x() { return kTX; }
 int bp_tile_z() { return kTZ; }
 
-cudaError_t launch_bp_batch(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n_items,
-                            cudaStream_t s) {
+cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpLaunch* descs, const int4* items,
+                            int n_items, cudaStream_t s) {
     if (n_items <= 0) return cudaSuccess;
-    if (sanitize) {
-        if (positivity) bp_kernel_batch<true, true><<<n_items, kBpThreads, 0, s>>>(descs, items);
-        else bp_kernel_batch<true, false><<<n_items, kBpThreads, 0, s>>>(descs, items);
-    } else {
-        if (positivity) bp_kernel_batch<false, true><<<n_items, kBpThreads, 0, s>>>(descs, items);
-        else bp_kernel_batch<false, false><<<n_items, kBpThreads, 0, s>>>(descs, items);
-    }
+    if (vtype == kVolF32) bp_batch_vt<kVolF32>(sanitize, positivity, descs, items, n_items, s);
+    else if (vtype == kVolBF16) bp_batch_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, s);
+    else if (vtype == kVolF16) bp_batch_vt<kVolF16>(sanitize, positivity, descs, items, n_items, s);
+    else return cudaErrorInvalidValue;
     count_launch();
     return cudaGetLastError();
 }
@@ -229,17 +320,10 @@ cudaError_t launch_bp_batch(bool sanitize, bool positivity, const BpLaunch* desc
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s) {
     if (a.T <= 0 || a.y1 <= a.y0) return cudaSuccess;
     dim3 grid((a.W + kTX - 1) / kTX, (a.D + kTZ - 1) / kTZ, a.y1 - a.y0);
-    if (a.sanitize) {
-        if (a.positivity)
-            bp_separable_kernel<true, true><<<grid, kBpThreads, 0, s>>>(a);
-        else
-            bp_separable_kernel<true, false><<<grid, kBpThreads, 0, s>>>(a);
-    } else {
-        if (a.positivity)
-            bp_separable_kernel<false, true><<<grid, kBpThreads, 0, s>>>(a);
-        else
-            bp_separable_kernel<false, false><<<grid, kBpThreads, 0, s>>>(a);
-    }
+    if (a.vtype == kVolF32) bp_separable_vt<kVolF32>(a, grid, s);
+    else if (a.vtype == kVolBF16) bp_separable_vt<kVolBF16>(a, grid, s);
+    else if (a.vtype == kVolF16) bp_separable_vt<kVolF16>(a, grid, s);
+    else return cudaErrorInvalidValue;
     count_launch();
     return cudaGetLastError();
 }

@@ -114,21 +114,32 @@ __global__ void row_filter_kernel(float* img, const float* __restrict__ mask, co
 }
 
 // Sum over rows of the per-row residuals, one thread per tilt, fixed order.
-__global__ void reduce_err_kernel(const double* __restrict__ errpart, double* __restrict__ err, int T, int h) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T) return;
+// Sum of one projection's per-row residual sums by one warp: lane l adds rows
+// l, l + 32, ... in order, then a fixed butterfly combines the lanes (deterministic).
+__device__ __forceinline__ double warp_row_sum(const double* __restrict__ rows, int h) {
+    const int lane = threadIdx.x & 31;
     double s = 0.0;
-    for (int j = 0; j < h; j++) s += errpart[(size_t)t * h + j];
-    err[t] = s;
+    for (int j = lane; j < h; j += 32) s += rows[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
+constexpr int kErrWarps = 4;  // projections per 128-thread block
+
+__global__ void reduce_err_kernel(const double* __restrict__ errpart, double* __restrict__ err, int T, int h) {
+    const int t = blockIdx.x * kErrWarps + (threadIdx.x >> 5);
+    if (t >= T) return;
+    const double s = warp_row_sum(errpart + (size_t)t * h, h);
+    if ((threadIdx.x & 31) == 0) err[t] = s;
 }
 
 __global__ void reduce_err_batch_kernel(const ErrReduce* __restrict__ jobs) {
     const ErrReduce j = jobs[blockIdx.y];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * kErrWarps + (threadIdx.x >> 5);
     if (t >= j.T) return;
-    double s = 0.0;
-    for (int r = 0; r < j.h; r++) s += j.errpart[(size_t)t * j.h + r];
-    j.err[t] = s;
+    const double s = warp_row_sum(j.errpart + (size_t)t * j.h, j.h);
+    if ((threadIdx.x & 31) == 0) j.err[t] = s;
 }
 
 // TotalVariationDenoising_3D.updateP (Filters/.../TotalVariationDenoising_3D.java:115-156).
@@ -313,14 +324,15 @@ cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2
 }
 
 cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s) {
-    reduce_err_kernel<<<(T + 127) / 128, 128, 0, s>>>(errpart, err, T, h);
+    if (T <= 0) return cudaSuccess;
+    reduce_err_kernel<<<(T + kErrWarps - 1) / kErrWarps, 32 * kErrWarps, 0, s>>>(errpart, err, T, h);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_reduce_err_batch(const ErrReduce* jobs, int n_jobs, int max_T, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;
-    reduce_err_batch_kernel<<<dim3((max_T + 127) / 128, n_jobs), 128, 0, s>>>(jobs);
+    reduce_err_batch_kernel<<<dim3((max_T + kErrWarps - 1) / kErrWarps, n_jobs), 32 * kErrWarps, 0, s>>>(jobs);
     count_launch();
     return cudaGetLastError();
 }

@@ -1,5 +1,6 @@
 // C ABI of the engine: handles, admission control, the Projector surface and
 // the TomoReconstruction2 drivers.  See include/tomoj_gb300.h for the contract.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -80,7 +81,10 @@ tomo_status check_status(tomo_projector* p) {
     CK(cudaStreamSynchronize(p->stream));
     if (st != 0) {
         CK(cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream));
-        return fail(TOMO_ERR_DEVICE, "a kernel reported status " + std::to_string(st) + " (bounded wait expired)");
+        std::string why;
+        if (st & kStatusTimeout) why += " (bounded wait expired)";
+        if (st & (int)kStatusRange) why += " (a volume value left the FP16 range of its slab scale)";
+        return fail(TOMO_ERR_DEVICE, "a kernel reported status " + std::to_string(st) + why);
     }
     return TOMO_OK;
 }
@@ -143,7 +147,9 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
     }
     if (j0 >= j1) return TOMO_OK;
     FpLaunch a{};
-    a.vol = p->d_vol;
+    a.vol = p->vol();
+    a.vtype = p->vtype;
+    a.vscale = p->vtype == kVolF32 ? nullptr : p->d_vscale;
     a.meas = (with_diff && !p->params.long_object) ? p->d_meas : nullptr;
     a.tilts = d_tilts;
     a.T = T;
@@ -180,13 +186,30 @@ tomo_status apply_weighting(tomo_projector* p, float* imgs, int T) {
     return TOMO_OK;
 }
 
+// Reduced storage: row maxima are rebuilt by every backprojection, then slabs whose
+// maximum left the target band are re-scaled (a no-op launch for most rows).
+tomo_status bp_pre(tomo_projector* p, cudaStream_t s) {
+    if (p->vtype == kVolF32) return TOMO_OK;
+    CK(cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * p->g.H, s));
+    return TOMO_OK;
+}
+
+tomo_status bp_post(tomo_projector* p, cudaStream_t s) {
+    if (p->vtype == kVolF32) return TOMO_OK;
+    CK(launch_vol_rescale(p->vol(), p->vtype, p->d_vscale, p->d_vmax, p->g.W, p->g.H, p->g.D, p->d_status, s));
+    return TOMO_OK;
+}
+
 tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int T, int y0, int y1, bool sanitize) {
     const Geometry& g = p->g;
     y0 = std::max(0, y0);
     y1 = std::min(g.H, y1);
     if (y1 <= y0 || T <= 0) return TOMO_OK;
     BpLaunch a{};
-    a.vol = p->d_vol;
+    a.vol = p->vol();
+    a.vtype = p->vtype;
+    a.vscale = p->d_vscale;
+    a.vmax = p->d_vmax;
     a.img = imgs;
     a.tilts = d_tilts;
     a.T = T;
@@ -203,7 +226,9 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     a.positivity = p->params.positivity;
     a.sanitize = sanitize || p->vol_nonfinite;
     a.status = p->d_status;
+    CKS(bp_pre(p, p->stream));
     CK(launch_bp_separable(a, p->stream));
+    CKS(bp_post(p, p->stream));
     return TOMO_OK;
 }
 
@@ -220,16 +245,27 @@ tomo_status tv_denoise(tomo_projector* p) {
     const Geometry& g = p->g;
     if (p->tv_iters <= 0) return TOMO_OK;
     const size_t bytes = sizeof(float) * p->nvox;
-    CK(cudaMemcpyAsync(p->d_tv_u, p->d_vol, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    // reduced storage: the step runs on an FP32 copy f and packs u back with fresh slab scales
+    const bool red = p->vtype != kVolF32;
+    const float* f = red ? p->d_tv_f : p->d_vol;
+    if (red) CK(launch_vol_unpack(p->vol(), p->vtype, p->d_vscale, g.H, 0, g.W, g.H, g.D, p->d_tv_f, p->stream));
+    CK(cudaMemcpyAsync(p->d_tv_u, f, bytes, cudaMemcpyDeviceToDevice, p->stream));
     CK(cudaMemsetAsync(p->d_px, 0, bytes, p->stream));
     CK(cudaMemsetAsync(p->d_py, 0, bytes, p->stream));
     CK(cudaMemsetAsync(p->d_pz, 0, bytes, p->stream));
     for (int it = 0; it < p->tv_iters; it++) {
         CK(launch_tv_p(p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->tv_g, p->tv_dt,
                        p->stream));
-        CK(launch_tv_u(p->d_vol, p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->stream));
+        CK(launch_tv_u(f, p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->stream));
     }
-    CK(cudaMemcpyAsync(p->d_vol, p->d_tv_u, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    if (red) {
+        CK(cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * g.H, p->stream));
+        CK(launch_vol_rowmax(p->d_tv_u, g.H, 0, g.W, g.H, g.D, p->d_vmax, p->stream));
+        CK(launch_vol_pack(p->d_tv_u, g.H, 0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax, p->d_status,
+                           p->stream));
+    } else {
+        CK(cudaMemcpyAsync(p->d_vol, p->d_tv_u, bytes, cudaMemcpyDeviceToDevice, p->stream));
+    }
     return TOMO_OK;
 }
 
@@ -258,6 +294,8 @@ tomo_status handle_need_series(tomo_projector* p) { return need_series(p); }
 tomo_status handle_start_iteration(tomo_projector* p) { return start_iteration(p); }
 tomo_status handle_end_iteration(tomo_projector* p) { return end_iteration(p); }
 int handle_tilts_per_cta(const tomo_projector* p, int T) { return auto_tilts_per_cta(p, T, 0); }
+tomo_status handle_bp_pre(tomo_projector* p, cudaStream_t s) { return bp_pre(p, s); }
+tomo_status handle_bp_post(tomo_projector* p, cudaStream_t s) { return bp_post(p, s); }
 }  // namespace tomo
 
 extern "C" {
@@ -298,6 +336,11 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
     for (int k = 0; k < 4; k++) g.pc[k] = std::isnan(geom->proj_center[k]) ? dpc[k] : geom->proj_center[k];
     g.scale = geom->scale == 0.0 ? 1.0 : geom->scale;
     if (params) p->params = *params;
+    if (p->params.precision < TOMO_PREC_FP32 || p->params.precision > TOMO_PREC_FP16) {
+        delete p;
+        return fail(TOMO_ERR_INVALID, "precision must be TOMO_PREC_FP32, TOMO_PREC_BF16 or TOMO_PREC_FP16");
+    }
+    p->vtype = p->params.precision;  // TOMO_PREC_* values equal the storage types
     cudaGetDevice(&p->device);
     p->npix = (size_t)g.w * g.h;
     p->nvox = (size_t)g.W * g.H * g.D;
@@ -306,7 +349,13 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
     auto A = [&](tomo_status s) {
         if (st == TOMO_OK) st = s;
     };
-    A(alloc_n(p, &p->d_vol, p->nvox));
+    if (p->vtype == kVolF32) {
+        A(alloc_n(p, &p->d_vol, p->nvox));
+    } else {
+        A(alloc_n(p, &p->d_vol16, p->nvox));
+        A(alloc_n(p, &p->d_vscale, (size_t)g.H));
+        A(alloc_n(p, &p->d_vmax, (size_t)g.H));
+    }
     A(alloc_n(p, &p->d_raw, N * p->npix));
     A(alloc_n(p, &p->d_meas, N * p->npix));
     A(alloc_n(p, &p->d_proj, N * p->npix));
@@ -344,7 +393,12 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
         tomo_destroy(p);
         return fail(TOMO_ERR_CUDA, "cannot configure kernel shared memory");
     }
-    cudaMemsetAsync(p->d_vol, 0, sizeof(float) * p->nvox, p->stream);
+    if (p->vtype == kVolF32) {
+        cudaMemsetAsync(p->d_vol, 0, sizeof(float) * p->nvox, p->stream);
+    } else {
+        launch_vol_fill(p->d_vol16, p->vtype, p->d_vscale, p->nvox, g.H, 0.0f, p->stream);
+        cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * g.H, p->stream);
+    }
     cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream);
     cudaMemsetAsync(p->d_err, 0, sizeof(double) * N, p->stream);
     if (cudaStreamSynchronize(p->stream) != cudaSuccess) {
@@ -472,6 +526,20 @@ tomo_status tomo_get_aligned(tomo_projector* p, int32_t index, float* out_host) 
     return TOMO_OK;
 }
 
+// FP32 staging of a reduced volume: enough rows for about 64 MB (at least one row).
+static tomo_status ensure_vtmp(tomo_projector* p, size_t* rows_out) {
+    const Geometry& g = p->g;
+    const size_t row_bytes = sizeof(float) * (size_t)g.W * g.D;
+    size_t rows = std::max<size_t>(1, ((size_t)64 << 20) / row_bytes);
+    rows = std::min<size_t>(rows, (size_t)g.H);
+    if (!p->d_vtmp) {
+        CKS(alloc_n(p, &p->d_vtmp, rows * (size_t)g.W * g.D));
+        p->vtmp_rows = rows;
+    }
+    *rows_out = p->vtmp_rows;
+    return TOMO_OK;
+}
+
 static tomo_status volume_copy(tomo_projector* p, float* host_or_dev, int on_device, int y0, int y1, bool to_dev) {
     const Geometry& g = p->g;
     if (y0 < 0 || y1 > g.H || y1 < y0) return fail(TOMO_ERR_INVALID, "row range outside the volume");
@@ -480,15 +548,41 @@ static tomo_status volume_copy(tomo_projector* p, float* host_or_dev, int on_dev
     // [D][rows][W] <-> [D][H][W] rows y0..y1 of every slice
     cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice
                                     : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
-    float* dev = p->d_vol + (size_t)y0 * g.W;
-    if (to_dev)
-        CK(cudaMemcpy2DAsync(dev, sizeof(float) * g.W * g.H, host_or_dev, sizeof(float) * g.W * rows,
-                             sizeof(float) * g.W * rows, g.D, kind, p->stream));
-    else
-        CK(cudaMemcpy2DAsync(host_or_dev, sizeof(float) * g.W * rows, dev, sizeof(float) * g.W * g.H,
-                             sizeof(float) * g.W * rows, g.D, kind, p->stream));
-    CK(cudaStreamSynchronize(p->stream));
-    return TOMO_OK;
+    if (p->vtype == kVolF32) {
+        float* dev = p->d_vol + (size_t)y0 * g.W;
+        if (to_dev)
+            CK(cudaMemcpy2DAsync(dev, sizeof(float) * g.W * g.H, host_or_dev, sizeof(float) * g.W * rows,
+                                 sizeof(float) * g.W * rows, g.D, kind, p->stream));
+        else
+            CK(cudaMemcpy2DAsync(host_or_dev, sizeof(float) * g.W * rows, dev, sizeof(float) * g.W * g.H,
+                                 sizeof(float) * g.W * rows, g.D, kind, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        return TOMO_OK;
+    }
+    // reduced storage: blocks of rows through the FP32 staging buffer
+    size_t cap = 0;
+    CKS(ensure_vtmp(p, &cap));
+    kind = on_device ? cudaMemcpyDeviceToDevice : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+    for (size_t a = 0; a < rows; a += cap) {
+        const size_t n = std::min(cap, rows - a);
+        float* user = host_or_dev + a * g.W;  // row a of the caller's [D][rows][W] buffer
+        const int r0 = y0 + (int)a;
+        if (to_dev) {
+            CK(cudaMemcpy2DAsync(p->d_vtmp, sizeof(float) * g.W * n, user, sizeof(float) * g.W * rows,
+                                 sizeof(float) * g.W * n, g.D, kind, p->stream));
+            CK(cudaMemsetAsync(p->d_vmax + r0, 0, sizeof(unsigned) * n, p->stream));
+            CK(launch_vol_rowmax(p->d_vtmp, (int)n, r0, g.W, g.H, g.D, p->d_vmax, p->stream));
+            CK(launch_vol_pack(p->d_vtmp, (int)n, r0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax,
+                               p->d_status, p->stream));
+        } else {
+            CK(launch_vol_unpack(p->vol(), p->vtype, p->d_vscale, (int)n, r0, g.W, g.H, g.D, p->d_vtmp, p->stream));
+            CK(cudaMemcpy2DAsync(user, sizeof(float) * g.W * rows, p->d_vtmp, sizeof(float) * g.W * n,
+                                 sizeof(float) * g.W * n, g.D, kind, p->stream));
+        }
+        // the staging buffer is reused by the next block
+        CK(cudaStreamSynchronize(p->stream));
+    }
+    return to_dev ? check_status(p) : TOMO_OK;
 }
 
 tomo_status tomo_set_volume(tomo_projector* p, const float* src, int32_t on_device, int32_t y0, int32_t y1) {
@@ -496,7 +590,7 @@ tomo_status tomo_set_volume(tomo_projector* p, const float* src, int32_t on_devi
     CKS(volume_copy(p, const_cast<float*>(src), on_device, y0, y1, true));
     int flags = 0;
     CK(cudaMemsetAsync(p->d_flags, 0, sizeof(int), p->stream));
-    CK(launch_scan_nonfinite(p->d_vol, p->nvox, p->d_flags, p->stream));
+    CK(launch_scan_nonfinite_vol(p->vol(), p->vtype, p->nvox, p->d_flags, p->stream));
     CK(cudaMemcpyAsync(&flags, p->d_flags, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaStreamSynchronize(p->stream));
     p->vol_nonfinite = flags != 0;
@@ -510,7 +604,10 @@ tomo_status tomo_get_volume(tomo_projector* p, float* dst, int32_t on_device, in
 
 tomo_status tomo_fill_volume(tomo_projector* p, float value) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
-    CK(launch_fill(p->d_vol, p->nvox, value, p->stream));
+    if (p->vtype == kVolF32)
+        CK(launch_fill(p->d_vol, p->nvox, value, p->stream));
+    else
+        CK(launch_vol_fill(p->vol(), p->vtype, p->d_vscale, p->nvox, p->g.H, value, p->stream));
     CK(cudaStreamSynchronize(p->stream));
     p->vol_nonfinite = !std::isfinite(value);
     return TOMO_OK;
@@ -518,6 +615,8 @@ tomo_status tomo_fill_volume(tomo_projector* p, float value) {
 
 tomo_status tomo_volume_device_ptr(tomo_projector* p, float** out) {
     if (!p || !out) return fail(TOMO_ERR_INVALID, "null argument");
+    if (p->vtype != kVolF32)
+        return fail(TOMO_ERR_UNSUPPORTED, "the volume is stored in 16 bits with slab scales; use tomo_get_volume");
     *out = p->d_vol;
     return TOMO_OK;
 }
@@ -673,6 +772,7 @@ tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int3
         CKS(alloc_n(p, &p->d_py, p->nvox));
         CKS(alloc_n(p, &p->d_pz, p->nvox));
     }
+    if (iterations > 0 && p->vtype != kVolF32 && !p->d_tv_f) CKS(alloc_n(p, &p->d_tv_f, p->nvox));
     p->tv_theta = theta;
     p->tv_g = g;
     p->tv_dt = dt;
@@ -682,6 +782,8 @@ tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int3
 
 tomo_status tomo_set_fista(tomo_projector* p, int32_t enabled) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (enabled && p->vtype != kVolF32)
+        return fail(TOMO_ERR_UNSUPPORTED, "FISTA momentum needs the FP32 volume (precision TOMO_PREC_FP32)");
     if (enabled && !p->d_prev) CKS(alloc_n(p, &p->d_prev, p->nvox));
     p->fista = enabled != 0;
     p->fista_t = 0.0;

@@ -6,6 +6,7 @@
 #include "../../include/tomoj_gb300.h"
 #include "tomo_internal.h"
 
+
 struct tomo_projector {
     tomo::Geometry g{};
     tomo_params params{};
@@ -16,7 +17,15 @@ struct tomo_projector {
     std::vector<void*> allocs;
     uint64_t bytes = 0;
 
-    float* d_vol = nullptr;
+    float* d_vol = nullptr;        // FP32 volume (precision TOMO_PREC_FP32)
+    int vtype = tomo::kVolF32;          // volume storage type (tomo_params.precision)
+    uint16_t* d_vol16 = nullptr;   // reduced volume [D][H][W] (BF16 / FP16 bit patterns)
+    float* d_vscale = nullptr;     // [H] slab scales of the reduced volume
+    unsigned* d_vmax = nullptr;    // [H] row max |value| after the last backprojection
+    float* d_vtmp = nullptr;       // FP32 staging rows for set/get of a reduced volume (lazy)
+    size_t vtmp_rows = 0;          // volume rows d_vtmp holds
+    float* d_tv_f = nullptr;       // FP32 copy of a reduced volume for the TV step (lazy)
+    void* vol() const { return vtype == tomo::kVolF32 ? static_cast<void*>(d_vol) : static_cast<void*>(d_vol16); }
     float* d_raw = nullptr;
     float* d_meas = nullptr;
     float* d_proj = nullptr;
@@ -72,4 +81,8 @@ tomo_status handle_need_series(tomo_projector* p);
 tomo_status handle_start_iteration(tomo_projector* p);
 tomo_status handle_end_iteration(tomo_projector* p);
 int handle_tilts_per_cta(const tomo_projector* p, int T);
+// Reduced-precision bookkeeping around a backprojection: zero the row maxima before,
+// re-scale the slabs that left their band after.
+tomo_status handle_bp_pre(tomo_projector* p, cudaStream_t s);
+tomo_status handle_bp_post(tomo_projector* p, cudaStream_t s);
 }  // namespace tomo

@@ -20,6 +20,10 @@ namespace tomo {
 
 constexpr double kFix = 4294967296.0;  // 2^32: fixed-point scale of positions
 
+// Device status word bits written by kernels (never trap: the host reads them).
+constexpr int kStatusTimeout = 1;       // an mbarrier wait exceeded its iteration budget
+constexpr unsigned kStatusRange = 4u;   // a volume value left the FP16 range of its slab scale
+
 // One forward-projection ray (tilt t, detector column i).  The ray is inside
 // the volume for z in [za, za + cnt); x(z) = X0 + z * step in 32.32 fixed point.
 struct alignas(16) FpRay {
@@ -58,9 +62,21 @@ int first_index(uint64_t seed, int iteration, int nproj);
 void weighting_row_filter(int kind, int w, int nproj, const double* sint, const double* tilts_deg, double diameter,
                           float* mask_row);
 
+// Volume storage types (values of tomo_params.precision).  Reduced types hold
+// value / vscale[r] per volume row r (an XZ slab), vscale a power of two.
+enum VolType : int { kVolF32 = 0, kVolBF16 = 1, kVolF16 = 2 };
+#ifdef __CUDACC__
+#define TOMO_HD __host__ __device__
+#else
+#define TOMO_HD
+#endif
+TOMO_HD inline size_t vol_elem_bytes(int vt) { return vt == kVolF32 ? 4 : 2; }
+
 // Device kernels (launch wrappers in the .cu files).  All return cudaError_t of the launch.
 struct FpLaunch {
-    const float* vol;       // [D][H][W]
+    const void* vol;        // [D][H][W] of vtype
+    int vtype;              // VolType
+    const float* vscale;    // [H] slab scales (reduced types), else nullptr
     const float* meas;      // aligned measured [N][h][w] (nullptr: projection only)
     const int* tilts;       // batch tilt indices [T]
     int T;                  // projections in the batch
@@ -78,9 +94,16 @@ struct FpLaunch {
     int* status;            // device error word
 };
 cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s);
+// Plane rows are staged with bulk copies when every row starts on a 16-byte boundary.
+inline int fp_use_tma(int W, int vtype, const void* vol) {
+    return ((W * vol_elem_bytes(vtype)) % 16 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+}
 
 struct BpLaunch {
-    float* vol;
+    void* vol;              // [D][H][W] of vtype
+    int vtype;              // VolType; reduced types add with Kahan compensation
+    const float* vscale;    // [H] slab scales (reduced types)
+    unsigned* vmax;         // [H] running max |value| per row as float bits (reduced types)
     const float* img;       // [T][h][w] images to backproject, batch order
     const int* tilts;       // [T] tilt index of each image (for geometry)
     int T;
@@ -95,8 +118,8 @@ struct BpLaunch {
 };
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
 // Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row}.
-cudaError_t launch_bp_batch(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n_items,
-                            cudaStream_t s);
+cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpLaunch* descs, const int4* items,
+                            int n_items, cudaStream_t s);
 int bp_tile_x();
 int bp_tile_z();
 
@@ -131,6 +154,22 @@ cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* 
 cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s);
 cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s);
 cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s);
+
+// Reduced-precision volume storage (kernels_vol.cu).  `src`/`dst` float buffers are
+// laid out [D][rows][W] and cover volume rows [y0, y0 + rows).
+// Max |value| of each of the rows into vmax[y0 + row] (float bits; vmax zeroed by the caller).
+cudaError_t launch_vol_rowmax(const float* src, int rows, int y0, int W, int H, int D, unsigned* vmax,
+                              cudaStream_t s);
+// Picks each row's scale from vmax (slab_scale_for) and packs src into the reduced volume.
+cudaError_t launch_vol_pack(const float* src, int rows, int y0, int W, int H, int D, int vtype, void* vol,
+                            float* vscale, const unsigned* vmax, int* status, cudaStream_t s);
+cudaError_t launch_vol_unpack(const void* vol, int vtype, const float* vscale, int rows, int y0, int W, int H,
+                              int D, float* dst, cudaStream_t s);
+// Re-scales the rows whose max (vmax, after a backprojection) left the target band.
+cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, const unsigned* vmax, int W, int H, int D,
+                               int* status, cudaStream_t s);
+cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, size_t nvox, int H, float value, cudaStream_t s);
+cudaError_t launch_scan_nonfinite_vol(const void* vol, int vtype, size_t n, int* flags, cudaStream_t s);
 
 // Sets the calling thread's message for tomo_last_error.
 void set_last_error(const char* msg);

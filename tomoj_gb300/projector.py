@@ -51,9 +51,10 @@ class VoxelProjector3D(Projector):
     Construction captures dimensions and centres from the tilt-series and the
     reconstruction (Projector.java:30-40); the tilt-series (aligned by the
     series' AffineAlignment, TiltSeries.getPixels) is uploaded once.
-    `weighting` is None or a (kind, radius) pair (WBP filter)."""
+    `weighting` is None or a (kind, radius) pair (WBP filter).  `precision` selects the
+    volume storage ("fp32", "bf16" or "fp16"; 16-bit forms keep per-row slab scales)."""
 
-    def __init__(self, ts, rec, weighting=None, positivity=False, long_object=False, scale=None):
+    def __init__(self, ts, rec, weighting=None, positivity=False, long_object=False, scale=None, precision="fp32"):
         self.ts = ts
         self.rec = rec
         lib = _abi.load()
@@ -65,7 +66,7 @@ class VoxelProjector3D(Projector):
                                     proj_center=(ts.getCenterX(), ts.getCenterY(), ts.getProjectionCenterX(),
                                                  ts.getProjectionCenterY()), scale=scale)
         self._params = _abi.make_params(positivity=positivity, long_object=long_object, fill=ts.getFillType(),
-                                        normalize=ts.isNormalized())
+                                        normalize=ts.isNormalized(), precision=_abi.precision_code(precision))
         h_ = C.c_void_p()
         check(lib.tomo_create(C.byref(self._geom), C.byref(self._params), C.byref(h_)))
         self._h = h_

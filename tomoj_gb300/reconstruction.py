@@ -157,6 +157,8 @@ class ReconstructionParameters:
         # TVM (AdvancedReconstructionParameters)
         self.tvmTheta, self.tvmG, self.tvmDt, self.tvmIterations = 25.0, 1.0, 0.1, 5
         self.regularizationWeight = 0.1
+        # volume storage precision (engine option; the reference stores float32)
+        self.precision = _abi.PREC_FP32
 
     @staticmethod
     def createOSSARTParameters(width, height, depth, nbIterations, relaxationCoefficient, updateNb):
@@ -211,11 +213,16 @@ class ReconstructionParameters:
     def setLongObjectCompensation(self, v):
         self.longObjectCompensation = bool(v)
 
+    def setPrecision(self, v):
+        """Volume storage: "fp32" (default), "bf16" or "fp16" (or a PREC_* value)."""
+        self.precision = _abi.precision_code(v)
+
     def getProjector(self, ts, rec) -> VoxelProjector3D:
         """ReconstructionParameters.getProjector (ReconstructionParameters.java:313-333)."""
         scale = ts.getWidth() / float(rec.getWidth()) if self.rescaleData else 1.0
         pos = self.positivityConstraint if self.reconstructionType in (OSSART, TVM) else False
-        proj = VoxelProjector3D(ts, rec, None, positivity=pos, long_object=self.longObjectCompensation, scale=scale)
+        proj = VoxelProjector3D(ts, rec, None, positivity=pos, long_object=self.longObjectCompensation, scale=scale,
+                                precision=self.precision)
         if self.reconstructionType == WBP:
             proj.setWeighting(self.weightingType, self.weightingRadius if self.weightingRadius == self.weightingRadius
                               else 0.0)
