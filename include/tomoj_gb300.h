@@ -152,6 +152,22 @@ tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, c
 tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int32_t iterations);
 /* FISTA momentum wrapper (FistaProjector3D.java). */
 tomo_status tomo_set_fista(tomo_projector* p, int32_t enabled);
+/* BayesianVoxelProjector3D (TomoJ_AdvancedReconstruction/.../projectors/
+ * BayesianVoxelProjector3D.java): startOfIteration sets a distance volume to
+ * -lambda times the 27-point [1,-2,1]^3 stencil of the volume, every update's
+ * differences are backprojected into it instead of the volume, and
+ * endOfIteration adds alpha times it to the volume (then positivity, if set).
+ * FP32 volumes only. */
+tomo_status tomo_set_bayesian(tomo_projector* p, double lambda, double alpha, int32_t enabled);
+/* BgARTVoxelProjector3D (TomoJ_AdvancedReconstruction/.../projectors/
+ * BgARTVoxelProjector3D.java): a 7-point cross median before every iteration
+ * (do_median), and after every iteration the histogram collapse filter: voxels
+ * on the background side of mode +/- k sigma become the background value (the
+ * histogram mode, or bg_value when it is not NaN).  Enabling applies the
+ * collapse once to the current volume, as the reference's constructor does.
+ * FP32 volumes only. */
+tomo_status tomo_set_bgart(tomo_projector* p, double k, int32_t dark_bg, int32_t do_median, double bg_value,
+                           int32_t enabled);
 
 /* ---- drivers (TomoReconstruction2) --------------------------------------- */
 /* WBP(ts, projector, params, y0, y1) with update 0 (TomoReconstruction2.java:499-538). */

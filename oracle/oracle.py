@@ -105,6 +105,13 @@ def lib():
         L.or_wbp.argtypes = [f32, G, f64, f32, C.c_int, f32, C.c_int, C.c_int]
         L.or_fista_step.argtypes = [f32, f32, C.c_size_t, C.c_double]
         L.or_fista_step.restype = C.c_double
+        L.or_ossart_iteration_into.argtypes = [f32, f32, G, f64, f32, C.c_int, i32, C.c_double, C.c_int, C.c_int,
+                                               C.c_int, f64]
+        L.or_bayes_start.argtypes = [f32, f32, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.or_bayes_end.argtypes = [f32, f32, C.c_size_t, C.c_double, C.c_int]
+        L.or_bgart_collapse.argtypes = [f32, C.c_size_t, C.c_double, C.c_int, C.c_double]
+        L.or_bgart_collapse.restype = C.c_double
+        L.or_bgart_median_cross.argtypes = [f32, C.c_int, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -260,6 +267,45 @@ def fista_step(rec, prev, t):
     _vol(rec)
     _vol(prev)
     return lib().or_fista_step(_p(rec, C.c_float), _p(prev, C.c_float), rec.size, float(t))
+
+
+def bayesian_iteration(vol, g: Geom, eulers, meas, order, relax, update, lam, alpha, y0=0, y1=None):
+    """One OS-SART iteration driven through BayesianVoxelProjector3D
+    (TomoJ_AdvancedReconstruction/.../projectors/BayesianVoxelProjector3D.java): the
+    distance volume starts as -lambda times the 27-point [1,-2,1]^3 stencil of the volume,
+    every update's differences are backprojected into it (the volume itself is projected
+    unchanged all iteration), and the end adds alpha times it to the volume (positivity
+    after, when g.positivity).  Returns err5."""
+    _vol(vol)
+    y1 = g.H if y1 is None else y1
+    D, H, W = vol.shape
+    dist = np.zeros_like(vol)
+    L = lib()
+    L.or_bayes_start(_p(vol, C.c_float), _p(dist, C.c_float), W, H, D, float(lam))
+    e = np.ascontiguousarray(eulers, np.float64)
+    meas = np.ascontiguousarray(meas, np.float32)
+    order = np.ascontiguousarray(order, np.int32)
+    err5 = np.zeros(5, np.float64)
+    gc = g.c()
+    L.or_ossart_iteration_into(_p(vol, C.c_float), _p(dist, C.c_float), C.byref(gc), _p(e, C.c_double),
+                               _p(meas, C.c_float), e.shape[0], _p(order, C.c_int), float(relax), int(update), y0,
+                               y1, _p(err5, C.c_double))
+    L.or_bayes_end(_p(vol, C.c_float), _p(dist, C.c_float), vol.size, float(alpha), int(g.positivity))
+    return err5
+
+
+def bgart_collapse(vol, k, dark_bg=True, bg_value=float("nan")):
+    """BgARTVoxelProjector3D.collapseFilter in place; returns the background value."""
+    _vol(vol)
+    return lib().or_bgart_collapse(_p(vol, C.c_float), vol.size, float(k), int(bool(dark_bg)), float(bg_value))
+
+
+def bgart_median_cross(vol):
+    """BgARTVoxelProjector3D.medianFilter3Dcross in place."""
+    _vol(vol)
+    D, H, W = vol.shape
+    lib().or_bgart_median_cross(_p(vol, C.c_float), W, H, D)
+    return vol
 
 
 def ossart(vol, g: Geom, eulers, meas, n_iter, relax, update, first=0, y0=0, y1=None, end_of_iteration=None):

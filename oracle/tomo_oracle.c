@@ -722,9 +722,28 @@ void or_order_shuffle(int nproj, const double* euler, int first, int* indexes) {
  * calls of VoxelProjector3D.  order: the projection order for this iteration.
  * err5 receives {average, min, argmin, max, argmax} as the reference computes them.
  * err_per_proj (nproj, may be NULL) receives each projection's sum of squares. */
+static void ossart_iteration_into(float* vol, float* bp_vol, const or_geom* g, const double* euler,
+                                  const float* meas, int nproj, const int* order, double relax, int update,
+                                  int startY, int endY, double* err5, double* err_per_proj);
+
 void or_ossart_iteration(float* vol, const or_geom* g, const double* euler, const float* meas, int nproj,
                          const int* order, double relax, int update, int startY, int endY, double* err5,
                          double* err_per_proj) {
+    ossart_iteration_into(vol, vol, g, euler, meas, nproj, order, relax, update, startY, endY, err5, err_per_proj);
+}
+
+/* The same iteration projecting `vol` but backprojecting into `bp_vol`
+ * (BayesianVoxelProjector3D.backproject adds the differences to its distance
+ * volume, BayesianVoxelProjector3D.java:77-116). */
+void or_ossart_iteration_into(float* vol, float* bp_vol, const or_geom* g, const double* euler, const float* meas,
+                              int nproj, const int* order, double relax, int update, int startY, int endY,
+                              double* err5) {
+    ossart_iteration_into(vol, bp_vol, g, euler, meas, nproj, order, relax, update, startY, endY, err5, NULL);
+}
+
+static void ossart_iteration_into(float* vol, float* bp_vol, const or_geom* g, const double* euler,
+                                  const float* meas, int nproj, const int* order, double relax, int update,
+                                  int startY, int endY, double* err5, double* err_per_proj) {
     const int upd = (update == 0) ? nproj : update;
     const float factorimg = (float)(relax / upd);
     const size_t npix = (size_t)g->w * g->h;
@@ -750,7 +769,7 @@ void or_ossart_iteration(float* vol, const or_geom* g, const double* euler, cons
                 else if (err < errmin) { errmin = err; imin = order[t - diffIndex + e + 1]; }
             }
             for (int e = 0; e < diffIndex; e++)
-                or_backproject(vol, g, euler + 9 * batch[e], diff + npix * e, startY, endY);
+                or_backproject(bp_vol, g, euler + 9 * batch[e], diff + npix * e, startY, endY);
             diffIndex = 0;
         }
     }
@@ -790,4 +809,161 @@ double or_fista_step(float* rec, const float* prev, size_t n, double t) {
         if (!isnan(val)) rec[i] = rec[i] + (float)val;
     }
     return t;
+}
+
+/* ------------------------------------------------------------------------ */
+/* BayesianVoxelProjector3D (TomoJ_AdvancedReconstruction/.../projectors/    */
+/* BayesianVoxelProjector3D.java).                                           */
+/* ------------------------------------------------------------------------ */
+
+/* startOfIteration -> convolve(rec, kernel, distanceVolume, -lambda) (:131-134, :168-194):
+ * dist = (float)(factor * sum_n neighbour_n * kernel_n) over the 3x3x3 neighbourhood of
+ * TomoReconstruction2.getCubicNeightborhoodWithClamp (TomoReconstruction2.java:317-339),
+ * which reads getPixel(x+i, y+j, z+k) for i, j, k = -1..1 (i outermost): despite its
+ * name, out-of-volume neighbours are 0 (getPixel, :241-246).  The kernel is
+ * [1,-2,1] x [1,-2,1] x [1,-2,1]; products are float, the sum double. */
+void or_bayes_start(const float* rec, float* dist, int W, int H, int D, double lambda) {
+    static const float kern[27] = {1, -2, 1, -2, 4, -2, 1, -2, 1, -2, 4, -2, 4, -8, 4, -2, 4, -2,
+                                   1, -2, 1, -2, 4, -2, 1, -2, 1};
+    const double factor = -lambda;
+    for (int z = 0; z < D; z++)
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                double total = 0;
+                int idx = 0;
+                for (int i = -1; i <= 1; i++)
+                    for (int j = -1; j <= 1; j++)
+                        for (int k = -1; k <= 1; k++) {
+                            const int xx = x + i, yy = y + j, zz = z + k;
+                            float v = 0.0f;
+                            if (xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D)
+                                v = rec[((size_t)zz * H + yy) * W + xx];
+                            total += (double)(v * kern[idx++]);
+                        }
+                dist[((size_t)z * H + y) * W + x] = (float)(total * factor);
+            }
+}
+
+/* endOfIteration (:119-129): distanceVolume *= alpha (FloatProcessor.multiply: float
+ * pixel times double, rounded to float), rec += distanceVolume (FloatBlitter.ADD,
+ * float), then the positivity constraint (FloatBlitter.MAX with zeros) when set. */
+void or_bayes_end(float* rec, float* dist, size_t n, double alpha, int positivity) {
+    for (size_t i = 0; i < n; i++) {
+        dist[i] = (float)((double)dist[i] * alpha);
+        float v = dist[i] + rec[i];
+        if (positivity && 0.0f > v) v = 0.0f;
+        rec[i] = v;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* BgARTVoxelProjector3D (TomoJ_AdvancedReconstruction/.../projectors/       */
+/* BgARTVoxelProjector3D.java).                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Stack histogram as ImageJ's StackStatistics computes it for 32-bit data (ij 1.53a,
+ * a dependency absent from the reference tree; restated from its documented
+ * behaviour): min and max over the non-NaN voxels, 256 bins over [min, max], bin
+ * (int)((v - min) * (256 / (max - min))) clamped to 255; every voxel falls in bin 0
+ * when max == min. */
+static void ij_stack_histogram(const float* v, size_t n, double* mn, double* mx, long long* hist) {
+    double lo = INFINITY, hi = -INFINITY;
+    for (size_t i = 0; i < n; i++) {
+        if (isnan(v[i])) continue;
+        if (v[i] < lo) lo = v[i];
+        if (v[i] > hi) hi = v[i];
+    }
+    memset(hist, 0, sizeof(long long) * 256);
+    const double scale = 256.0 / (hi - lo);
+    for (size_t i = 0; i < n; i++) {
+        if (isnan(v[i])) continue;
+        int b = 0;
+        if (hi > lo) {
+            b = jint((v[i] - lo) * scale);
+            if (b > 255) b = 255;
+        }
+        hist[b]++;
+    }
+    *mn = lo;
+    *mx = hi;
+}
+
+/* collapseFilter (:29-90): the background is the histogram mode (or bgValue when it is
+ * not NaN), sigma the spread of the bins below the mode around it; with a dark
+ * background every voxel below mode + k sigma becomes the background, otherwise every
+ * voxel above mode - k sigma.  Returns the background value. */
+double or_bgart_collapse(float* vol, size_t n, double k, int dark_bg, double bg_value) {
+    long long hist[256];
+    double histmin, histmax;
+    ij_stack_histogram(vol, n, &histmin, &histmax, hist);
+    const double bin = (histmax - histmin) / 256;
+    double best = 0;
+    int max_index = 0;
+    for (int i = 0; i < 256; i++)
+        if ((double)hist[i] > best) {
+            best = (double)hist[i];
+            max_index = i;
+        }
+    const double bg = isnan(bg_value) ? histmin + max_index * bin : bg_value;
+    double sigma = 0;
+    long long count = 0;
+    for (int i = 0; i < max_index; i++) {
+        const double d = histmin + i * bin - bg;
+        sigma += d * d * (double)hist[i];
+        count += hist[i];
+    }
+    sigma = sqrt(sigma / (double)count);
+    const double th1 = bg - k * sigma, th2 = bg + k * sigma;
+    for (size_t i = 0; i < n; i++) {
+        const double val = vol[i];
+        if (dark_bg && val < th2) vol[i] = (float)bg;
+        if (!dark_bg && val > th1) vol[i] = (float)bg;
+    }
+    return bg;
+}
+
+/* Java's Arrays.sort(float[]) order as an unsigned key: -0.0 before 0.0, NaN last. */
+static inline uint32_t java_float_key(float f) {
+    uint32_t b;
+    if (isnan(f)) return 0xFFFFFFFFu;
+    memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+/* medianFilter3Dcross (:117-145): median of the voxel, its two z neighbours (0 outside
+ * the stack) and four in-plane neighbours addressed by flat index within the slice,
+ * so x neighbours wrap across rows, indices must be > 0 for the -1 and -W neighbours
+ * and < W*H for the +1 and +W neighbours (0 otherwise); all reads from a copy. */
+void or_bgart_median_cross(float* vol, int W, int H, int D) {
+    const size_t P = (size_t)W * H, n = P * D;
+    float* tmp = (float*)malloc(sizeof(float) * n);
+    memcpy(tmp, vol, sizeof(float) * n);
+    for (int z = 0; z < D; z++) {
+        const float* cur = tmp + P * z;
+        const float* lo = z > 0 ? tmp + P * (z - 1) : NULL;
+        const float* hi = z < D - 1 ? tmp + P * (z + 1) : NULL;
+        for (long long idx = 0; idx < (long long)P; idx++) {
+            float nb[7];
+            nb[0] = lo ? lo[idx] : 0.0f;
+            nb[1] = hi ? hi[idx] : 0.0f;
+            nb[2] = cur[idx];
+            nb[3] = (idx + 1 < (long long)P) ? cur[idx + 1] : 0.0f;
+            nb[4] = (idx - 1 > 0) ? cur[idx - 1] : 0.0f;
+            nb[5] = (idx - W > 0) ? cur[idx - W] : 0.0f;
+            nb[6] = (idx + W < (long long)P) ? cur[idx + W] : 0.0f;
+            /* insertion sort by Java's float order */
+            for (int a = 1; a < 7; a++) {
+                const float f = nb[a];
+                const uint32_t kf = java_float_key(f);
+                int b = a - 1;
+                while (b >= 0 && java_float_key(nb[b]) > kf) {
+                    nb[b + 1] = nb[b];
+                    b--;
+                }
+                nb[b + 1] = f;
+            }
+            vol[P * z + idx] = nb[3];
+        }
+    }
+    free(tmp);
 }

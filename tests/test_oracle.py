@@ -177,3 +177,99 @@ def test_order_shuffle_picks_most_perpendicular(oracle_lib):
     assert idx[0] == 30 and sorted(idx) == list(range(61))
     # from 0 deg the beam is most perpendicular to +-60 deg; the first of equals wins
     assert idx[1] == 0
+
+
+def test_bayesian_stencil_is_zero_padded_mixed_second_difference(oracle_lib):
+    # BayesianVoxelProjector3D.startOfIteration: -lambda * sum of the 3x3x3 neighbours weighted
+    # by [1,-2,1]^3, out-of-volume neighbours 0 (getCubicNeightborhoodWithClamp reads getPixel)
+    rng = np.random.default_rng(5)
+    D, H, W = 6, 5, 7
+    vol = rng.uniform(-1, 1, (D, H, W)).astype(np.float32)
+    k1 = np.array([1.0, -2.0, 1.0])
+    pad = np.pad(vol.astype(np.float64), 1)
+    ref = np.zeros((D, H, W))
+    for dz in range(3):
+        for dy in range(3):
+            for dx in range(3):
+                ref += k1[dz] * k1[dy] * k1[dx] * pad[dz:dz + D, dy:dy + H, dx:dx + W]
+    lam = 0.3
+    dist = np.zeros_like(vol)
+    O.lib().or_bayes_start(vol.ctypes.data_as(O.C.POINTER(O.C.c_float)),
+                           dist.ctypes.data_as(O.C.POINTER(O.C.c_float)), W, H, D, lam)
+    assert np.allclose(dist, -lam * ref, rtol=1e-6, atol=1e-6)
+    # a linear ramp has zero mixed second differences away from the border
+    ramp = np.fromfunction(lambda z, y, x: x + 2 * y + 3 * z, (D, H, W)).astype(np.float32)
+    O.lib().or_bayes_start(ramp.ctypes.data_as(O.C.POINTER(O.C.c_float)),
+                           dist.ctypes.data_as(O.C.POINTER(O.C.c_float)), W, H, D, lam)
+    assert np.all(dist[1:-1, 1:-1, 1:-1] == 0)
+
+
+def test_bayesian_iteration_backprojects_into_the_distance_volume(oracle_lib):
+    # with lambda = 0 and alpha = 1 one Bayesian iteration is a SIRT iteration whose
+    # projections all see the volume at the start of the iteration: for update = nproj
+    # (SIRT) that equals plain SIRT exactly
+    c = series_case(W=32, H=4, D=24, n=7, seed=2, noise=0.0)
+    meas = np.array([O.align(c["series"][i], c["T"][i], fill=O.FILL_NAN) for i in range(c["n"])], np.float32)
+    order = O.order_shuffle(c["eul"], 0)
+    a = np.zeros_like(c["vol"])
+    b = np.zeros_like(c["vol"])
+    O.ossart_iteration(a, c["g"], c["eul"], meas, order, 1.0, 0)
+    O.bayesian_iteration(b, c["g"], c["eul"], meas, order, 1.0, 0, 0.0, 1.0)
+    assert rel_l2(b, a) < 1e-6
+    # with subsets the Bayesian form differs (later subsets project the unchanged volume)
+    a2 = np.zeros_like(c["vol"])
+    b2 = np.zeros_like(c["vol"])
+    O.ossart_iteration(a2, c["g"], c["eul"], meas, order, 1.0, 2)
+    O.bayesian_iteration(b2, c["g"], c["eul"], meas, order, 1.0, 2, 0.0, 1.0)
+    assert rel_l2(b2, a2) > 1e-3
+
+
+def _median_cross_numpy(vol):
+    # BgARTVoxelProjector3D.medianFilter3Dcross written out independently
+    D, H, W = vol.shape
+    P = W * H
+    out = np.empty_like(vol)
+    flat = vol.reshape(D, P)
+    for z in range(D):
+        for idx in range(P):
+            nb = [flat[z - 1, idx] if z > 0 else 0.0, flat[z + 1, idx] if z < D - 1 else 0.0, flat[z, idx],
+                  flat[z, idx + 1] if idx + 1 < P else 0.0, flat[z, idx - 1] if idx - 1 > 0 else 0.0,
+                  flat[z, idx - W] if idx - W > 0 else 0.0, flat[z, idx + W] if idx + W < P else 0.0]
+            out.reshape(D, P)[z, idx] = sorted(nb)[3]
+    return out
+
+
+def test_bgart_median_cross_matches_its_definition(oracle_lib):
+    rng = np.random.default_rng(8)
+    vol = rng.normal(0, 1, (4, 5, 6)).astype(np.float32)
+    ref = _median_cross_numpy(vol)
+    got = O.bgart_median_cross(vol.copy())
+    assert np.array_equal(got, ref)
+
+
+def test_bgart_collapse_snaps_background_side_to_the_mode(oracle_lib):
+    rng = np.random.default_rng(9)
+    n = 20000
+    v = np.zeros(n, np.float32)
+    v[:12000] = rng.normal(0.0, 0.05, 12000)        # background around 0
+    v[12000:] = rng.uniform(0.5, 1.0, n - 12000)    # object
+    vol = v.reshape(10, 40, 50).copy()
+    k = 2.0
+    bg = O.bgart_collapse(vol, k, True)
+    # recompute the thresholds from the stated histogram rules
+    lo, hi = float(v.min()), float(v.max())
+    b = np.minimum(((v.astype(np.float64) - lo) * (256.0 / (hi - lo))).astype(np.int64), 255)
+    hist = np.bincount(b, minlength=256)
+    mi = int(np.argmax(hist))
+    binw = (hi - lo) / 256
+    mode = lo + mi * binw
+    centers = lo + np.arange(mi) * binw
+    sigma = np.sqrt(np.sum((centers - mode) ** 2 * hist[:mi]) / hist[:mi].sum())
+    assert bg == pytest.approx(mode)
+    expect = np.where(v.astype(np.float64) < mode + k * sigma, np.float32(mode), v).reshape(vol.shape)
+    assert np.array_equal(vol, expect)
+    # bright-background variant keeps the dark side and snaps the rest
+    vol2 = v.reshape(10, 40, 50).copy()
+    O.bgart_collapse(vol2, k, False)
+    expect2 = np.where(v.astype(np.float64) > mode - k * sigma, np.float32(mode), v).reshape(vol.shape)
+    assert np.array_equal(vol2, expect2)

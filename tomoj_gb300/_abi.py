@@ -92,6 +92,8 @@ SIGNATURES = {
     "tomo_set_weighting": (C.c_int32, [_P, C.c_int32, C.c_double, _f64p]),
     "tomo_set_tvm": (C.c_int32, [_P, C.c_float, C.c_float, C.c_float, C.c_int32]),
     "tomo_set_fista": (C.c_int32, [_P, C.c_int32]),
+    "tomo_set_bayesian": (C.c_int32, [_P, C.c_double, C.c_double, C.c_int32]),
+    "tomo_set_bgart": (C.c_int32, [_P, C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_int32]),
     "tomo_run_wbp": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "tomo_run_ossart": (C.c_int32, [_P, C.c_int32, C.c_double, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
                                     C.c_int32, _f64p]),

@@ -162,8 +162,8 @@ tomo_status build_plan(tomo_batch* b) {
                 for (int j = j0; j < g.h; j++) items.push_back(make_int4(di, g0, j, use_tma));
             reds[s].push_back(ErrReduce{a.errpart, p->d_err + slot, T, g.h});
             BpLaunch c{};
-            c.vol = p->vol();
-            c.vtype = p->vtype;
+            c.vol = p->bp_target();
+            c.vtype = p->bayes ? kVolF32 : p->vtype;
             c.vscale = p->d_vscale;
             c.vmax = p->d_vmax;
             c.img = a.diff;

@@ -31,7 +31,7 @@ namespace fpk {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kWaitTries = 1u << 24;
-constexpr size_t kMaxSmem = 112 * 1024;  // two CTAs per SM
+constexpr size_t kMaxSmem = kFpSmemBudget;
 
 struct Smem {
     int PW;
@@ -127,10 +127,62 @@ __device__ __forceinline__ float sample(const float2* __restrict__ P, long long 
     return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
 }
 
-// One CTA's work: projection row j, tilts [g0, g0 + tilts_per_cta) of problem `a`.
+// Detector column of ray slot (t, q) of thread tid: warps own blocks of 32 consecutive
+// columns (contiguous shared-memory reads).
+template <int QP>
+__device__ __forceinline__ int ray_column(int t, int q, int tid) {
+    (void)t;
+    return tid + q * kThreads;
+}
+
+// Partial chunk of one ray (it enters or leaves the volume inside the chunk):
+// branch-free, the load is predicated and an out-of-range sample adds fma(F, 0, 0) = 0.
+// Kept out of line: it is rare, and inlining it for every ray slot bloats the
+// instruction footprint of the sampling loop.
+struct PartialOut {
+    long long x;
+    float s;
+};
+static __device__ __noinline__ PartialOut partial_chunk(const float2* __restrict__ P, long long x, long long step, int lo,
+                                                 int cnt, int zc) {
+    float s = 0.0f;
+    for (int zz = 0; zz < zc; zz++) {
+        const bool in = (unsigned)(zz - lo) < (unsigned)cnt;
+        float2 p = make_float2(0.0f, 0.0f);
+        if (in) p = P[(int)(x >> 32)];
+        s += fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
+        x += step;
+    }
+    return PartialOut{x, s};
+}
+
+// Full chunk of one ray (all ZC planes inside): two interleaved sub-chains (even / odd
+// planes).  Returns the position after ZC steps and the chunk's sum.
+template <int ZC>
+__device__ __forceinline__ PartialOut full_chunk_inl(const float2* __restrict__ P, long long x, long long step) {
+    const long long s2 = 2 * step;
+    long long x0 = x, x1 = x + step;
+    float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+    for (int zz = 0; zz < ZC; zz += 2) {
+        a0 += sample(P, x0);
+        a1 += sample(P, x1);
+        x0 += s2;
+        x1 += s2;
+    }
+    return PartialOut{x0, a0 + a1};
+}
+template <int ZC>
+static __device__ __noinline__ PartialOut full_chunk_call(const float2* __restrict__ P, long long x, long long step) {
+    return full_chunk_inl<ZC>(P, x, step);
+}
+
+// One CTA's work: projection row j, tilts [g0, g0 + tilts_per_cta) of problem `a`,
+// depth part zp of a.zparts.
 template <int QP, int ZC>
-__device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma) {
-    constexpr int TGMAX = 16 / QP;
+__device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma,
+                                        const int zp) {
+    constexpr int TGMAX = kFpRays / QP > 0 ? kFpRays / QP : 1;
     constexpr int NR = TGMAX * QP;
     extern __shared__ __align__(16) unsigned char smem[];
     const Smem L = layout(ZC, a.W, TGMAX);
@@ -146,15 +198,21 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     const int TG = min(a.tilts_per_cta, a.T - g0);
     const int r = j - a.row_off;
     const bool row_in = (r >= 0 && r < H);
+    // chunks [c_begin, c_end) of the plane stack belong to this depth part
+    const int P = a.zparts > 1 ? a.zparts : 1;
+    const int nch_all = (D + ZC - 1) / ZC;
+    const int cpp = (nch_all + P - 1) / P;
+    const int c_begin = min(nch_all, zp * cpp);
+    const int c_end = min(nch_all, c_begin + cpp);
 
-    // ray k = t * QP + q: tilt g0 + t, detector column tid + q * kThreads
+    // ray k = t * QP + q: tilt g0 + t, detector column ray_column(t, q, tid)
     long long X[NR];
     float acc[NR];
     int zab[NR];
 #pragma unroll
     for (int k = 0; k < NR; k++) {
         const int t = k / QP, q = k % QP;
-        const int i = tid + q * kThreads;
+        const int i = ray_column<QP>(t, q, tid);
         acc[k] = 0.0f;
         X[k] = 0;
         zab[k] = 0;
@@ -163,7 +221,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             if (tid == 0 && q == 0) s_step[t] = a.ftilt[tilt].step;
             if (i < w && row_in) {
                 const FpRay ray = a.rays[(size_t)tilt * w + i];
-                X[k] = ray.X0;
+                X[k] = ray.X0 + (long long)(c_begin * ZC) * a.ftilt[tilt].step;
                 zab[k] = ray.zab;
             }
         } else if (tid == 0 && q == 0) {
@@ -171,8 +229,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
         }
     }
 
-    if (row_in) {
-        const int nchunks = (D + ZC - 1) / ZC;
+    if (row_in && c_begin < c_end) {
         const bool last_row = (r == H - 1);
         const long long pitch = (long long)PW << 32;  // one pair row in position units
         const int vt = a.vtype;
@@ -206,16 +263,17 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             fence_mbar_init();
         }
         __syncthreads();
-        stage(0);
-        for (int c = 0; c < nchunks; c++) {
+        stage(c_begin);
+        for (int c = c_begin; c < c_end; c++) {
             const int z0 = c * ZC;
             const int zc = min(ZC, D - z0);
+            const uint32_t parity = (uint32_t)((c - c_begin) & 1);
             if (use_tma) {
-                const bool ok = mbar_wait_bounded(bar, (uint32_t)(c & 1), kWaitTries);
+                const bool ok = mbar_wait_bounded(bar, parity, kWaitTries);
                 if (__syncthreads_or(!ok)) {
                     if (tid == 0) atomicOr(a.status, kStatusTimeout);
                     // let any copy still in flight land before the CTA's shared memory is released
-                    mbar_wait_bounded(bar, (uint32_t)(c & 1), kWaitTries);
+                    mbar_wait_bounded(bar, parity, kWaitTries);
                     return;
                 }
             } else {
@@ -233,7 +291,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                                                pairs + (size_t)zz * PW, W, flat);
             }
             __syncthreads();
-            if (c + 1 < nchunks && use_tma) stage(c + 1);
+            if (c + 1 < c_end && use_tma) stage(c + 1);
             const float2* P = pairs + 2;
 #pragma unroll
             for (int k = 0; k < NR; k++) {
@@ -245,19 +303,13 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 const bool none = (cnt == 0) || (za + cnt <= z0) || (za >= z0 + zc);
                 if (__all_sync(0xffffffffu, full) && zc == ZC) {
                     if (ZC >= 2) {
-                        // two interleaved sub-chains (even / odd planes)
-                        const long long s2 = 2 * (st + pitch);
-                        long long x0 = X[k], x1 = x0 + st + pitch;
-                        float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll
-                        for (int zz = 0; zz < ZC; zz += 2) {
-                            a0 += sample(P, x0);
-                            a1 += sample(P, x1);
-                            x0 += s2;
-                            x1 += s2;
-                        }
-                        X[k] = x0 - (long long)ZC * pitch;
-                        acc[k] += a0 + a1;
+#ifdef TOMO_FP_FULL_NOINLINE
+                        const PartialOut fo = full_chunk_call<ZC>(P, X[k], st + pitch);
+#else
+                        const PartialOut fo = full_chunk_inl<ZC>(P, X[k], st + pitch);
+#endif
+                        X[k] = fo.x - (long long)ZC * pitch;
+                        acc[k] += fo.s;
                     } else {
                         acc[k] += sample(P, X[k]);
                         X[k] += st;
@@ -265,8 +317,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 } else if (__all_sync(0xffffffffu, none)) {
                     X[k] += (long long)zc * st;
                 } else {
-                    // partial chunk: branch-free, the load is predicated and an
-                    // out-of-range sample adds fma(F, 0, 0) = 0
+#ifdef TOMO_FP_PARTIAL_INLINE
                     const int lo = za - z0;
                     long long x = X[k];
                     float s = 0.0f;
@@ -280,10 +331,47 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                     }
                     X[k] = x - (long long)zc * pitch;
                     acc[k] += s;
+#else
+                    const PartialOut po = partial_chunk(P, X[k], st + pitch, za - z0, cnt, zc);
+                    X[k] = po.x - (long long)zc * pitch;
+                    acc[k] += po.s;
+#endif
                 }
             }
             __syncthreads();
-            if (c + 1 < nchunks && !use_tma) stage(c + 1);
+            if (c + 1 < c_end && !use_tma) stage(c + 1);
+        }
+    }
+
+    // Depth split: publish this part's sums; the last part to arrive adds all parts in
+    // order (deterministic) and runs the epilogue.
+    if (P > 1) {
+        __shared__ int s_last;
+#pragma unroll
+        for (int k = 0; k < NR; k++) {
+            const int t = k / QP, q = k % QP;
+            const int i = ray_column<QP>(t, q, tid);
+            if (t < TG && i < w) a.part[(((size_t)zp * a.T + g0 + t) * h + j) * w + i] = acc[k];
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            unsigned* tk = a.tickets + (size_t)(g0 / a.tilts_per_cta) * h + j;
+            const unsigned ticket = atomicAdd(tk, 1u);
+            s_last = (ticket == (unsigned)(P - 1));
+            if (s_last) *tk = 0u;  // every part has arrived: ready for the next launch
+        }
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+#pragma unroll
+        for (int k = 0; k < NR; k++) {
+            const int t = k / QP, q = k % QP;
+            const int i = ray_column<QP>(t, q, tid);
+            float sum = 0.0f;
+            if (t < TG && i < w)
+                for (int pp = 0; pp < P; pp++) sum += __ldcg(a.part + (((size_t)pp * a.T + g0 + t) * h + j) * w + i);
+            acc[k] = sum;
         }
     }
 
@@ -299,7 +387,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
         double e2 = 0.0;
 #pragma unroll
         for (int q = 0; q < QP; q++) {
-            const int i = tid + q * kThreads;
+            const int i = ray_column<QP>(t, q, tid);
             if (i >= w) continue;
             const int cnt = (int)((uint32_t)zab[t * QP + q] >> 16);
             float th, nrm;
@@ -341,16 +429,16 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
 }
 
 template <int QP, int ZC>
-__global__ void __launch_bounds__(kThreads, 2) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
-    fp_body<QP, ZC>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma);
+__global__ void __launch_bounds__(kThreads, kFpCtasPerSm) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
+    fp_body<QP, ZC>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
 }
 
 // Batched form: CTA b works on item {problem, first tilt, row, use_tma} of many problems.
 template <int QP, int ZC>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kFpCtasPerSm)
     fp_kernel_batch(const FpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
-    fp_body<QP, ZC>(descs[it.x], it.y, it.z, it.w);
+    fp_body<QP, ZC>(descs[it.x], it.y, it.z, it.w, 0);
 }
 
 template <int QP, int ZC>
@@ -374,17 +462,17 @@ cudaError_t set_attr_qp() {
 // Largest chunk (planes per stage) whose shared memory fits two CTAs per SM.
 inline int choose_zc(int W) {
     for (int zc = 16; zc > 1; zc >>= 1)
-        if (layout(zc, W, 16).total <= kMaxSmem) return zc;
+        if (layout(zc, W, kFpRays > 0 ? kFpRays : 1).total <= kMaxSmem) return zc;
     return 1;
 }
 
 template <int QP>
 cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     const int ZC = choose_zc(a.W);
-    const Smem L = layout(ZC, a.W, 16 / QP);
+    const Smem L = layout(ZC, a.W, kFpRays / QP > 0 ? kFpRays / QP : 1);
     if (L.total > kMaxSmem) return cudaErrorInvalidValue;
     const int use_tma = fp_use_tma(a.W, a.vtype, a.vol);
-    dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0);
+    dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0, a.zparts > 1 ? a.zparts : 1);
     switch (ZC) {
         case 16: fp_kernel<QP, 16><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
         case 8: fp_kernel<QP, 8><<<grid, kThreads, L.total, s>>>(a, use_tma); break;

@@ -38,11 +38,11 @@ cudaError_t fp_init_attributes() {
 
 int fp_max_tilts_per_cta(int w) {
     const int qp = (w + kFpThreads - 1) / kFpThreads;
-    if (qp <= 1) return 16;
-    if (qp <= 2) return 8;
-    if (qp <= 4) return 4;
-    if (qp <= 8) return 2;
-    if (qp <= 16) return 1;
+    if (qp <= 1) return kFpRays;
+    if (qp <= 2) return kFpRays / 2;
+    if (qp <= 4) return kFpRays / 4;
+    if (qp <= 8) return kFpRays / 8;
+    if (qp <= 16) return kFpRays / 16 > 0 ? kFpRays / 16 : 1;
     return 0;
 }
 
@@ -57,14 +57,39 @@ size_t fp_smem_bytes(int ZC, int W, int qp) {
     o = (o + 15) & ~(size_t)15;
     o += (size_t)ZC * (W + 4) * sizeof(float2);
     o = (o + 15) & ~(size_t)15;
-    o += (kFpThreads / 32) * sizeof(double) + (size_t)(16 / qp) * sizeof(long long);
+    o += (kFpThreads / 32) * sizeof(double) + (size_t)(kFpRays / qp > 0 ? kFpRays / qp : 1) * sizeof(long long);
     return o;
 }
 
 int fp_choose_zc(int W) {
     for (int zc = 16; zc > 1; zc >>= 1)
-        if (fp_smem_bytes(zc, W, 1) <= 112 * 1024) return zc;
+        if (fp_smem_bytes(zc, W, 1) <= kFpSmemBudget) return zc;
     return 1;
+}
+
+#ifndef TOMO_FP_MAX_ZPARTS
+#define TOMO_FP_MAX_ZPARTS 8
+#endif
+
+int fp_zparts(int ctas, int D, int zc, int sms) {
+    const int slots = kFpCtasPerSm * sms;  // resident forward-projector CTAs
+    if (ctas <= 0 || ctas >= slots) return 1;
+    const int nch = (D + zc - 1) / zc;
+    // A CTA's time is about (chunks + 1) chunk-times (the +1 is its set-up, first
+    // bulk copy and partial-sum exchange), independent of what else runs on its SM:
+    // minimise waves x (chunks per part + 1).
+    int best = 1;
+    long long best_cost = (long long)nch + 1;
+    for (int P = 2; P <= TOMO_FP_MAX_ZPARTS && P <= nch; P++) {
+        const int cpp = (nch + P - 1) / P;
+        const long long waves = ((long long)ctas * P + slots - 1) / slots;
+        const long long cost = waves * (cpp + 1);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = P;
+        }
+    }
+    return best;
 }
 
 cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,

@@ -195,6 +195,172 @@ __global__ void fista_kernel(float* rec, const float* __restrict__ prev, size_t 
     }
 }
 
+// BayesianVoxelProjector3D.startOfIteration -> convolve(rec, kernel, distanceVolume, -lambda)
+// (TomoJ_AdvancedReconstruction/.../projectors/BayesianVoxelProjector3D.java:131-134, 168-194):
+// the 27-point stencil [1,-2,1]^3 over TomoReconstruction2.getCubicNeightborhoodWithClamp
+// (TomoReconstruction2.java:317-339), whose out-of-volume neighbours read 0 through getPixel;
+// float products (exact: the weights are powers of two) summed in double in the reference's
+// neighbour order (x offset outermost, z innermost), times factor, rounded to float.
+__global__ void bayes_conv_kernel(const float* __restrict__ rec, float* __restrict__ dist, int W, int H, int D,
+                                  double factor) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const float k1[3] = {1.0f, -2.0f, 1.0f};
+    double total = 0.0;
+#pragma unroll
+    for (int i = -1; i <= 1; i++)
+#pragma unroll
+        for (int j = -1; j <= 1; j++)
+#pragma unroll
+            for (int k = -1; k <= 1; k++) {
+                const int xx = x + i, yy = y + j, zz = z + k;
+                float v = 0.0f;
+                if (xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D)
+                    v = rec[((size_t)zz * H + yy) * W + xx];
+                total = __dadd_rn(total, (double)__fmul_rn(v, k1[i + 1] * k1[j + 1] * k1[k + 1]));
+            }
+    dist[((size_t)z * H + y) * W + x] = __double2float_rn(__dmul_rn(total, factor));
+}
+
+// BayesianVoxelProjector3D.endOfIteration (:119-129): distance *= alpha (float pixel times
+// double, rounded to float), volume += distance (float), then positivity (max with 0).
+__global__ void bayes_apply_kernel(float* rec, float* dist, size_t n, double alpha, int positivity) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float d = __double2float_rn(__dmul_rn((double)dist[i], alpha));
+        dist[i] = d;
+        float v = __fadd_rn(d, rec[i]);
+        if (positivity && 0.0f > v) v = 0.0f;
+        rec[i] = v;
+    }
+}
+
+// ---- BgARTVoxelProjector3D (TomoJ_AdvancedReconstruction/.../BgARTVoxelProjector3D.java) ----
+
+// Order-preserving unsigned key of a float (-0.0 before 0.0), and back.
+__device__ __forceinline__ unsigned float_key(float f) {
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+// Java's Arrays.sort(float[]) order: as float_key, with NaN last.
+__device__ __forceinline__ unsigned java_sort_key(float f) { return isnan(f) ? 0xFFFFFFFFu : float_key(f); }
+
+// keys[0] = min key, keys[1] = max key over the non-NaN voxels (keys preset to ~0 / 0).
+__global__ void bg_minmax_kernel(const float* __restrict__ v, size_t n, unsigned* keys) {
+    unsigned lo = 0xFFFFFFFFu, hi = 0u;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float f = v[i];
+        if (isnan(f)) continue;
+        const unsigned k = float_key(f);
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(keys, lo);
+        atomicMax(keys + 1, hi);
+    }
+}
+
+// ImageJ StackStatistics histogram of 32-bit data: 256 bins over [min, max], bin
+// (int)((v - min) * (256 / (max - min))) clamped to 255, all in bin 0 when max == min.
+__global__ void bg_hist_kernel(const float* __restrict__ v, size_t n, const unsigned* keys,
+                               unsigned long long* hist) {
+    __shared__ unsigned h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const double lo = key_float(keys[0]), hi = key_float(keys[1]);
+    const double scale = __ddiv_rn(256.0, hi - lo);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float f = v[i];
+        if (isnan(f)) continue;
+        int b = 0;
+        if (hi > lo) {
+            b = (int)__dmul_rn((double)f - lo, scale);  // truncation toward zero, as Java's (int)
+            if (b > 255) b = 255;
+        }
+        atomicAdd(&h[b], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (h[i]) atomicAdd(hist + i, (unsigned long long)h[i]);
+}
+
+// collapseFilter thresholds (:29-83) in one thread: out = {background, th1, th2}.
+__global__ void bg_finalize_kernel(const unsigned* keys, const unsigned long long* hist, double k, double bg_value,
+                                   double* out) {
+    const double histmin = key_float(keys[0]), histmax = key_float(keys[1]);
+    const double bin = (histmax - histmin) / 256;
+    double best = 0;
+    int max_index = 0;
+    for (int i = 0; i < 256; i++)
+        if ((double)hist[i] > best) {
+            best = (double)hist[i];
+            max_index = i;
+        }
+    const double bg = isnan(bg_value) ? __dadd_rn(histmin, __dmul_rn((double)max_index, bin)) : bg_value;
+    double sigma = 0;
+    long long count = 0;
+    for (int i = 0; i < max_index; i++) {
+        const double d = __dsub_rn(__dadd_rn(histmin, __dmul_rn((double)i, bin)), bg);
+        sigma = __dadd_rn(sigma, __dmul_rn(__dmul_rn(d, d), (double)hist[i]));
+        count += (long long)hist[i];
+    }
+    sigma = __dsqrt_rn(__ddiv_rn(sigma, (double)count));
+    out[0] = bg;
+    out[1] = __dsub_rn(bg, __dmul_rn(k, sigma));
+    out[2] = __dadd_rn(bg, __dmul_rn(k, sigma));
+}
+
+__global__ void bg_apply_kernel(float* v, size_t n, const double* out, int dark_bg) {
+    const double bg = out[0], th1 = out[1], th2 = out[2];
+    const float bgf = __double2float_rn(bg);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double val = v[i];
+        if (dark_bg && val < th2) v[i] = bgf;
+        if (!dark_bg && val > th1) v[i] = bgf;
+    }
+}
+
+// medianFilter3Dcross (:117-145) from the copy `src` into `dst`: the voxel, its z
+// neighbours (0 outside) and its in-plane neighbours by flat index within the slice
+// (x neighbours wrap across rows; -1 / -W need an index > 0, +1 / +W one < W*H).
+__global__ void median_cross_kernel(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int D) {
+    const long long P = (long long)W * H;
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int z = blockIdx.y;
+    if (idx >= P) return;
+    const float* cur = src + P * z;
+    float nb[7];
+    nb[0] = z > 0 ? cur[idx - P] : 0.0f;
+    nb[1] = z < D - 1 ? cur[idx + P] : 0.0f;
+    nb[2] = cur[idx];
+    nb[3] = (idx + 1 < P) ? cur[idx + 1] : 0.0f;
+    nb[4] = (idx - 1 > 0) ? cur[idx - 1] : 0.0f;
+    nb[5] = (idx - W > 0) ? cur[idx - W] : 0.0f;
+    nb[6] = (idx + W < P) ? cur[idx + W] : 0.0f;
+    unsigned key[7];
+#pragma unroll
+    for (int a = 0; a < 7; a++) key[a] = java_sort_key(nb[a]);
+    // rank selection: the element with 3 keys below it (ties broken by position) is the median
+    float med = nb[0];
+#pragma unroll
+    for (int a = 0; a < 7; a++) {
+        int below = 0;
+#pragma unroll
+        for (int b = 0; b < 7; b++) below += (key[b] < key[a]) || (key[b] == key[a] && b < a);
+        if (below == 3) med = nb[a];
+    }
+    dst[P * z + idx] = med;
+}
+
 // Long-object compensation: every norm pixel of a projection becomes the projection's maximum.
 __global__ void long_object_kernel(float* norm, int npix) {
     __shared__ float red[32];
@@ -365,6 +531,49 @@ cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor,
     if (n == 0) return cudaSuccess;
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
     fista_kernel<<<blocks, 256, 0, s>>>(rec, prev, n, factor);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bayes_conv(const float* rec, float* dist, int W, int H, int D, double factor, cudaStream_t s) {
+    dim3 grid((W + 127) / 128, H, D);
+    bayes_conv_kernel<<<grid, 128, 0, s>>>(rec, dist, W, H, D, factor);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bayes_apply(float* rec, float* dist, size_t n, double alpha, int positivity, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    bayes_apply_kernel<<<blocks, 256, 0, s>>>(rec, dist, n, alpha, positivity);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bgart_collapse(float* vol, size_t n, double k, int dark_bg, double bg_value, void* scratch,
+                                  cudaStream_t s) {
+    unsigned* keys = static_cast<unsigned*>(scratch);
+    unsigned long long* hist = reinterpret_cast<unsigned long long*>(static_cast<char*>(scratch) + 16);
+    double* out = reinterpret_cast<double*>(static_cast<char*>(scratch) + 16 + 256 * 8);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(keys, 0xFF, 4, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(keys + 1, 0, 4, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(hist, 0, 256 * 8, s)) != cudaSuccess) return e;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+    bg_minmax_kernel<<<blocks, 256, 0, s>>>(vol, n, keys);
+    bg_hist_kernel<<<blocks, 256, 0, s>>>(vol, n, keys, hist);
+    bg_finalize_kernel<<<1, 1, 0, s>>>(keys, hist, k, bg_value, out);
+    bg_apply_kernel<<<blocks, 256, 0, s>>>(vol, n, out, dark_bg);
+    count_launch(4);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bgart_median(float* vol, float* tmp, int W, int H, int D, cudaStream_t s) {
+    const size_t n = (size_t)W * H * D;
+    cudaError_t e = cudaMemcpyAsync(tmp, vol, sizeof(float) * n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    const long long P = (long long)W * H;
+    median_cross_kernel<<<dim3((unsigned)((P + 255) / 256), D), 256, 0, s>>>(tmp, vol, W, H, D);
     count_launch();
     return cudaGetLastError();
 }

@@ -81,6 +81,8 @@ tomo_status check_status(tomo_projector* p) {
     CK(cudaStreamSynchronize(p->stream));
     if (st != 0) {
         CK(cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream));
+        // a kernel that gave up may have left depth-split tickets behind
+        if (p->d_tickets) CK(cudaMemsetAsync(p->d_tickets, 0, sizeof(unsigned) * p->tickets_cap, p->stream));
         std::string why;
         if (st & kStatusTimeout) why += " (bounded wait expired)";
         if (st & (int)kStatusRange) why += " (a volume value left the FP16 range of its slab scale)";
@@ -120,6 +122,45 @@ int auto_tilts_per_cta(const tomo_projector* p, int T, int rows) {
     if (p->tilts_per_cta > 0) return std::min(p->tilts_per_cta, tgmax);
     const int groups = (T + tgmax - 1) / tgmax;
     return (T + groups - 1) / groups;
+}
+
+// Depth split of a forward projection of T tilts over rows [j0, j1): the number of
+// parts, after making sure the scratch exists.  Scratch is only allocated outside
+// stream capture; a captured launch that lacks it runs unsplit.
+int fp_split(tomo_projector* p, int T, int rows, int tpc) {
+    const Geometry& g = p->g;
+    const int groups = (T + tpc - 1) / tpc;
+    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W), p->sms);
+    if (P <= 1) return 1;
+    const size_t need_part = (size_t)P * T * p->npix;
+    const size_t need_tk = (size_t)groups * g.h;
+    if (need_part <= p->fppart_cap && need_tk <= p->tickets_cap) return P;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 1;
+    auto release = [&](void* q, size_t bytes) {
+        if (!q) return;
+        cudaFree(q);
+        for (auto& a : p->allocs)
+            if (a == q) a = nullptr;
+        g_in_use -= bytes;
+        p->bytes -= bytes;
+    };
+    if (need_part > p->fppart_cap) {
+        release(p->d_fppart, sizeof(float) * p->fppart_cap);
+        p->d_fppart = nullptr;
+        p->fppart_cap = 0;
+        if (alloc_n(p, &p->d_fppart, need_part) != TOMO_OK) return 1;
+        p->fppart_cap = need_part;
+    }
+    if (need_tk > p->tickets_cap) {
+        release(p->d_tickets, sizeof(unsigned) * p->tickets_cap);
+        p->d_tickets = nullptr;
+        p->tickets_cap = 0;
+        if (alloc_n(p, &p->d_tickets, need_tk) != TOMO_OK) return 1;
+        if (cudaMemsetAsync(p->d_tickets, 0, sizeof(unsigned) * need_tk, p->stream) != cudaSuccess) return 1;
+        p->tickets_cap = need_tk;
+    }
+    return P;
 }
 
 // Forward projection of the current batch, with the fused difference when meas is given.
@@ -163,6 +204,9 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
     a.j0 = j0;
     a.j1 = j1;
     a.tilts_per_cta = auto_tilts_per_cta(p, T, j1 - j0);
+    a.zparts = fp_split(p, T, j1 - j0, a.tilts_per_cta);
+    a.part = p->d_fppart;
+    a.tickets = p->d_tickets;
     a.W = g.W;
     a.H = g.H;
     a.D = g.D;
@@ -200,14 +244,18 @@ tomo_status bp_post(tomo_projector* p, cudaStream_t s) {
     return TOMO_OK;
 }
 
-tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int T, int y0, int y1, bool sanitize) {
+// Backprojection of T images into volume rows [y0, y1).  `diffs`: the images are
+// differences of an update, which a Bayesian handle adds to its distance volume.
+tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int T, int y0, int y1, bool sanitize,
+                   bool diffs) {
     const Geometry& g = p->g;
     y0 = std::max(0, y0);
     y1 = std::min(g.H, y1);
     if (y1 <= y0 || T <= 0) return TOMO_OK;
+    const bool to_dist = diffs && p->bayes;
     BpLaunch a{};
-    a.vol = p->vol();
-    a.vtype = p->vtype;
+    a.vol = to_dist ? p->bp_target() : p->vol();
+    a.vtype = to_dist ? kVolF32 : p->vtype;
     a.vscale = p->d_vscale;
     a.vmax = p->d_vmax;
     a.img = imgs;
@@ -226,6 +274,10 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     a.positivity = p->params.positivity;
     a.sanitize = sanitize || p->vol_nonfinite;
     a.status = p->d_status;
+    if (to_dist) {
+        CK(launch_bp_separable(a, p->stream));
+        return TOMO_OK;
+    }
     CKS(bp_pre(p, p->stream));
     CK(launch_bp_separable(a, p->stream));
     CKS(bp_post(p, p->stream));
@@ -270,6 +322,10 @@ tomo_status tv_denoise(tomo_projector* p) {
 }
 
 tomo_status end_iteration(tomo_projector* p) {
+    if (p->bayes)
+        CK(launch_bayes_apply(p->d_vol, p->d_dist, p->nvox, p->bayes_alpha, p->params.positivity, p->stream));
+    if (p->bgart)
+        CK(launch_bgart_collapse(p->d_vol, p->nvox, p->bg_k, p->bg_dark, p->bg_value, p->d_bgscratch, p->stream));
     CKS(tv_denoise(p));
     if (p->fista) {
         const double t_1 = p->fista_t;
@@ -281,6 +337,9 @@ tomo_status end_iteration(tomo_projector* p) {
 }
 
 tomo_status start_iteration(tomo_projector* p) {
+    if (p->bgart && p->bg_median) CK(launch_bgart_median(p->d_vol, p->d_bgtmp, p->g.W, p->g.H, p->g.D, p->stream));
+    if (p->bayes)
+        CK(launch_bayes_conv(p->d_vol, p->d_dist, p->g.W, p->g.H, p->g.D, -p->bayes_lambda, p->stream));
     if (p->fista)
         CK(cudaMemcpyAsync(p->d_prev, p->d_vol, sizeof(float) * p->nvox, cudaMemcpyDeviceToDevice, p->stream));
     return TOMO_OK;
@@ -342,6 +401,10 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
     }
     p->vtype = p->params.precision;  // TOMO_PREC_* values equal the storage types
     cudaGetDevice(&p->device);
+    if (cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+        cudaGetLastError();
+        p->sms = 1;
+    }
     p->npix = (size_t)g.w * g.h;
     p->nvox = (size_t)g.W * g.H * g.D;
     const size_t N = (size_t)g.N;
@@ -677,6 +740,8 @@ tomo_status tomo_backproject(tomo_projector* p, int32_t y0, int32_t y1) {
     if (T == 0) return TOMO_OK;
     const float* imgs;
     bool sanitize;
+    // BayesianVoxelProjector3D.backproject only acts on differences (:77-116)
+    if (p->bayes && !p->diffs_valid) return TOMO_OK;
     if (p->diffs_valid) {
         CKS(apply_weighting(p, p->d_diff, T));
         imgs = p->d_diff;
@@ -690,7 +755,7 @@ tomo_status tomo_backproject(tomo_projector* p, int32_t y0, int32_t y1) {
         imgs = p->d_obatch;
         sanitize = p->meas_has_nan || p->meas_has_inf;
     }
-    CKS(run_bp(p, imgs, p->d_batch, T, y0, y1, sanitize));
+    CKS(run_bp(p, imgs, p->d_batch, T, y0, y1, sanitize, p->diffs_valid));
     CKS(check_status(p));
     return TOMO_OK;
 }
@@ -790,6 +855,37 @@ tomo_status tomo_set_fista(tomo_projector* p, int32_t enabled) {
     return TOMO_OK;
 }
 
+tomo_status tomo_set_bayesian(tomo_projector* p, double lambda, double alpha, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (enabled && p->vtype != kVolF32)
+        return fail(TOMO_ERR_UNSUPPORTED, "the Bayesian regulariser needs the FP32 volume (precision TOMO_PREC_FP32)");
+    if (enabled && !p->d_dist) CKS(alloc_n(p, &p->d_dist, p->nvox));
+    p->bayes = enabled != 0;
+    p->bayes_lambda = lambda;
+    p->bayes_alpha = alpha;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_bgart(tomo_projector* p, double k, int32_t dark_bg, int32_t do_median, double bg_value,
+                           int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (enabled && p->vtype != kVolF32)
+        return fail(TOMO_ERR_UNSUPPORTED, "the BgART filters need the FP32 volume (precision TOMO_PREC_FP32)");
+    if (enabled && !p->d_bgscratch) CKS(dalloc(p, &p->d_bgscratch, kBgScratchBytes));
+    if (enabled && do_median && !p->d_bgtmp) CKS(alloc_n(p, &p->d_bgtmp, p->nvox));
+    p->bgart = enabled != 0;
+    p->bg_k = k;
+    p->bg_dark = dark_bg != 0;
+    p->bg_median = do_median != 0;
+    p->bg_value = bg_value;
+    if (p->bgart) {
+        // the reference's constructor collapses the starting volume once (BgARTVoxelProjector3D.java:22-27)
+        CK(launch_bgart_collapse(p->d_vol, p->nvox, k, p->bg_dark, bg_value, p->d_bgscratch, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+    }
+    return TOMO_OK;
+}
+
 tomo_status tomo_set_profiling(tomo_projector* p, int32_t enabled) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
     p->profile = enabled != 0;
@@ -847,7 +943,7 @@ tomo_status tomo_run_wbp(tomo_projector* p, int32_t y0, int32_t y1) {
     CK(cudaMemcpyAsync(p->d_batch, all.data(), sizeof(int) * N, cudaMemcpyHostToDevice, p->stream));
     CK(launch_gather(p->d_obatch, p->d_meas, p->d_batch, N, p->npix, p->stream));
     CKS(apply_weighting(p, p->d_obatch, N));
-    CKS(run_bp(p, p->d_obatch, p->d_batch, N, y0, y1, p->meas_has_nan || p->meas_has_inf));
+    CKS(run_bp(p, p->d_obatch, p->d_batch, N, y0, y1, p->meas_has_nan || p->meas_has_inf, false));
     CKS(check_status(p));
     p->batch.clear();
     p->batch_uploaded = false;
@@ -893,6 +989,13 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
             p->ev.push_back(e);
         }
     }
+    {
+        // depth-split scratch for the subset sizes of this run, before any capture
+        int j0, j1;
+        fp_rows(p, y0, &j0, &j1);
+        for (int T : {upd, N - (nsub - 1) * upd})
+            if (T > 0) fp_split(p, T, j1 - j0, auto_tilts_per_cta(p, T, j1 - j0));
+    }
     auto body = [&](const int* d_ord) -> tomo_status {
         CKS(start_iteration(p));
         for (int s = 0, k = 0; s < N; s += upd, k++) {
@@ -900,7 +1003,7 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
             if (p->profile) CK(cudaEventRecordWithFlags(p->ev[4 * k + 0], p->stream, cudaEventRecordExternal));
             CKS(run_fp(p, d_ord + s, T, y0, true, factor, s));
             if (p->profile) CK(cudaEventRecordWithFlags(p->ev[4 * k + 1], p->stream, cudaEventRecordExternal));
-            CKS(run_bp(p, p->d_diff + (size_t)s * p->npix, d_ord + s, T, y0, y1, p->meas_has_inf));
+            CKS(run_bp(p, p->d_diff + (size_t)s * p->npix, d_ord + s, T, y0, y1, p->meas_has_inf, true));
             if (p->profile) CK(cudaEventRecordWithFlags(p->ev[4 * k + 2], p->stream, cudaEventRecordExternal));
         }
         CKS(end_iteration(p));

@@ -65,8 +65,26 @@ struct tomo_projector {
     int tv_iters = 0;
     bool fista = false;
     double fista_t = 0.0;
+    // BayesianVoxelProjector3D: differences go to d_dist, applied at the end of an iteration
+    bool bayes = false;
+    double bayes_lambda = 0.1, bayes_alpha = 0.1;
+    float* d_dist = nullptr;
+    // BgARTVoxelProjector3D: cross median before, histogram collapse after every iteration
+    bool bgart = false;
+    double bg_k = 0.0, bg_value = 0.0;
+    int bg_dark = 1, bg_median = 1;
+    void* d_bgscratch = nullptr;
+    float* d_bgtmp = nullptr;
+    // volume a backprojection of differences adds to
+    void* bp_target() const { return bayes ? static_cast<void*>(d_dist) : vol(); }
     std::atomic<int> cancel{0};
     int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+    int sms = 0;            // multiprocessors of the device
+    // forward-projector depth split scratch (partial ray sums, per-group tickets)
+    float* d_fppart = nullptr;
+    size_t fppart_cap = 0;  // floats
+    unsigned* d_tickets = nullptr;
+    size_t tickets_cap = 0;
     // per-kernel timing of the OS-SART driver (tomo_set_profiling)
     bool profile = false;
     std::vector<cudaEvent_t> ev;

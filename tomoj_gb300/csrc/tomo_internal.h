@@ -20,6 +20,18 @@ namespace tomo {
 
 constexpr double kFix = 4294967296.0;  // 2^32: fixed-point scale of positions
 
+// Forward-projector occupancy: rays per thread (tilts per CTA x detector columns per
+// thread) and resident CTAs per SM, which sets the shared-memory budget of a CTA.
+#ifndef TOMO_FP_RAYS
+#define TOMO_FP_RAYS 16
+#endif
+#ifndef TOMO_FP_MIN_BLOCKS
+#define TOMO_FP_MIN_BLOCKS 2
+#endif
+constexpr int kFpRays = TOMO_FP_RAYS;
+constexpr int kFpCtasPerSm = TOMO_FP_MIN_BLOCKS;
+constexpr size_t kFpSmemBudget = (kFpCtasPerSm <= 2 ? 112 : 227 / kFpCtasPerSm - 1) * 1024;
+
 // Device status word bits written by kernels (never trap: the host reads them).
 constexpr int kStatusTimeout = 1;       // an mbarrier wait exceeded its iteration budget
 constexpr unsigned kStatusRange = 4u;   // a volume value left the FP16 range of its slab scale
@@ -92,8 +104,17 @@ struct FpLaunch {
     int W, H, D, w, h;
     int row_off;
     int* status;            // device error word
+    // Depth split: zparts CTAs share each (tilt group, row), each summing its own run of
+    // planes; partial ray sums go to part[zparts][T][h][w] and the last CTA of the group
+    // (ticket in tickets[groups][h], left at zero) adds them in part order and finishes.
+    int zparts;             // 0 or 1: no split
+    float* part;
+    unsigned* tickets;
 };
 cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s);
+// Depth parts for `ctas` (tilt group, row) CTAs: balances the grid over the resident
+// CTA slots of the device (1 = no split).
+int fp_zparts(int ctas, int D, int zc, int sms);
 // Plane rows are staged with bulk copies when every row starts on a 16-byte boundary.
 inline int fp_use_tma(int W, int vtype, const void* vol) {
     return ((W * vol_elem_bytes(vtype)) % 16 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
@@ -154,6 +175,16 @@ cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* 
 cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s);
 cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s);
 cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s);
+// Bayesian regularisation (BayesianVoxelProjector3D): dist = factor * stencil(rec); and
+// dist *= alpha, rec += dist (+ positivity).
+cudaError_t launch_bayes_conv(const float* rec, float* dist, int W, int H, int D, double factor, cudaStream_t s);
+cudaError_t launch_bayes_apply(float* rec, float* dist, size_t n, double alpha, int positivity, cudaStream_t s);
+// BgART (BgARTVoxelProjector3D): histogram collapse filter (scratch: kBgScratchBytes) and
+// the 7-point cross median (tmp: a volume-sized copy).
+constexpr size_t kBgScratchBytes = 16 + 256 * 8 + 3 * 8;
+cudaError_t launch_bgart_collapse(float* vol, size_t n, double k, int dark_bg, double bg_value, void* scratch,
+                                  cudaStream_t s);
+cudaError_t launch_bgart_median(float* vol, float* tmp, int W, int H, int D, cudaStream_t s);
 
 // Reduced-precision volume storage (kernels_vol.cu).  `src`/`dst` float buffers are
 // laid out [D][rows][W] and cover volume rows [y0, y0 + rows).

@@ -203,6 +203,43 @@ class VoxelProjector3D(Projector):
         return out
 
 
+class BayesianVoxelProjector3D(VoxelProjector3D):
+    """BayesianVoxelProjector3D (TomoJ_AdvancedReconstruction/.../projectors/
+    BayesianVoxelProjector3D.java): the differences of an iteration accumulate in a
+    distance volume seeded with -lambda times the 27-point [1,-2,1]^3 stencil of the
+    volume, and alpha times it is added to the volume at the end of the iteration."""
+
+    def __init__(self, ts, rec, weighting=None, **kw):
+        super().__init__(ts, rec, weighting, **kw)
+        self.regularizationLambda = 0.1
+        self.regularizationAlpha = 0.1
+        self._apply()
+
+    def _apply(self):
+        check(self._lib.tomo_set_bayesian(self._h, float(self.regularizationLambda),
+                                          float(self.regularizationAlpha), 1))
+
+    def setRegularizationLambda(self, v: float):
+        self.regularizationLambda = float(v)
+        self._apply()
+
+    def setRegularizationAlpha(self, v: float):
+        self.regularizationAlpha = float(v)
+        self._apply()
+
+
+class BgARTVoxelProjector3D(VoxelProjector3D):
+    """BgARTVoxelProjector3D (TomoJ_AdvancedReconstruction/.../projectors/
+    BgARTVoxelProjector3D.java): cross median before and histogram collapse filter
+    after every iteration; the constructor collapses the starting volume once."""
+
+    def __init__(self, ts, rec, weighting, k, darkBG=True, doMedian=True, **kw):
+        super().__init__(ts, rec, weighting, **kw)
+        self.k, self.darkBG, self.doMedian = float(k), bool(darkBG), bool(doMedian)
+        self.bgValue = float("nan")
+        check(self._lib.tomo_set_bgart(self._h, self.k, int(self.darkBG), int(self.doMedian), self.bgValue, 1))
+
+
 def first_index(seed: int, iteration: int, nproj: int) -> int:
     """Deterministic replacement of orderShuffleART's Math.random() first index."""
     return int(_abi.load().tomo_first_index(int(seed), int(iteration), int(nproj)))

@@ -110,9 +110,163 @@ class AffineAlignment:
             T = _flat(_mat(E) @ _mat(T))
         return T
 
+    def addTransform(self, index, T):
+        """AffineAlignment.addTransform (AffineAlignment.java:97-102): transforms[i] <- transforms[i] * T."""
+        self.transforms[index] = concatenate(self.transforms[index], tuple(float(v) for v in T))
+
+    def addToZeroTransform(self, T):
+        """AffineAlignment.addToZeroTransform (:118-124)."""
+        self.zeroT = concatenate(self.zeroT, tuple(float(v) for v in T))
+
+    def getZeroTransform(self):
+        return self.zeroT
+
+    def setTiltAxisVertical(self, value: bool):
+        self.tiltAxisVertical = bool(value)
+
+    def convertTolocalTransform(self):
+        """AffineAlignment.convertTolocalTransform (:337-380): final (per-image) transforms
+        become the zero-tilt transform plus transforms between consecutive images, going
+        forward from the zero tilt with getTransform(i - 1) of the state built so far, and
+        backward with the inverse of getTransform(i + 1)."""
+        self.combine = True
+        old = list(self.transforms)
+        self.transforms = [IDENTITY] * len(old)
+        z = self.ts.zeroindex
+        self.setZeroTransform(old[z])
+        for i in range(z + 1, len(old)):
+            T = concatenate(inverse(old[i]), self.getTransform(i - 1))
+            self.transforms[i - 1] = T
+        for i in range(z - 1, -1, -1):
+            T0 = inverse(self.getTransform(i + 1))
+            self.transforms[i] = concatenate(T0, old[i])  # T.preConcatenate(T0) = T0 * T
+
+    def loadFromFile(self, path: str, binning: float = 1.0, finalTransforms: bool = False,
+                     combineWithExisting: bool = False, tiff2mrc: bool = False):
+        """AffineAlignment.loadFromFile (:420-507): IMOD .xf / .prexg (final transforms
+        a11 a12 a21 a22 dx dy per line, read as AffineTransform's flat matrix, shifts
+        times binning, all negated for tiff2mrc stacks, then converted to local
+        transforms), IMOD .prexf (consecutive transforms, shifts negated, the first
+        line belongs to the last image), or a TomoJ csv / txt file (angle, tilt axis and
+        six matrix values per image; the zero-tilt transform on the last line unless
+        the transforms are final)."""
+        n = self.ts.getImageStackSize()
+
+        def lines():
+            with open(path) as f:
+                for raw in f:
+                    yield raw
+
+        it = lines()
+
+        def next_data(strip=True):
+            line = next(it)
+            line = line.strip() if strip else line.rstrip("\n")
+            while line.startswith(";") or line.startswith("#"):
+                line = next(it)
+                line = line.strip() if strip else line.rstrip("\n")
+            return line
+
+        if path.endswith(".xf") or path.endswith(".prexg"):
+            for i in range(n):
+                words = next_data().split()
+                tmp = []
+                for j in range(6):
+                    v = float(words[j])
+                    if j > 3:
+                        v *= binning
+                    if tiff2mrc:
+                        v = -v
+                    tmp.append(v)
+                if combineWithExisting:
+                    self.addTransform(i, tmp)
+                else:
+                    self.setTransform(i, tmp)
+            self.convertTolocalTransform()
+        elif path.endswith(".prexf"):
+            for i in range(n):
+                words = next_data().split()
+                tmp = [float(words[0]), float(words[1]), float(words[2]), float(words[3]),
+                       -float(words[4]) * binning,
+                       float(words[5]) * binning if finalTransforms else -float(words[5]) * binning]
+                self.setTransform(n - 1 if i == 0 else i - 1, tmp)
+        else:
+            import re
+            sep = ";" if path.lower().endswith("csv") else None
+            split = (lambda ln: ln.split(";")) if sep else (lambda ln: re.split(r"\s+", ln))
+            for i in range(n):
+                words = split(next_data(strip=False))
+                self.ts.setTiltAngle(i, float(words[0]))
+                self.ts.setTiltAxis(float(words[1]))
+                tmp = [float(words[j + 2]) * (binning if j > 3 else 1.0) for j in range(6)]
+                if combineWithExisting:
+                    self.addTransform(i, tmp)
+                else:
+                    self.setTransform(i, tmp)
+            if finalTransforms:
+                self.convertTolocalTransform()
+            else:
+                words = split(next(it).rstrip("\n"))
+                tmp = [float(words[j]) * (binning if j > 3 else 1.0) for j in range(6)]
+                if combineWithExisting:
+                    self.addToZeroTransform(tmp)
+                else:
+                    self.setZeroTransform(tmp)
+
+    def saveToFile(self, path: str, finalTransforms: bool = False):
+        """AffineAlignment.saveToFile (:509-539): angle, tilt axis and the six matrix
+        values per image (';' for .csv, tab otherwise, each value followed by the
+        separator), written with the tilt axis not put vertical; then the zero-tilt
+        transform unless the transforms are final."""
+        sep = ";" if path.lower().endswith("csv") else "\t"
+        vertical = self.tiltAxisVertical
+        self.tiltAxisVertical = False
+        try:
+            with open(path, "w") as f:
+                for i in range(self.ts.getImageStackSize()):
+                    f.write(f"{_jd(self.ts.getTiltAngle(i))}{sep}{_jd(self.tiltaxis)}{sep}")
+                    t = self.getTransform(i, True) if finalTransforms else self.getTransform(i, False)
+                    for v in t:
+                        f.write(f"{_jd(v)}{sep}")
+                    f.write("\n")
+                if not finalTransforms:
+                    for v in self.zeroT:
+                        f.write(f"{_jd(v)}{sep}")
+                f.write("\n")
+        finally:
+            self.tiltAxisVertical = vertical
+
     def getEulerMatrix(self, index):
         ta = 0.0 if self.tiltAxisVertical else self.tiltaxis
         return euler_angles_to_matrix(ta, self.ts.getTiltAngle(index), -ta)
+
+
+def _jd(v: float) -> str:
+    """Java's Double.toString for the values an alignment file holds (repr, with
+    Java's forms of integral values and of exponents)."""
+    v = float(v)
+    if v != v:
+        return "NaN"
+    if v in (float("inf"), float("-inf")):
+        return "Infinity" if v > 0 else "-Infinity"
+    a = abs(v)
+    if a == 0 or 1e-3 <= a < 1e7:
+        r = repr(v)
+        if "e" in r or "E" in r:  # repr switches to exponents earlier than Java
+            r = f"{v:.17f}".rstrip("0")
+            if r.endswith("."):
+                r += "0"
+        return r if "." in r else r + ".0"
+    # shortest round-trip mantissa
+    m, e = f"{v:.16e}".split("e")
+    for digits in range(1, 17):
+        cand = f"{v:.{digits}e}"
+        if float(cand) == v:
+            m, e = cand.split("e")
+            break
+    if "." not in m:
+        m += ".0"
+    return f"{m}E{int(e)}"
 
 
 class TiltSeries:
@@ -133,6 +287,24 @@ class TiltSeries:
         # zeroindex keeps the first minimum of |angle|, as the reference's strict '<' scan does
         self.alignment = AffineAlignment(self, True)
         self.stats = None
+
+    def setTiltAngle(self, index: int, angleDeg: float):
+        """TiltSeries.setTiltAngle / updateZeroIndex (TiltSeries.java:366-392): the zero
+        index moves only to a strictly smaller |angle| than |angle[0]|."""
+        self.tiltAngles[index] = float(angleDeg)
+        tmp = abs(self.tiltAngles[0])
+        for i in range(self.tiltAngles.size):
+            if abs(self.tiltAngles[i]) < tmp:
+                tmp = abs(self.tiltAngles[i])
+                self.zeroindex = i
+
+    def setTiltAxis(self, angleDeg: float):
+        """TiltSeries.setTiltAxis (:1440-1447): also puts the tilt axis vertical."""
+        self.alignment.setTiltAxis(angleDeg)
+        self.alignment.setTiltAxisVertical(True)
+
+    def getTiltAxis(self) -> float:
+        return self.alignment.tiltaxis
 
     # --- TiltSeries accessors used by the projectors ---------------------------------
     def getWidth(self) -> int:
