@@ -216,6 +216,24 @@ def test_wbp_radermacher_matches_oracle(engine, oracle_lib):
         hd.close()
 
 
+@pytest.mark.parametrize("W", [60, 100, 37])
+def test_wbp_radermacher_any_width_matches_oracle(engine, oracle_lib, W):
+    # widths that are not powers of two go through the circular-convolution row filter
+    c = series_case(W=W, H=6, D=30, n=15, seed=6, misalign=False, noise=0.0)
+    hd = Handle(engine, c, fill=_abi.FILL_AVG)
+    try:
+        radius = 0.45
+        _abi.check(engine.tomo_set_weighting(hd.h, _abi.WEIGHT_RADERMACHER, radius, None))
+        _abi.check(engine.tomo_run_wbp(hd.h, 0, c["H"]))
+        got = hd.volume()
+        ref = np.zeros_like(c["vol"])
+        mask = O.weighting_mask(c["w"], c["h"], c["angles"], None, radius * c["w"])
+        O.wbp(ref, c["g"], c["eul"], c["series"], mask)
+        assert rel_l2(got, ref) <= TOL_PASS, rel_l2(got, ref)
+    finally:
+        hd.close()
+
+
 def test_tvm_iteration_matches_oracle(engine, oracle_lib):
     c = series_case(W=40, H=8, D=24, n=11, seed=8)
     hd = Handle(engine, c)

@@ -115,6 +115,9 @@ tomo_status build_plan(tomo_batch* b) {
     for (size_t m = 0; m < b->members.size(); m++) {
         tomo_projector* p = b->members[m];
         const Geometry& g = p->g;
+        if (!g.separable)
+            return handle_fail(TOMO_ERR_UNSUPPORTED,
+                               "batched iterations need the separable geometry (vertical tilt axis, scale 1)");
         const int N = g.N, upd = b->upd[m];
         const int nsub = (N + upd - 1) / upd;
         b->max_nsub = std::max(b->max_nsub, nsub);

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "tomo_internal.h"
@@ -53,6 +54,19 @@ bool tilt_is_separable(const double* R, const Geometry& g) {
     if (R[1] != 0.0 || R[3] != 0.0 || R[4] != 1.0 || R[5] != 0.0) return false;
     const double o1 = g.pc[1] - g.vc[1], o3 = g.pc[3] - g.vc[1];
     return o1 == std::floor(o1) && o3 == std::floor(o3);
+}
+
+void build_generic_fp_tilt(const double* R, GenericFpTilt* o) {
+    // VoxelProjector3D.projectJosephPartial (VoxelProjector3D.java:682-694), same operation order
+    o->icF = R[3] / R[0];
+    o->zcF = (R[5] - (R[3] * R[2] / R[0]));
+    o->divY = R[4] - (R[3] * R[1] / R[0]);
+    o->yFx = R[1];
+    o->zFx = R[2];
+    o->divX = R[0];
+    o->dirY = -(R[5] - R[3] * R[2] / R[0]) / (R[4] - R[3] * R[1] / R[0]);
+    o->dirX = (R[1] * (-o->dirY) - R[2]) / R[0];
+    o->ninc = std::sqrt(o->dirX * o->dirX + o->dirY * o->dirY + 1);
 }
 
 // Forward-projection ray table of one tilt, following
@@ -231,3 +245,44 @@ void weighting_row_filter(int kind, int w, int nproj, const double* sint, const 
 }
 
 }  // namespace tomo
+
+// The row filter of a non-power-of-two width as a convolution: h[n] = (1/w) sum_k
+// mask[k] e^{2 pi i k n / w} (real for the even masks used here; the real part is
+// kept), zero-padded to M points and transformed by an M-point radix-2 FFT in double.
+void row_filter_spectrum(const float* mask_row, int w, int M, float2* H) {
+    std::vector<double> re((size_t)M, 0.0), im((size_t)M, 0.0);
+    for (int n = 0; n < w; n++) {
+        double acc = 0.0;
+        for (int k = 0; k < w; k++) {
+            const long long kn = ((long long)k * n) % w;
+            acc += (double)mask_row[k] * std::cos(2.0 * M_PI * (double)kn / w);
+        }
+        re[n] = acc / w;
+    }
+    // iterative radix-2 FFT (forward, e^{-2 pi i})
+    int logM = 0;
+    while ((1 << logM) < M) logM++;
+    for (int i = 0; i < M; i++) {
+        int r = 0;
+        for (int b = 0; b < logM; b++) r |= ((i >> b) & 1) << (logM - 1 - b);
+        if (r > i) {
+            std::swap(re[i], re[r]);
+            std::swap(im[i], im[r]);
+        }
+    }
+    for (int len = 2; len <= M; len <<= 1) {
+        const int half = len / 2;
+        for (int i = 0; i < M; i += len)
+            for (int k = 0; k < half; k++) {
+                const double a = -2.0 * M_PI * k / len;
+                const double wr = std::cos(a), wi = std::sin(a);
+                const double xr = re[i + k + half], xi = im[i + k + half];
+                const double tr = xr * wr - xi * wi, ti = xr * wi + xi * wr;
+                re[i + k + half] = re[i + k] - tr;
+                im[i + k + half] = im[i + k] - ti;
+                re[i + k] += tr;
+                im[i + k] += ti;
+            }
+    }
+    for (int m = 0; m < M; m++) H[m] = make_float2((float)re[m], (float)im[m]);
+}

@@ -113,6 +113,40 @@ __global__ void row_filter_kernel(float* img, const float* __restrict__ mask, co
     }
 }
 
+// Any width: the row filter is a circular convolution of length w with the real
+// kernel h = IDFT_w(mask).  Rows are laid out twice ([row, row], the periodic
+// extension) in a zero-padded power-of-two buffer of M >= 2w - 1 points; the linear
+// convolution with h (spectrum H, M points) equals the circular one on outputs
+// [w, 2w).  Two real rows are packed into one complex sequence as above (h is real).
+__global__ void row_filter_conv_kernel(float* img, const float2* __restrict__ H, const float2* __restrict__ tw, int rows,
+                                       int w, int M, int logM) {
+    extern __shared__ float2 sbuf[];
+    float2* a = sbuf;
+    const int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+    float* row0 = img + (size_t)r0 * w;
+    float* row1 = (r1 < rows) ? img + (size_t)r1 * w : nullptr;
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        float2 v = make_float2(0.0f, 0.0f);
+        if (k < 2 * w) {
+            const int m = k < w ? k : k - w;
+            v = make_float2(row0[m], row1 ? row1[m] : 0.0f);
+        }
+        a[bitrev(k, logM)] = v;
+    }
+    fft_stages(a, tw, M, logM, false);
+    float2* b = sbuf + M;
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        const float2 v = a[k], f = H[k];
+        b[bitrev(k, logM)] = make_float2(v.x * f.x - v.y * f.y, v.x * f.y + v.y * f.x);
+    }
+    fft_stages(b, tw, M, logM, true);
+    const float inv = 1.0f / (float)M;
+    for (int k = threadIdx.x; k < w; k += blockDim.x) {
+        row0[k] = b[w + k].x * inv;
+        if (row1) row1[k] = b[w + k].y * inv;
+    }
+}
+
 // Sum over rows of the per-row residuals, one thread per tilt, fixed order.
 // Sum of one projection's per-row residual sums by one warp: lane l adds rows
 // l, l + 32, ... in order, then a fixed butterfly combines the lanes (deterministic).
@@ -450,8 +484,11 @@ __global__ void scan_nonfinite_kernel(const float* __restrict__ p, size_t n, int
 }  // namespace
 
 cudaError_t misc_init_attributes() {
-    return cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                2 * 4096 * (int)sizeof(float2));
+    cudaError_t e = cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         2 * 4096 * (int)sizeof(float2));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(row_filter_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                2 * kRowConvMaxM * (int)sizeof(float2));
 }
 
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s) {
@@ -485,6 +522,17 @@ cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2
     if ((1 << logn) != w) return cudaErrorInvalidValue;
     const size_t smem = 2 * (size_t)w * sizeof(float2);
     row_filter_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, mask_row, tw, rows, w, logn);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_filter_conv(float* img, const float2* H, const float2* tw, int rows, int w, int M,
+                                   cudaStream_t s) {
+    int logM = 0;
+    while ((1 << logM) < M) logM++;
+    if ((1 << logM) != M || M < 2 * w - 1 || M > kRowConvMaxM) return cudaErrorInvalidValue;
+    const size_t smem = 2 * (size_t)M * sizeof(float2);
+    row_filter_conv_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, H, tw, rows, w, M, logM);
     count_launch();
     return cudaGetLastError();
 }

@@ -187,6 +187,39 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
         if (with_diff) CK(cudaMemsetAsync(errpart, 0, sizeof(double) * (size_t)T * g.h, p->stream));
     }
     if (j0 >= j1) return TOMO_OK;
+    if (!g.separable) {
+        // any geometry: reference arithmetic per ray, then the difference pass
+        FpGenericLaunch ga{};
+        ga.vol = p->d_vol;
+        ga.tilts = d_tilts;
+        ga.T = T;
+        ga.gtilt = p->d_gtilt;
+        ga.proj = proj;
+        ga.norm = norm;
+        ga.j0 = j0;
+        ga.j1 = j1;
+        ga.W = g.W;
+        ga.H = g.H;
+        ga.D = g.D;
+        ga.w = g.w;
+        ga.h = g.h;
+        ga.pc0x = g.pc[0];
+        ga.pc0y = g.pc[1];
+        ga.scale = g.scale;
+        ga.vcx = g.vc[0];
+        ga.vcy = g.vc[1];
+        ga.vcz = g.vc[2];
+        ga.bXmax = (double)((float)g.W + 1e-10f);  // int + float ACCURACY rounds to W (VoxelProjector3D.java:33)
+        ga.bYmax = (double)((float)g.H + 1e-10f);
+        ga.acc = (double)1e-10f;
+        CK(launch_fp_generic(ga, p->stream));
+        if (p->params.long_object) CK(launch_long_object(norm, T, g.h, g.w, p->stream));
+        if (with_diff) {
+            CK(launch_diff(p->d_meas, d_tilts, proj, norm, diff, errpart, T, g.w, g.h, j0, j1, factor, p->stream));
+            CK(launch_reduce_err(errpart, p->d_err + slot0, T, g.h, p->stream));
+        }
+        return TOMO_OK;
+    }
     FpLaunch a{};
     a.vol = p->vol();
     a.vtype = p->vtype;
@@ -226,7 +259,10 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
 
 tomo_status apply_weighting(tomo_projector* p, float* imgs, int T) {
     if (p->weight_kind == TOMO_WEIGHT_NONE || T <= 0) return TOMO_OK;
-    CK(launch_row_filter_tw(imgs, p->d_mask, p->d_tw, T * p->g.h, p->g.w, p->stream));
+    if (p->conv_M > 0)
+        CK(launch_row_filter_conv(imgs, p->d_convH, p->d_convTw, T * p->g.h, p->g.w, p->conv_M, p->stream));
+    else
+        CK(launch_row_filter_tw(imgs, p->d_mask, p->d_tw, T * p->g.h, p->g.w, p->stream));
     return TOMO_OK;
 }
 
@@ -253,6 +289,30 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     y1 = std::min(g.H, y1);
     if (y1 <= y0 || T <= 0) return TOMO_OK;
     const bool to_dist = diffs && p->bayes;
+    if (!g.separable) {
+        BpGenericLaunch ga{};
+        ga.vol = to_dist ? p->d_dist : p->d_vol;
+        ga.img = imgs;
+        ga.tilts = d_tilts;
+        ga.T = T;
+        ga.euler = p->d_euler;
+        ga.y0 = y0;
+        ga.y1 = y1;
+        ga.W = g.W;
+        ga.H = g.H;
+        ga.D = g.D;
+        ga.w = g.w;
+        ga.h = g.h;
+        ga.vc0 = g.vc[0];
+        ga.vc1 = g.vc[1];
+        ga.vc2 = g.vc[2];
+        ga.cix = g.pc[2];
+        ga.ciy = g.pc[3];
+        ga.scale = g.scale;
+        ga.positivity = p->params.positivity;
+        CK(launch_bp_generic(ga, p->stream));
+        return TOMO_OK;
+    }
     BpLaunch a{};
     a.vol = to_dist ? p->bp_target() : p->vol();
     a.vtype = to_dist ? kVolF32 : p->vtype;
@@ -286,10 +346,6 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
 
 tomo_status need_series(tomo_projector* p) {
     if (!p->series_loaded) return fail(TOMO_ERR_STATE, "no tilt-series loaded (tomo_load_series)");
-    if (!p->g.separable)
-        return fail(TOMO_ERR_UNSUPPORTED,
-                    "geometry is not supported on the device: it needs a vertical tilt axis, scale 1 and "
-                    "integral row offsets between projection and volume centres");
     return TOMO_OK;
 }
 
@@ -518,6 +574,17 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
         CK(cudaMemcpyAsync(p->d_btilt, bt.data(), sizeof(BpTilt) * N, cudaMemcpyHostToDevice, p->stream));
         CK(cudaMemcpyAsync(p->d_zint, zint.data(), sizeof(int32_t) * zint.size(), cudaMemcpyHostToDevice,
                            p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+    } else {
+        if (p->vtype != kVolF32)
+            return fail(TOMO_ERR_UNSUPPORTED,
+                        "16-bit volume storage needs the separable geometry (vertical tilt axis, scale 1)");
+        if (!p->d_gtilt) CKS(alloc_n(p, &p->d_gtilt, (size_t)N));
+        if (!p->d_euler) CKS(alloc_n(p, &p->d_euler, (size_t)N * 9));
+        std::vector<GenericFpTilt> gt(N);
+        for (int t = 0; t < N; t++) build_generic_fp_tilt(&p->euler[9 * t], &gt[t]);
+        CK(cudaMemcpyAsync(p->d_gtilt, gt.data(), sizeof(GenericFpTilt) * N, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_euler, p->euler.data(), sizeof(double) * 9 * N, cudaMemcpyHostToDevice, p->stream));
         CK(cudaStreamSynchronize(p->stream));
     }
     // alignment: Tinv = AffineTransform.createInverse (general case)
@@ -806,7 +873,6 @@ tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, c
         for (int t = 0; t < g.N; t++)
             if (tilt_axes[t] != 0.0)
                 return fail(TOMO_ERR_UNSUPPORTED, "weighting with a non-zero tilt-axis angle needs a 2-D filter");
-    if ((g.w & (g.w - 1)) != 0) return fail(TOMO_ERR_UNSUPPORTED, "weighting needs a power-of-two width");
     if (kind == TOMO_WEIGHT_RADERMACHER && !(radius > 0))
         return fail(TOMO_ERR_INVALID, "Radermacher weighting needs a positive radius");
     std::vector<double> sint(g.N), deg(g.N);
@@ -816,6 +882,28 @@ tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, c
     }
     std::vector<float> mask(g.w);
     weighting_row_filter(kind, g.w, g.N, sint.data(), deg.data(), radius * g.w, mask.data());
+    if ((g.w & (g.w - 1)) != 0) {
+        // any width: circular convolution with h = IDFT_w(mask) through an M-point FFT
+        int M = 1;
+        while (M < 2 * g.w - 1) M <<= 1;
+        if (M > kRowConvMaxM) return fail(TOMO_ERR_UNSUPPORTED, "weighting supports widths up to 4096");
+        std::vector<float2> H(M), twm(M);
+        row_filter_spectrum(mask.data(), g.w, M, H.data());
+        for (int k = 0; k < M; k++) {
+            const double a = -2.0 * M_PI * k / M;
+            twm[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        if (p->conv_M < M) {
+            CKS(alloc_n(p, &p->d_convH, (size_t)M));
+            CKS(alloc_n(p, &p->d_convTw, (size_t)M));
+        }
+        CK(cudaMemcpyAsync(p->d_convH, H.data(), sizeof(float2) * M, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_convTw, twm.data(), sizeof(float2) * M, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        p->conv_M = M;
+        p->weight_kind = kind;
+        return TOMO_OK;
+    }
     std::vector<float2> tw(g.w);
     for (int k = 0; k < g.w; k++) {
         const double a = -2.0 * M_PI * k / g.w;

@@ -42,12 +42,17 @@ struct tomo_projector {
     tomo::FpTilt* d_ftilt = nullptr;
     tomo::FpRay* d_rays = nullptr;
     tomo::BpTilt* d_btilt = nullptr;
+    tomo::GenericFpTilt* d_gtilt = nullptr;  // generic geometry: per-tilt FP constants
+    double* d_euler = nullptr;               // generic geometry: [N][9] Euler matrices
     int32_t* d_zint = nullptr;
     double* d_tinv = nullptr;
     double* d_stats = nullptr;
     unsigned char* d_identity = nullptr;
     float* d_mask = nullptr;
     float2* d_tw = nullptr;
+    float2* d_convH = nullptr;   // non-power-of-two widths: spectrum of the circular kernel
+    float2* d_convTw = nullptr;  // and twiddles, conv_M points
+    int conv_M = 0;
     float *d_tv_u = nullptr, *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;
     float* d_prev = nullptr;
 

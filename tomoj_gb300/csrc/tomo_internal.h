@@ -56,6 +56,12 @@ struct alignas(8) BpTilt {
     long long K, C, S;
 };
 
+// Generic-geometry forward projection constants of one tilt, the reference's
+// expressions of R (VoxelProjector3D.java:682-694).
+struct GenericFpTilt {
+    double icF, zcF, divY, yFx, zFx, divX, dirX, dirY, ninc;
+};
+
 // Per-handle geometry constants (host-computed).
 struct Geometry {
     int W, H, D, w, h, N;
@@ -69,6 +75,10 @@ struct Geometry {
 bool tilt_is_separable(const double* R, const Geometry& g);
 void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays /* w entries */);
 void build_bp_tables(const Geometry& g, const double* R, BpTilt* tilt, int32_t* zint /* W entries */);
+void build_generic_fp_tilt(const double* R, GenericFpTilt* out);
+// M-point spectrum (M a power of two >= 2w - 1) of the real circular kernel
+// h = IDFT_w(mask_row), zero-padded: the row filter as a convolution.
+void row_filter_spectrum(const float* mask_row, int w, int M, float2* H);
 void order_shuffle(int n, const double* euler, int first, int* out);
 int first_index(uint64_t seed, int iteration, int nproj);
 void weighting_row_filter(int kind, int w, int nproj, const double* sint, const double* tilts_deg, double diameter,
@@ -112,6 +122,33 @@ struct FpLaunch {
     unsigned* tickets;
 };
 cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s);
+// Any geometry (kernels_generic.cu): one thread per ray / voxel in the reference's
+// double arithmetic.  proj/norm are [T][h][w] in batch order.
+struct FpGenericLaunch {
+    const float* vol;
+    const int* tilts;
+    int T;
+    const GenericFpTilt* gtilt;  // [N]
+    float* proj;
+    float* norm;
+    int j0, j1;                  // projection rows; row j0 starts the first 2-row task
+    int W, H, D, w, h;
+    double pc0x, pc0y, scale, vcx, vcy, vcz, bXmax, bYmax, acc;
+};
+cudaError_t launch_fp_generic(const FpGenericLaunch& a, cudaStream_t s);
+struct BpGenericLaunch {
+    float* vol;
+    const float* img;            // [T][h][w] batch order
+    const int* tilts;
+    int T;
+    const double* euler;         // [N][9]
+    int y0, y1;
+    int W, H, D, w, h;
+    double vc0, vc1, vc2, cix, ciy, scale;
+    int positivity;
+};
+cudaError_t launch_bp_generic(const BpGenericLaunch& a, cudaStream_t s);
+
 // Depth parts for `ctas` (tilt group, row) CTAs: balances the grid over the resident
 // CTA slots of the device (1 = no split).
 int fp_zparts(int ctas, int D, int zc, int sms);
@@ -147,6 +184,11 @@ int bp_tile_z();
 cudaError_t launch_align(const float* raw, float* out, const double* tinv /*[N][6]*/, const double* stats, int N,
                          int w, int h, int normalize, int fill, const unsigned char* identity, cudaStream_t s);
 cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2* tw, int rows, int w, cudaStream_t s);
+// Row filter of any width as a circular convolution (spectrum H and twiddles of M points,
+// M a power of two >= 2w - 1, at most kRowConvMaxM).
+constexpr int kRowConvMaxM = 8192;
+cudaError_t launch_row_filter_conv(float* img, const float2* H, const float2* tw, int rows, int w, int M,
+                                   cudaStream_t s);
 cudaError_t launch_diff(const float* meas, const int* tilts, const float* th, const float* norm, float* diff,
                         double* errpart, int T, int w, int h, int j0, int j1, double factor, cudaStream_t s);
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s);
