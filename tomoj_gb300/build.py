@@ -70,7 +70,8 @@ def build(force: bool = False, verbose: bool = False, out: str | None = None, de
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = lib + ".tmp"
-    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["--cudart", "static"]
+    # --no-undefined: a declared but undefined symbol fails here, not at load time
+    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["--cudart", "static", "-Xlinker", "--no-undefined"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

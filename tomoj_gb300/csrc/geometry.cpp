@@ -246,6 +246,8 @@ void weighting_row_filter(int kind, int w, int nproj, const double* sint, const 
 
 }  // namespace tomo
 
+namespace tomo {
+
 // The row filter of a non-power-of-two width as a convolution: h[n] = (1/w) sum_k
 // mask[k] e^{2 pi i k n / w} (real for the even masks used here; the real part is
 // kept), zero-padded to M points and transformed by an M-point radix-2 FFT in double.
@@ -286,3 +288,5 @@ void row_filter_spectrum(const float* mask_row, int w, int M, float2* H) {
     }
     for (int m = 0; m < M; m++) H[m] = make_float2((float)re[m], (float)im[m]);
 }
+
+}  // namespace tomo
