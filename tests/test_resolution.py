@@ -1,0 +1,83 @@
+"""Resolution estimation (ResolutionEstimation.fsc / frc / frcSlices) on the host, and
+the even / odd half-data reconstructions on the engine."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tomoj_gb300 import resolution as R
+
+
+def _fsc_loops(even, odd):
+    # the reference's loops written out directly (ResolutionEstimation.java:456-557)
+    D, H, W = even.shape
+    mask = np.zeros_like(even)
+    for z in range(D):
+        for y in range(H):
+            for x in range(W):
+                d = np.sqrt((x - W / 2.0) ** 2 + ((z - D / 2.0) ** 2 + (y - H / 2.0) ** 2))
+                mask[z, y, x] = 1 if d < D else (np.float32((1 + np.cos((d - D) * np.pi / 20)) * .5) if d < D + 20 else 0)
+    fe = np.fft.fftn((even * mask).astype(np.float64))
+    fo = np.fft.fftn((odd * mask).astype(np.float64))
+    nb = W // 2 + 1
+    num, de, do, err, cnt = (np.zeros(nb) for _ in range(5))
+    for z in range(D):
+        for y in range(H):
+            for x in range(W):
+                w = np.sqrt(R.convert_to_frequency(x, W) ** 2 + R.convert_to_frequency(y, H) ** 2
+                            + R.convert_to_frequency(z, D) ** 2)
+                i = int(np.floor(w * W + 0.5))
+                if i >= nb:
+                    continue
+                e, o = fe[z, y, x], fo[z, y, x]
+                num[i] += (e * np.conj(o)).real
+                de[i] += abs(e) ** 2
+                do[i] += abs(o) ** 2
+                err[i] += abs(e - o)
+                cnt[i] += 1
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.array([np.arange(nb) / W, num / np.sqrt(de * do), 2 / np.sqrt(cnt), err / cnt])
+
+
+def test_fsc_matches_the_reference_loops():
+    rng = np.random.default_rng(0)
+    a = rng.normal(0, 1, (6, 7, 8)).astype(np.float32)
+    b = (a + 0.5 * rng.normal(0, 1, a.shape)).astype(np.float32)
+    got = R.fsc(a, b)
+    ref = _fsc_loops(a, b)
+    assert np.allclose(got, ref, rtol=1e-9, atol=1e-12, equal_nan=True)
+
+
+def test_fsc_of_identical_and_independent_volumes():
+    rng = np.random.default_rng(1)
+    a = rng.normal(0, 1, (16, 16, 16)).astype(np.float32)
+    same = R.fsc(a, a)
+    assert np.allclose(same[1][np.isfinite(same[1])], 1.0)
+    b = rng.normal(0, 1, a.shape).astype(np.float32)
+    ind = R.fsc(a, b)
+    # independent data: |FSC| mostly inside the 2/sqrt(n) curve (skip the DC shell)
+    inside = np.abs(ind[1][1:]) <= 2.5 * ind[2][1:]
+    assert inside.mean() > 0.8
+
+
+def test_frc_and_frc_slices_accumulate_like_the_reference():
+    rng = np.random.default_rng(2)
+    a = rng.normal(0, 1, (3, 20, 24)).astype(np.float32)
+    b = (a + rng.normal(0, 1, a.shape)).astype(np.float32)
+    s = R.frc_slices(a, b)
+    assert s.shape == (3, 4, 24 // 2 + 1)
+    # slice sums are cumulative: the count row of slice z is (z + 1) times slice 0's
+    c0 = 4.0 / s[0, 2] ** 2
+    c2 = 4.0 / s[2, 2] ** 2
+    ok = np.isfinite(c0) & np.isfinite(c2)
+    assert np.allclose(c2[ok], 3 * c0[ok])
+    f = R.frc(a[0], a[0])
+    assert np.allclose(f[1][np.isfinite(f[1])], 1.0)
+
+
+@pytest.mark.parametrize("n,even,odd", [(7, [0, 2, 4], [1, 3, 5]), (6, [0, 2, 4], [1, 3, 5]),
+                                        (5, [0, 2], [1, 3])])
+def test_even_odd_available_indexes(n, even, odd):
+    assert list(R.available_indexes(n, R.EVEN_PROJECTIONS)) == even
+    assert list(R.available_indexes(n, R.ODD_PROJECTIONS)) == odd
+    assert list(R.available_indexes(n, R.ALL_PROJECTIONS)) == list(range(n))

@@ -1,0 +1,212 @@
+"""Resolution estimation: Fourier shell / ring correlation of two half-data
+reconstructions.
+
+Mirrors ResolutionEstimation (TomoJ_Base/src/main/java/fr/curie/tomoj/tomography/
+ResolutionEstimation.java): the tilt-series is split into even and odd projections
+as ReconstructionParameters.getAvailableIndexes does for EVEN_PROJECTIONS /
+ODD_PROJECTIONS (ReconstructionParameters.java:212-256), each half is reconstructed
+with the same parameters (here on the GPU engine), and the two volumes are compared
+shell by shell:
+
+  * fsc (:456-557): both volumes times a soft spherical mask (1 inside a radius of
+    the stack depth, a 20-voxel raised-cosine edge), 3-D FFT, shells indexed by
+    round(|f| * W) with f the signed frequency of each axis (convertToFrequency,
+    :699-701); per shell: sum Re(E conj(O)), sum |E|^2, sum |O|^2, sum |E - O|,
+    count; output rows {i / W, FSC, 2 / sqrt(count), mean |E - O|};
+  * frc (:376-454): the same on one pair of images with a circular mask;
+  * frcSlices (:275-374): per-slice 2-D FFTs with a cylinder mask; the shell sums
+    are not reset between slices, so slice z reports the sums over slices 0..z
+    (reproduced as the reference computes it).
+
+The reference transforms float data with ParallelColt (absent from the reference
+tree); here the transforms are numpy's double-precision FFTs.  The result agrees
+to FP32 rounding, and that correspondence is not pinned by any reference test.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .reconstruction import BP, WBP, ReconstructionParameters, TomoReconstruction2
+from .tiltseries import TiltSeries
+
+ALL_PROJECTIONS, EVEN_PROJECTIONS, ODD_PROJECTIONS = 0, 11, 12
+
+
+def available_indexes(nproj: int, projection_type: int) -> np.ndarray:
+    """ReconstructionParameters.getAvailableIndexes: even / odd indexes, at most nproj // 2 of them."""
+    sel = []
+    count = 0
+    for i in range(nproj):
+        if projection_type == EVEN_PROJECTIONS:
+            take = i % 2 == 0
+        elif projection_type == ODD_PROJECTIONS:
+            take = i % 2 == 1
+        else:
+            take = True
+        if take:
+            count += 1
+            if projection_type in (EVEN_PROJECTIONS, ODD_PROJECTIONS) and count > nproj // 2:
+                take = False
+                count -= 1
+        if take:
+            sel.append(i)
+    return np.array(sel, np.int64)
+
+
+def convert_to_frequency(x, size: int):
+    """convertToFrequency (:699-701): signed frequency of index x in cycles per sample."""
+    x = np.asarray(x, np.float64)
+    return np.where(x <= (size >> 1), x, x - size) / size
+
+
+def _shell_sums(fe, fo, widx, nbins):
+    keep = widx < nbins
+    idx = widx[keep]
+    e = fe[keep]
+    o = fo[keep]
+    num = np.bincount(idx, weights=(e * np.conj(o)).real, minlength=nbins)
+    den_e = np.bincount(idx, weights=np.abs(e) ** 2, minlength=nbins)
+    den_o = np.bincount(idx, weights=np.abs(o) ** 2, minlength=nbins)
+    err = np.bincount(idx, weights=np.abs(e - o), minlength=nbins)
+    cnt = np.bincount(idx, minlength=nbins).astype(np.float64)
+    return num, den_e, den_o, err, cnt
+
+
+def _rows(num, den_e, den_o, err, cnt, width):
+    nb = num.size
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.array([np.arange(nb) / width, num / np.sqrt(den_e * den_o), 2 / np.sqrt(cnt), err / cnt])
+
+
+def _java_round(v):
+    return np.floor(v + 0.5).astype(np.int64)
+
+
+def fsc(even: np.ndarray, odd: np.ndarray) -> np.ndarray:
+    """Fourier shell correlation of two (D, H, W) volumes: rows {frequency, FSC,
+    2/sqrt(count), mean |E - O|} over W // 2 + 1 shells."""
+    even = np.asarray(even, np.float32)
+    odd = np.asarray(odd, np.float32)
+    D, H, W = even.shape
+    z = (np.arange(D) - D / 2.0) ** 2
+    y = (np.arange(H) - H / 2.0) ** 2
+    x = (np.arange(W) - W / 2.0) ** 2
+    dist = np.sqrt(x[None, None, :] + (z[:, None, None] + y[None, :, None]))
+    mask = np.where(dist < D, 1.0, np.where(dist < D + 20, (1 + np.cos((dist - D) * np.pi / 20)) * 0.5, 0.0))
+    mask = mask.astype(np.float32)
+    fe = np.fft.fftn((even * mask).astype(np.float64))
+    fo = np.fft.fftn((odd * mask).astype(np.float64))
+    fz = convert_to_frequency(np.arange(D), D) ** 2
+    fy = convert_to_frequency(np.arange(H), H) ** 2
+    fx = convert_to_frequency(np.arange(W), W) ** 2
+    w = np.sqrt(fx[None, None, :] + fy[None, :, None] + fz[:, None, None])
+    widx = _java_round(w * W)
+    nb = W // 2 + 1
+    return _rows(*_shell_sums(fe.ravel(), fo.ravel(), widx.ravel(), nb), W)
+
+
+def frc(img1: np.ndarray, img2: np.ndarray) -> np.ndarray:
+    """Fourier ring correlation of two (H, W) images (ResolutionEstimation.frc)."""
+    a = np.asarray(img1, np.float32)
+    b = np.asarray(img2, np.float32)
+    H, W = a.shape
+    y = (np.arange(H) - H / 2.0) ** 2
+    x = (np.arange(W) - W / 2.0) ** 2
+    dist = np.sqrt(x[None, :] + y[:, None])
+    mask = np.where(dist < W, 1.0, np.where(dist < W + 20, (1 + np.cos((dist - W) * np.pi / 20)) * 0.5, 0.0))
+    mask = mask.astype(np.float32)
+    fe = np.fft.fft2((a * mask).astype(np.float64))
+    fo = np.fft.fft2((b * mask).astype(np.float64))
+    fy = convert_to_frequency(np.arange(H), H) ** 2
+    fx = convert_to_frequency(np.arange(W), W) ** 2
+    widx = _java_round(np.sqrt(fx[None, :] + fy[:, None]) * W)
+    return _rows(*_shell_sums(fe.ravel(), fo.ravel(), widx.ravel(), W // 2 + 1), W)
+
+
+def frc_slices(even: np.ndarray, odd: np.ndarray) -> np.ndarray:
+    """ResolutionEstimation.frcSlices: (D, 4, W // 2 + 1); slice z holds the ring sums of
+    slices 0..z (the reference never resets them)."""
+    even = np.asarray(even, np.float32)
+    odd = np.asarray(odd, np.float32)
+    D, H, W = even.shape
+    y = (np.arange(H) - H / 2.0) ** 2
+    x = (np.arange(W) - W / 2.0) ** 2
+    dist = np.sqrt(x[None, :] + y[:, None])
+    mask = np.where(dist < W - 20, 1.0,
+                    np.where(dist < W, (1 + np.cos((dist - W - 20) * np.pi / 20)) * 0.5, 0.0)).astype(np.float32)
+    fy = convert_to_frequency(np.arange(H), H) ** 2
+    fx = convert_to_frequency(np.arange(W), W) ** 2
+    widx = _java_round(np.sqrt(fx[None, :] + fy[:, None]) * W).ravel()
+    nb = W // 2 + 1
+    acc = [np.zeros(nb) for _ in range(5)]
+    out = np.zeros((D, 4, nb))
+    for zi in range(D):
+        fe = np.fft.fft2((even[zi] * mask).astype(np.float64)).ravel()
+        fo = np.fft.fft2((odd[zi] * mask).astype(np.float64)).ravel()
+        for a, s in zip(acc, _shell_sums(fe, fo, widx, nb)):
+            a += s
+        out[zi] = _rows(*acc, W)
+    return out
+
+
+class _FixedAlignment:
+    """Alignment of a sub-series: each image keeps the final transform and Euler matrix it
+    has in the full series (the reference reconstructs a half from the full series through
+    getAvailableIndexes, so consecutive transforms of skipped images still compose)."""
+
+    def __init__(self, transforms, eulers):
+        self._t = [tuple(map(float, t)) for t in transforms]
+        self._e = [np.asarray(e, np.float64) for e in eulers]
+
+    def getTransform(self, index, combine=None):
+        return self._t[index]
+
+    def getEulerMatrix(self, index):
+        return self._e[index]
+
+
+def subseries(ts: TiltSeries, indexes) -> TiltSeries:
+    """The tilt-series restricted to `indexes`, with their full-series geometry."""
+    idx = np.asarray(indexes, np.int64)
+    sub = TiltSeries(ts.pixels[idx], ts.tiltAngles[idx])
+    sub.setNormalize(ts.isNormalized())
+    sub.setFillType(ts.getFillType())
+    T, E = ts.transforms(), ts.eulers()
+    sub.alignment = _FixedAlignment(T[idx], E[idx])
+    if ts.stats is not None:
+        sub.setStatistics(np.asarray(ts.statistics())[idx])
+    return sub
+
+
+class ResolutionEstimation:
+    """ResolutionEstimation on the engine: generateFSCData reconstructs the even and odd
+    halves with `params` (WBP, OS-SART / SIRT or TVM), fsc() compares them."""
+
+    def __init__(self, ts: TiltSeries, params: ReconstructionParameters, seed: int = 0):
+        self.ts = ts
+        self.params = params
+        self.seed = seed
+        self.recFSCeven = None
+        self.recFSCodd = None
+
+    def _reconstruct(self, ts: TiltSeries) -> np.ndarray:
+        p = self.params
+        rec = TomoReconstruction2(p.width, p.height, p.depth)
+        proj = p.getProjector(ts, rec)
+        try:
+            if p.reconstructionType in (BP, WBP):
+                rec.WBP(ts, proj, p)
+            else:
+                rec.OSSART(ts, proj, p, seed=self.seed)
+            return rec.getVolume()
+        finally:
+            proj.close()
+
+    def generateFSCData(self):
+        n = self.ts.getImageStackSize()
+        self.recFSCodd = self._reconstruct(subseries(self.ts, available_indexes(n, ODD_PROJECTIONS)))
+        self.recFSCeven = self._reconstruct(subseries(self.ts, available_indexes(n, EVEN_PROJECTIONS)))
+
+    def fsc(self) -> np.ndarray:
+        self.generateFSCData()
+        return fsc(self.recFSCeven, self.recFSCodd)
