@@ -316,15 +316,25 @@ def run_engine(args, wl):
     h2d = series_pin.nbytes + eul.nbytes + T.nbytes + stats.nbytes
     d2h = vol_pin.nbytes
     e2e_steps = max(1, min(args.steps, 3))
+    phase = {"load_s": 0.0, "job_s": 0.0, "readback_s": 0.0}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        load(series_pin)
+        ta = time.perf_counter()
+        load(series_pin)  # synchronous: series H2D, geometry tables, alignment
+        tb = time.perf_counter()
         step()
+        torch.cuda.synchronize()
+        tc = time.perf_counter()
         _abi.check(lib.tomo_get_volume(h, vol_pin.ctypes.data, 0, 0, H))
+        td = time.perf_counter()
+        phase["load_s"] += tb - ta
+        phase["job_s"] += tc - tb
+        phase["readback_s"] += td - tc
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = updates_per_step * e2e_steps * world / e2e_s
+    phase = {k: v / e2e_steps for k, v in phase.items()}
 
     # ---- roofline of the dominant kernel ----
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -399,7 +409,7 @@ def run_engine(args, wl):
                        "updates_per_step": updates_per_step, "l2": "inputs larger than L2 (volume 268 MB)",
                        "parallelism": f"replicas{world}"},
             "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps, "phases_s": phase},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
             "batched": batched, "serving": serving, "precision": precision,
             "sirt_error_last_iteration": float(errs[-1, 0]),
