@@ -39,11 +39,24 @@ void find_interval(int n, double za, double zb, F in, int* lo_out, int* cnt_out)
     for (int c : cands)
         if (in(c)) { seed = c; break; }
     if (seed < 0) return;
-    int lo = seed, hi = seed;
-    while (lo > 0 && in(lo - 1)) lo--;
-    while (hi + 1 < n && in(hi + 1)) hi++;
+    // Bisect both ends: every probe evaluates the exact predicate, and the last probes
+    // of each search are the two planes on either side of that end.
+    int a = 0, b = seed;  // in(b); everything below a is outside
+    while (a < b) {
+        const int m = a + (b - a) / 2;
+        if (in(m)) b = m;
+        else a = m + 1;
+    }
+    const int lo = a;
+    a = seed;
+    b = n - 1;  // in(a); everything above b is outside
+    while (a < b) {
+        const int m = a + (b - a + 1) / 2;
+        if (in(m)) a = m;
+        else b = m - 1;
+    }
     *lo_out = lo;
-    *cnt_out = hi - lo + 1;
+    *cnt_out = a - lo + 1;
 }
 
 }  // namespace
