@@ -1,6 +1,8 @@
 """Any geometry on the GPU against the oracle: a tilt axis that is not vertical
-(full Euler matrices), scale != 1 (projections finer than the volume grid) and a
-half-pixel offset between projection and volume centres.  The generic kernels
+(full Euler matrices, generic kernels), and on the XZ-plane kernels with blended
+rows: scale != 1 (projections finer or coarser than the volume grid, with
+backprojection tiles spanning up to 192 image columns) and a half-pixel offset
+between projection and volume centres.  The generic kernels
 follow the reference's double arithmetic step by step, so norms and NaN patterns
 must match exactly and values to float rounding (tolerance 1e-5 per pass, 1e-4
 after iterations)."""
@@ -19,8 +21,12 @@ from tomoj_gb300 import phantom as P
 pytestmark = pytest.mark.gpu
 
 CASES = {
+    # generic kernels (full Euler matrices)
     "tilt_axis_7deg": dict(W=40, H=10, D=30, w=40, h=10, axis=7.0, scale=1.0),
+    # vertical axis with blended rows on the XZ-plane kernels
     "scale_2": dict(W=24, H=6, D=20, w=48, h=12, axis=0.0, scale=2.0),
+    "scale_2_tiles": dict(W=80, H=5, D=72, w=160, h=10, axis=0.0, scale=2.0),
+    "scale_half": dict(W=48, H=8, D=32, w=24, h=4, axis=0.0, scale=0.5),
     "half_pixel_rows": dict(W=36, H=8, D=24, w=36, h=9, axis=0.0, scale=1.0),
 }
 

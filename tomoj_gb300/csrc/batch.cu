@@ -115,9 +115,9 @@ tomo_status build_plan(tomo_batch* b) {
     for (size_t m = 0; m < b->members.size(); m++) {
         tomo_projector* p = b->members[m];
         const Geometry& g = p->g;
-        if (!g.separable)
+        if (!g.separable || g.fractional || p->bp_wide || p->bp_generic)
             return handle_fail(TOMO_ERR_UNSUPPORTED,
-                               "batched iterations need the separable geometry (vertical tilt axis, scale 1)");
+                               "batched iterations need a vertical tilt axis, scale 1 and whole-row centre offsets");
         const int N = g.N, upd = b->upd[m];
         const int nsub = (N + upd - 1) / upd;
         b->max_nsub = std::max(b->max_nsub, nsub);

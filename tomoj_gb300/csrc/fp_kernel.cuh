@@ -38,13 +38,13 @@ struct Smem {
     size_t raw_off, pair_off, red_off, step_off, total;
 };
 
-// Shared memory: mbarrier | raw chunk [ZC][W] | pairs [ZC][W+4] | reduction scratch | steps.
-__host__ __device__ inline Smem layout(int ZC, int W, int tgmax) {
+// Shared memory: mbarrier | raw chunk [rows][ZC][W] | pairs [ZC][W+4] | reduction scratch | steps.
+__host__ __device__ inline Smem layout(int ZC, int W, int tgmax, int rows = 1) {
     Smem L;
     L.PW = W + 4;
     size_t o = 16;
     L.raw_off = o;
-    o += (size_t)ZC * W * sizeof(float);
+    o += (size_t)rows * ZC * W * sizeof(float);
     o = (o + 15) & ~(size_t)15;
     L.pair_off = o;
     o += (size_t)ZC * L.PW * sizeof(float2);
@@ -122,6 +122,41 @@ __device__ __forceinline__ void build_pairs_row16(const uint16_t* __restrict__ s
     }
 }
 
+// Pairs of a plane row blended between volume rows r (src0) and r + 1 (src1) with
+// weight yf: b = v0 + yf (v1 - v0), then pairs of b as above.  The reference returns
+// the raw voxel of row r (unblended) at the last column, so that slot keeps v0; on
+// the last plane (`flat`) every sample is the raw voxel of row r.
+__device__ __forceinline__ void build_pairs_row_blend(const float* __restrict__ src0, const float* __restrict__ src1,
+                                                      float yf, float2* __restrict__ dst, int W, bool flat) {
+    const int tid = threadIdx.x;
+    if (flat) {
+        for (int k = tid; k < W; k += kThreads) dst[k + 2] = make_float2(src0[k], 0.0f);
+    } else {
+        for (int k = tid; k < W; k += kThreads) {
+            const float v0 = src0[k];
+            const float b = __fadd_rn(v0, __fmul_rn(yf, __fsub_rn(src1[k], v0)));
+            float2 pr;
+            if (k + 1 < W) {
+                const float v0n = src0[k + 1];
+                const float bn = __fadd_rn(v0n, __fmul_rn(yf, __fsub_rn(src1[k + 1], v0n)));
+                const float d = __fsub_rn(bn, b);
+                pr = make_float2(__fsub_rn(b, d), d);
+            } else {
+                pr = make_float2(v0, 0.0f);  // last column: the raw voxel of row r
+            }
+            dst[k + 2] = pr;
+        }
+    }
+    if (tid < 4) {
+        // x in [-ACCURACY, 0) samples column 0 with weight 0 (the blended value);
+        // slots past the row are never sampled (x < W)
+        const float v0 = src0[0];
+        const float b0 = flat ? v0 : __fadd_rn(v0, __fmul_rn(yf, __fsub_rn(src1[0], v0)));
+        const int k = (tid < 2) ? tid - 2 : W + tid - 2;  // -2, -1, W, W+1
+        dst[k + 2] = make_float2(tid < 2 ? b0 : src0[W - 1], 0.0f);
+    }
+}
+
 __device__ __forceinline__ float sample(const float2* __restrict__ P, long long x) {
     const float2 p = P[(int)(x >> 32)];
     return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
@@ -185,7 +220,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     constexpr int TGMAX = kFpRays / QP > 0 ? kFpRays / QP : 1;
     constexpr int NR = TGMAX * QP;
     extern __shared__ __align__(16) unsigned char smem[];
-    const Smem L = layout(ZC, a.W, TGMAX);
+    const Smem L = layout(ZC, a.W, TGMAX, a.two_rows ? 2 : 1);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     float* raw = reinterpret_cast<float*>(smem + L.raw_off);
     float2* pairs = reinterpret_cast<float2*>(smem + L.pair_off);
@@ -196,8 +231,11 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
     const int PW = L.PW;
     const int TG = min(a.tilts_per_cta, a.T - g0);
-    const int r = j - a.row_off;
+    const int r = a.rowmap ? a.rowmap[j] : j - a.row_off;
     const bool row_in = (r >= 0 && r < H);
+    const float yf = a.rowyf ? a.rowyf[j] : 0.0f;
+    // blend rows r and r + 1 (the raw floor voxel rule makes the last row unblended)
+    const bool blend = a.two_rows && yf != 0.0f && r < H - 1;
     // chunks [c_begin, c_end) of the plane stack belong to this depth part
     const int P = a.zparts > 1 ? a.zparts : 1;
     const int nch_all = (D + ZC - 1) / ZC;
@@ -236,19 +274,28 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
         const uint32_t rowb = (uint32_t)(W * vol_elem_bytes(vt));  // bytes of one plane row
         const unsigned char* volb = static_cast<const unsigned char*>(a.vol);
         unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
+        float* raw1 = raw + (size_t)ZC * W;  // row r + 1 of every plane (blended rows only)
         auto stage = [&](int c) {  // chunk c -> raw
             const int z0 = c * ZC, zn = min(ZC, D - z0);
             if (use_tma) {
                 if (tid == 0) {
                     fence_proxy_async();
-                    mbar_arrive_expect_tx(bar, (uint32_t)zn * rowb);
-                    for (int zz = 0; zz < zn; zz++)
+                    mbar_arrive_expect_tx(bar, (uint32_t)zn * rowb * (blend ? 2u : 1u));
+                    for (int zz = 0; zz < zn; zz++) {
                         tma_load_1d(rawb + (size_t)zz * rowb, volb + ((size_t)(z0 + zz) * H + r) * rowb, rowb, bar);
+                        if (blend)
+                            tma_load_1d(raw1 + (size_t)zz * W, volb + ((size_t)(z0 + zz) * H + r + 1) * rowb, rowb,
+                                        bar);
+                    }
                 }
             } else if (vt == kVolF32) {
                 for (int zz = 0; zz < zn; zz++) {
                     const float* src = reinterpret_cast<const float*>(volb + ((size_t)(z0 + zz) * H + r) * rowb);
                     for (int k = tid; k < W; k += kThreads) raw[(size_t)zz * W + k] = src[k];
+                    if (blend) {
+                        const float* s1 = src + (size_t)W;
+                        for (int k = tid; k < W; k += kThreads) raw1[(size_t)zz * W + k] = s1[k];
+                    }
                 }
             } else {
                 uint16_t* raw16 = reinterpret_cast<uint16_t*>(raw);
@@ -281,7 +328,10 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             }
             for (int zz = 0; zz < zc; zz++) {
                 const bool flat = last_row || (z0 + zz == D - 1);  // raw floor voxel on the last row / plane
-                if (vt == kVolF32)
+                if (blend)
+                    build_pairs_row_blend(raw + (size_t)zz * W, raw1 + (size_t)zz * W, yf, pairs + (size_t)zz * PW, W,
+                                          flat);
+                else if (vt == kVolF32)
                     build_pairs_row(raw + (size_t)zz * W, pairs + (size_t)zz * PW, W, flat);
                 else if (vt == kVolBF16)
                     build_pairs_row16<kVolBF16>(reinterpret_cast<const uint16_t*>(raw) + (size_t)zz * W,
@@ -459,17 +509,11 @@ cudaError_t set_attr_qp() {
     return set_attr_one<QP, 1>();
 }
 
-// Largest chunk (planes per stage) whose shared memory fits two CTAs per SM.
-inline int choose_zc(int W) {
-    for (int zc = 16; zc > 1; zc >>= 1)
-        if (layout(zc, W, kFpRays > 0 ? kFpRays : 1).total <= kMaxSmem) return zc;
-    return 1;
-}
-
 template <int QP>
 cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
-    const int ZC = choose_zc(a.W);
-    const Smem L = layout(ZC, a.W, kFpRays / QP > 0 ? kFpRays / QP : 1);
+    const int rows = a.two_rows ? 2 : 1;
+    const int ZC = fp_choose_zc(a.W, rows);
+    const Smem L = layout(ZC, a.W, kFpRays / QP > 0 ? kFpRays / QP : 1, rows);
     if (L.total > kMaxSmem) return cudaErrorInvalidValue;
     const int use_tma = fp_use_tma(a.W, a.vtype, a.vol);
     dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0, a.zparts > 1 ? a.zparts : 1);

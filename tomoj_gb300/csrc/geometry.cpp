@@ -61,6 +61,48 @@ void find_interval(int n, double za, double zb, F in, int* lo_out, int* cnt_out)
 
 }  // namespace
 
+bool tilt_is_vertical(const double* R) {
+    return R[0] != 0.0 && R[1] == 0.0 && R[3] == 0.0 && R[4] == 1.0 && R[5] == 0.0;
+}
+
+// projectJosephPartial on a vertical-axis tilt (VoxelProjector3D.java:716-760): icF, zcF and
+// dirY are signed zeros and divY is 1, so the ray's y is the task-stepped jcentered plus
+// the volume centre, constant along the ray; getPixel (TomoReconstruction2.java:154-190)
+// then takes ybase = (int)y and yFraction = (float)y - ybase.
+void build_fp_rowmap(const Geometry& g, int j0, int* row, float* yf) {
+    const double jinc = 1.0 / g.scale;
+    const double bYmax = (double)((float)g.H + 1e-10f);
+    for (int j = 0; j < g.h; j++) {
+        row[j] = -1;
+        yf[j] = 0.0f;
+        if (j < j0) continue;
+        const int s = j0 + 2 * ((j - j0) / 2);  // first row of the reference's 2-row task
+        double jc = (s - 1.0 - g.pc[1]) / g.scale;
+        jc = jc + jinc;
+        if (j == s + 1) jc = jc + jinc;
+        const double y = jc + g.vc[1];
+        if (!(y + kAcc >= 0 && y < bYmax)) continue;
+        const int yb = (y < 0) ? 0 : (int)y;
+        row[j] = yb;
+        yf[j] = (y < 0) ? 0.0f : (float)y - (float)yb;
+    }
+}
+
+// backProjectPartial on a vertical-axis tilt (VoxelProjector3D.java:266-283): the x~ R10
+// and z~ R12 terms are signed zeros, so yy = y~ * scale + cy for the whole row, and the
+// voxel is inside when 0 <= yy < h.
+void build_bp_rowmap(const Geometry& g, int* row, float* yf) {
+    for (int r = 0; r < g.H; r++) {
+        const double yy = (r - g.vc[1]) * g.scale + g.pc[3];
+        row[r] = -1;
+        yf[r] = 0.0f;
+        if (!(yy >= 0 && yy < g.h)) continue;
+        const int yb = (int)yy;
+        row[r] = yb;
+        yf[r] = (float)(yy - yb);
+    }
+}
+
 bool tilt_is_separable(const double* R, const Geometry& g) {
     if (g.scale != 1.0) return false;
     if (!(R[0] != 0.0)) return false;
@@ -157,9 +199,10 @@ void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* ra
 // signed zero, so the decision depends on (x, z) only.
 void build_bp_tables(const Geometry& g, const double* R, BpTilt* tilt, int32_t* zint) {
     const double cix = g.pc[2];
-    tilt->C = to_fix(R[0]);
-    tilt->S = to_fix(R[2]);
-    tilt->K = to_fix(cix - g.vc[0] * R[0] - g.vc[2] * R[2]);
+    const double sc = g.scale;
+    tilt->C = to_fix(R[0] * sc);
+    tilt->S = to_fix(R[2] * sc);
+    tilt->K = to_fix(cix - g.vc[0] * R[0] * sc - g.vc[2] * R[2] * sc);
     for (int x = 0; x < g.W; x++) {
         const double xt = x - g.vc[0];
         const double a = xt * R[0] + 0.0 * R[1];

@@ -30,11 +30,19 @@ constexpr int kBpThreads = 256;
 constexpr int kTX = 64;
 constexpr int kTZ = 64;
 constexpr int kKZ = 16;      // voxels per thread along z
-constexpr int kTC = 32;      // tilts staged per chunk
-constexpr int kSeg = 96;     // >= 63 * (|cos| + |sin|) + 3 pairs per tilt segment
-constexpr int kRawSeg = 104; // floats staged per tilt (kSeg + 1 rounded up to float4, + alignment slack)
+// Image-row segment a tile projects onto: 63 * scale * (|cos| + |sin|) + 3 pairs per
+// tilt.  SEG = 96 covers scale 1; SEG = 192 (with half as many tilts per chunk, to stay
+// within static shared memory) covers scale up to 2.1.
+template <int SEG>
+struct BpSeg {
+    static constexpr int kTC = SEG <= 96 ? 32 : 16;  // tilts staged per chunk
+    static constexpr int kSeg = SEG;
+    static constexpr int kRawSeg = SEG + 8;           // floats staged per tilt (kSeg + 1 up to float4, + slack)
+};
 
+template <int SEG>
 struct BpShared {
+    static constexpr int kTC = BpSeg<SEG>::kTC, kSeg = BpSeg<SEG>::kSeg, kRawSeg = BpSeg<SEG>::kRawSeg;
     float2 seg[kTC * kSeg];  // tilt t's pairs at [t * kSeg, (t + 1) * kSeg)
     float raw[kTC][kRawSeg];
     int seg_start[kTC];
@@ -88,15 +96,20 @@ __device__ __forceinline__ void bp_acc(float& vox, float& comp, float val) {
 }
 
 // One CTA's work: tile (x0, z0) of volume row r of problem `a`.
-template <bool SANITIZE, bool POS, int VT>
+template <bool SANITIZE, bool POS, int VT, int SEG>
 __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const int z0, const int r) {
-    __shared__ __align__(16) BpShared sh;
+    constexpr int kTC = BpSeg<SEG>::kTC, kSeg = BpSeg<SEG>::kSeg, kRawSeg = BpSeg<SEG>::kRawSeg;
+    __shared__ __align__(16) BpShared<SEG> sh;
     const int tid = threadIdx.x;
     const int tx = tid & (kTX - 1);
     const int tzg = tid >> 6;
     const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
-    const int jp = r + a.row_off;  // projection row seen by this volume row
+    const int jp = a.bprow ? a.bprow[r] : r + a.row_off;  // projection row seen by this volume row
     if (jp < 0 || jp >= h) return;  // no tilt reaches this row (yy outside [0,h))
+    // fractional rows: blend projection rows jp and jp + 1 with weight byf (ImageJ's bilinear
+    // weight along y); at jp = h - 1 ImageJ blends the row with itself
+    const float byf = a.bpyf ? a.bpyf[r] : 0.0f;
+    const bool blend = byf != 0.0f && jp < h - 1;
     const int x = x0 + tx;
     const int zs = z0 + tzg * kKZ;
     const bool xin = x < W;
@@ -146,20 +159,30 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
         }
         __syncthreads();
         // --- stage image segments: 128-bit loads of the row, then (value, slope) pairs --
-        // one warp per tilt, lane v < 26 loads 4 floats
-        for (int t = tid >> 5; t < tc; t += kBpThreads / 32) {
-            const int v = tid & 31;
-            if (v >= kRawSeg / 4) continue;
+        // one warp per tilt, each lane loading 4 floats at a time
+        for (int t = tid >> 5; t < tc; t += kBpThreads / 32)
+          for (int v = tid & 31; v < kRawSeg / 4; v += 32) {
             const float* row = a.img + ((size_t)(c0 + t) * h + jp) * w;
             const int k0 = sh.raw_start[t] + 4 * v;
-            float4 q;
-            if (vec4 && k0 >= 0 && k0 + 3 < w) {
-                q = *reinterpret_cast<const float4*>(row + k0);
-            } else {
-                q.x = row[min(max(k0 + 0, 0), w - 1)];
-                q.y = row[min(max(k0 + 1, 0), w - 1)];
-                q.z = row[min(max(k0 + 2, 0), w - 1)];
-                q.w = row[min(max(k0 + 3, 0), w - 1)];
+            auto load4 = [&](const float* rw) {
+                float4 q;
+                if (vec4 && k0 >= 0 && k0 + 3 < w) {
+                    q = *reinterpret_cast<const float4*>(rw + k0);
+                } else {
+                    q.x = rw[min(max(k0 + 0, 0), w - 1)];
+                    q.y = rw[min(max(k0 + 1, 0), w - 1)];
+                    q.z = rw[min(max(k0 + 2, 0), w - 1)];
+                    q.w = rw[min(max(k0 + 3, 0), w - 1)];
+                }
+                return q;
+            };
+            float4 q = load4(row);
+            if (blend) {
+                const float4 q1 = load4(row + w);
+                q.x = __fadd_rn(q.x, __fmul_rn(byf, __fsub_rn(q1.x, q.x)));
+                q.y = __fadd_rn(q.y, __fmul_rn(byf, __fsub_rn(q1.y, q.y)));
+                q.z = __fadd_rn(q.z, __fmul_rn(byf, __fsub_rn(q1.z, q.z)));
+                q.w = __fadd_rn(q.w, __fmul_rn(byf, __fsub_rn(q1.w, q.w)));
             }
             *reinterpret_cast<float4*>(&sh.raw[t][4 * v]) = q;
         }
@@ -181,8 +204,9 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
                 // arises from fixed-point rounding of positions just above 0.
                 k0 = k1 = (k < 0) ? 0 : w - 1;
                 v0 = row[k0];
+                if (blend) v0 = __fadd_rn(v0, __fmul_rn(byf, __fsub_rn(row[w + k0], v0)));
             }
-            if (SANITIZE) {
+            if (SANITIZE && !blend) {
                 // getInterpolatedValue blends in the next row with weight 0, so a
                 // non-finite neighbour there still turns the sample into NaN.
                 const float* up = (jp < h - 1) ? row + w : row;
@@ -266,9 +290,9 @@ struct BpOcc {
     static constexpr int value = VT == kVolF32 ? TOMO_BP_MIN_BLOCKS : 2;
 };
 
-template <bool SANITIZE, bool POS, int VT>
+template <bool SANITIZE, bool POS, int VT, int SEG>
 __global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value) bp_separable_kernel(const __grid_constant__ BpLaunch a) {
-    bp_body<SANITIZE, POS, VT>(a, blockIdx.x * kTX, blockIdx.y * kTZ, a.y0 + blockIdx.z);
+    bp_body<SANITIZE, POS, VT, SEG>(a, blockIdx.x * kTX, blockIdx.y * kTZ, a.y0 + blockIdx.z);
 }
 
 // Batched form: CTA b works on item {problem, x tile, z tile, row} of many problems.
@@ -276,7 +300,7 @@ template <bool SANITIZE, bool POS, int VT>
 __global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value)
     bp_kernel_batch(const BpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
-    bp_body<SANITIZE, POS, VT>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
+    bp_body<SANITIZE, POS, VT, 96>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
 }
 
 template <int VT>
@@ -290,14 +314,14 @@ void bp_batch_vt(bool sanitize, bool positivity, const BpLaunch* descs, const in
     }
 }
 
-template <int VT>
+template <int VT, int SEG>
 void bp_separable_vt(const BpLaunch& a, dim3 grid, cudaStream_t s) {
     if (a.sanitize) {
-        if (a.positivity) bp_separable_kernel<true, true, VT><<<grid, kBpThreads, 0, s>>>(a);
-        else bp_separable_kernel<true, false, VT><<<grid, kBpThreads, 0, s>>>(a);
+        if (a.positivity) bp_separable_kernel<true, true, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
+        else bp_separable_kernel<true, false, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
     } else {
-        if (a.positivity) bp_separable_kernel<false, true, VT><<<grid, kBpThreads, 0, s>>>(a);
-        else bp_separable_kernel<false, false, VT><<<grid, kBpThreads, 0, s>>>(a);
+        if (a.positivity) bp_separable_kernel<false, true, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
+        else bp_separable_kernel<false, false, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
     }
 }
 
@@ -305,6 +329,7 @@ void bp_separable_vt(const BpLaunch& a, dim3 grid, cudaStream_t s) {
 
 int bp_tile_x() { return kTX; }
 int bp_tile_z() { return kTZ; }
+int bp_segment_pairs(bool wide) { return wide ? 192 : 96; }
 
 cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpLaunch* descs, const int4* items,
                             int n_items, cudaStream_t s) {
@@ -320,9 +345,12 @@ cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpL
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s) {
     if (a.T <= 0 || a.y1 <= a.y0) return cudaSuccess;
     dim3 grid((a.W + kTX - 1) / kTX, (a.D + kTZ - 1) / kTZ, a.y1 - a.y0);
-    if (a.vtype == kVolF32) bp_separable_vt<kVolF32>(a, grid, s);
-    else if (a.vtype == kVolBF16) bp_separable_vt<kVolBF16>(a, grid, s);
-    else if (a.vtype == kVolF16) bp_separable_vt<kVolF16>(a, grid, s);
+    if (a.wide_seg) {
+        if (a.vtype != kVolF32) return cudaErrorInvalidValue;
+        bp_separable_vt<kVolF32, 192>(a, grid, s);
+    } else if (a.vtype == kVolF32) bp_separable_vt<kVolF32, 96>(a, grid, s);
+    else if (a.vtype == kVolBF16) bp_separable_vt<kVolBF16, 96>(a, grid, s);
+    else if (a.vtype == kVolF16) bp_separable_vt<kVolF16, 96>(a, grid, s);
     else return cudaErrorInvalidValue;
     count_launch();
     return cudaGetLastError();

@@ -52,8 +52,8 @@ int fp_qp(int w) {
 }
 
 // Shared-memory bytes of a CTA for width W and planes per chunk ZC (matches fpk::layout).
-size_t fp_smem_bytes(int ZC, int W, int qp) {
-    size_t o = 16 + (size_t)ZC * W * sizeof(float);
+size_t fp_smem_bytes(int ZC, int W, int qp, int rows) {
+    size_t o = 16 + (size_t)rows * ZC * W * sizeof(float);
     o = (o + 15) & ~(size_t)15;
     o += (size_t)ZC * (W + 4) * sizeof(float2);
     o = (o + 15) & ~(size_t)15;
@@ -61,9 +61,9 @@ size_t fp_smem_bytes(int ZC, int W, int qp) {
     return o;
 }
 
-int fp_choose_zc(int W) {
+int fp_choose_zc(int W, int rows) {
     for (int zc = 16; zc > 1; zc >>= 1)
-        if (fp_smem_bytes(zc, W, 1) <= kFpSmemBudget) return zc;
+        if (fp_smem_bytes(zc, W, 1, rows) <= kFpSmemBudget) return zc;
     return 1;
 }
 

@@ -130,7 +130,7 @@ int auto_tilts_per_cta(const tomo_projector* p, int T, int rows) {
 int fp_split(tomo_projector* p, int T, int rows, int tpc) {
     const Geometry& g = p->g;
     const int groups = (T + tpc - 1) / tpc;
-    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W), p->sms);
+    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W, g.fractional ? 2 : 1), p->sms);
     if (P <= 1) return 1;
     const size_t need_part = (size_t)P * T * p->npix;
     const size_t need_tk = (size_t)groups * g.h;
@@ -161,6 +161,20 @@ int fp_split(tomo_projector* p, int T, int rows, int tpc) {
         p->tickets_cap = need_tk;
     }
     return P;
+}
+
+// Forward row map of the fractional-row form for projections whose tasks start at
+// row j0 (uploaded when j0 changes; the host copy stays alive for captured copies).
+tomo_status ensure_fp_rowmap(tomo_projector* p, int j0) {
+    if (p->fprow_j0 == j0) return TOMO_OK;
+    const Geometry& g = p->g;
+    p->h_fprow.assign(g.h, -1);
+    p->h_fpyf.assign(g.h, 0.0f);
+    build_fp_rowmap(g, j0, p->h_fprow.data(), p->h_fpyf.data());
+    CK(cudaMemcpyAsync(p->d_fprow, p->h_fprow.data(), sizeof(int) * g.h, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_fpyf, p->h_fpyf.data(), sizeof(float) * g.h, cudaMemcpyHostToDevice, p->stream));
+    p->fprow_j0 = j0;
+    return TOMO_OK;
 }
 
 // Forward projection of the current batch, with the fused difference when meas is given.
@@ -240,6 +254,12 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
     a.zparts = fp_split(p, T, j1 - j0, a.tilts_per_cta);
     a.part = p->d_fppart;
     a.tickets = p->d_tickets;
+    if (g.fractional) {
+        CKS(ensure_fp_rowmap(p, j0));
+        a.rowmap = p->d_fprow;
+        a.rowyf = p->d_fpyf;
+        a.two_rows = 1;
+    }
     a.W = g.W;
     a.H = g.H;
     a.D = g.D;
@@ -289,7 +309,7 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     y1 = std::min(g.H, y1);
     if (y1 <= y0 || T <= 0) return TOMO_OK;
     const bool to_dist = diffs && p->bayes;
-    if (!g.separable) {
+    if (!g.separable || p->bp_generic) {
         BpGenericLaunch ga{};
         ga.vol = to_dist ? p->d_dist : p->d_vol;
         ga.img = imgs;
@@ -314,6 +334,11 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
         return TOMO_OK;
     }
     BpLaunch a{};
+    if (g.fractional) {
+        a.bprow = p->d_bprow;
+        a.bpyf = p->d_bpyf;
+    }
+    a.wide_seg = p->bp_wide;
     a.vol = to_dist ? p->bp_target() : p->vol();
     a.vtype = to_dist ? kVolF32 : p->vtype;
     a.vscale = p->d_vscale;
@@ -555,9 +580,46 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
                        pixels_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, p->stream));
     p->euler.assign(euler, euler + 9 * (size_t)N);
     // geometry tables
-    bool sep = true;
-    for (int t = 0; t < N && sep; t++) sep = tilt_is_separable(&p->euler[9 * t], g);
+    bool integral = true, vertical = true;
+    for (int t = 0; t < N; t++) {
+        integral = integral && tilt_is_separable(&p->euler[9 * t], g);
+        vertical = vertical && tilt_is_vertical(&p->euler[9 * t]);
+    }
+    // vertical-axis tilts run on the XZ-plane kernels; rows that are not a whole row
+    // apart (scale != 1, half-row centre offsets) blend two rows (16-bit volumes excepted)
+    const bool sep = integral || (vertical && p->vtype == kVolF32);
     g.separable = sep;
+    g.fractional = sep && !integral;
+    if (g.fractional) {
+        if (!p->d_fprow) {
+            CKS(alloc_n(p, &p->d_fprow, (size_t)g.h));
+            CKS(alloc_n(p, &p->d_fpyf, (size_t)g.h));
+            CKS(alloc_n(p, &p->d_bprow, (size_t)g.H));
+            CKS(alloc_n(p, &p->d_bpyf, (size_t)g.H));
+        }
+        std::vector<int> br(g.H);
+        std::vector<float> by(g.H);
+        build_bp_rowmap(g, br.data(), by.data());
+        CK(cudaMemcpyAsync(p->d_bprow, br.data(), sizeof(int) * g.H, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_bpyf, by.data(), sizeof(float) * g.H, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        p->fprow_j0 = -1;
+    }
+    // image columns one backprojection tile (64 x 64 voxels) may span for a tilt
+    p->bp_wide = 0;
+    p->bp_generic = false;
+    if (sep) {
+        double span = 0;
+        for (int t = 0; t < N; t++) {
+            const double* R = &p->euler[9 * t];
+            span = std::max(span, (bp_tile_x() - 1) * std::fabs(R[0] * g.scale) +
+                                      (bp_tile_z() - 1) * std::fabs(R[2] * g.scale) + 3.0);
+        }
+        if (span > bp_segment_pairs(true)) p->bp_generic = true;
+        else if (span > bp_segment_pairs(false)) p->bp_wide = 1;
+        if ((p->bp_generic || p->bp_wide) && p->vtype != kVolF32)
+            return fail(TOMO_ERR_UNSUPPORTED, "16-bit volume storage needs scale 1");
+    }
     if (sep) {
         g.fp_row_off = (int)(g.pc[1] - g.vc[1]);
         g.bp_row_off = (int)(g.pc[3] - g.vc[1]);
@@ -575,10 +637,11 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
         CK(cudaMemcpyAsync(p->d_zint, zint.data(), sizeof(int32_t) * zint.size(), cudaMemcpyHostToDevice,
                            p->stream));
         CK(cudaStreamSynchronize(p->stream));
-    } else {
+    }
+    if (!sep || p->bp_generic) {
         if (p->vtype != kVolF32)
             return fail(TOMO_ERR_UNSUPPORTED,
-                        "16-bit volume storage needs the separable geometry (vertical tilt axis, scale 1)");
+                        "16-bit volume storage needs a vertical tilt axis, scale 1 and whole-row centre offsets");
         if (!p->d_gtilt) CKS(alloc_n(p, &p->d_gtilt, (size_t)N));
         if (!p->d_euler) CKS(alloc_n(p, &p->d_euler, (size_t)N * 9));
         std::vector<GenericFpTilt> gt(N);
@@ -1083,6 +1146,7 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
         fp_rows(p, y0, &j0, &j1);
         for (int T : {upd, N - (nsub - 1) * upd})
             if (T > 0) fp_split(p, T, j1 - j0, auto_tilts_per_cta(p, T, j1 - j0));
+        if (g.separable && g.fractional) CKS(ensure_fp_rowmap(p, j0));
     }
     auto body = [&](const int* d_ord) -> tomo_status {
         CKS(start_iteration(p));

@@ -42,6 +42,16 @@ struct tomo_projector {
     tomo::FpTilt* d_ftilt = nullptr;
     tomo::FpRay* d_rays = nullptr;
     tomo::BpTilt* d_btilt = nullptr;
+    // fractional rows: forward row map for the task start fprow_j0, backward row map
+    int* d_fprow = nullptr;
+    float* d_fpyf = nullptr;
+    int* d_bprow = nullptr;
+    float* d_bpyf = nullptr;
+    int fprow_j0 = -1;
+    int bp_wide = 0;        // backprojection tiles need the 192-column segments
+    bool bp_generic = false;  // ... or are wider still: the generic backprojector
+    std::vector<int> h_fprow;
+    std::vector<float> h_fpyf;
     tomo::GenericFpTilt* d_gtilt = nullptr;  // generic geometry: per-tilt FP constants
     double* d_euler = nullptr;               // generic geometry: [N][9] Euler matrices
     int32_t* d_zint = nullptr;

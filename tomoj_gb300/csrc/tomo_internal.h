@@ -66,13 +66,23 @@ struct GenericFpTilt {
 struct Geometry {
     int W, H, D, w, h, N;
     double vc[3], pc[4], scale;
-    bool separable;  // all tilts have the vertical-axis form, scale 1, integral row offsets
-    int fp_row_off;  // r = j - fp_row_off for the forward projector
-    int bp_row_off;  // j = r + bp_row_off for the backprojector
+    bool separable;   // all tilts have the vertical-axis form: the XZ-plane kernels apply
+    bool fractional;  // ... but rows map with a blend (scale != 1 or centres not a whole row apart)
+    int fp_row_off;   // integral rows: r = j - fp_row_off for the forward projector
+    int bp_row_off;   // integral rows: j = r + bp_row_off for the backprojector
 };
 
 // Host-side table builders (geometry.cpp).  Return false if the tilt is not separable.
 bool tilt_is_separable(const double* R, const Geometry& g);
+// The vertical-axis form of R (any scale and centres): the XZ-plane kernels apply with
+// row maps (fractional rows).
+bool tilt_is_vertical(const double* R);
+// Row maps of the fractional-row form.  Forward: projection rows [j0, h) of a
+// projection whose 2-row tasks start at j0 (VoxelProjector3D.project) -> volume row
+// (-1 outside) and float blend weight.  Backward: volume rows [0, H) -> projection row
+// (-1 outside) and blend weight (ImageJ getInterpolatedValue's y weight).
+void build_fp_rowmap(const Geometry& g, int j0, int* row, float* yf);
+void build_bp_rowmap(const Geometry& g, int* row, float* yf);
 void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays /* w entries */);
 void build_bp_tables(const Geometry& g, const double* R, BpTilt* tilt, int32_t* zint /* W entries */);
 void build_generic_fp_tilt(const double* R, GenericFpTilt* out);
@@ -120,6 +130,12 @@ struct FpLaunch {
     int zparts;             // 0 or 1: no split
     float* part;
     unsigned* tickets;
+    // Fractional rows (scale != 1 or centres not a whole row apart): projection row j
+    // samples volume rows rowmap[j] and rowmap[j] + 1 blended with weight rowyf[j]
+    // (rowmap[j] < 0: the row misses the volume).  nullptr: row j - row_off, no blend.
+    const int* rowmap;
+    const float* rowyf;
+    int two_rows;           // shared memory holds both rows of every plane
 };
 cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s);
 // Any geometry (kernels_generic.cu): one thread per ray / voxel in the reference's
@@ -158,6 +174,10 @@ inline int fp_use_tma(int W, int vtype, const void* vol) {
 }
 
 struct BpLaunch {
+    // Fractional rows: volume row r reads projection rows bprow[r] and bprow[r] + 1
+    // (clamped) blended with weight bpyf[r]; bprow[r] < 0: outside.  nullptr: row r + row_off.
+    const int* bprow;
+    const float* bpyf;
     void* vol;              // [D][H][W] of vtype
     int vtype;              // VolType; reduced types add with Kahan compensation
     const float* vscale;    // [H] slab scales (reduced types)
@@ -173,6 +193,7 @@ struct BpLaunch {
     int positivity;
     int sanitize;           // apply NaN/Inf checks of the reference (images may be non-finite)
     int* status;
+    int wide_seg;           // tile footprints up to 192 image columns (scale up to ~2.1)
 };
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
 // Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row}.
@@ -180,6 +201,8 @@ cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpL
                             int n_items, cudaStream_t s);
 int bp_tile_x();
 int bp_tile_z();
+// Image columns a BP tile may span for one tilt (segment pairs staged per tilt).
+int bp_segment_pairs(bool wide);
 
 cudaError_t launch_align(const float* raw, float* out, const double* tinv /*[N][6]*/, const double* stats, int N,
                          int w, int h, int normalize, int fill, const unsigned char* identity, cudaStream_t s);
@@ -195,8 +218,8 @@ cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T,
 cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s);
 int fp_max_tilts_per_cta(int w);
 int fp_qp(int w);
-int fp_choose_zc(int W);
-size_t fp_smem_bytes(int ZC, int W, int qp);
+int fp_choose_zc(int W, int rows = 1);
+size_t fp_smem_bytes(int ZC, int W, int qp, int rows = 1);
 // Batched forward projection: CTA b runs items[b] = {descriptor, first tilt, row, use_tma}.
 cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,
                             cudaStream_t s);
