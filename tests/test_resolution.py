@@ -81,3 +81,32 @@ def test_even_odd_available_indexes(n, even, odd):
     assert list(R.available_indexes(n, R.EVEN_PROJECTIONS)) == even
     assert list(R.available_indexes(n, R.ODD_PROJECTIONS)) == odd
     assert list(R.available_indexes(n, R.ALL_PROJECTIONS)) == list(range(n))
+
+
+def _rings_loops(signal, th_s, noise, th_n, ring_width):
+    H, W = signal.shape
+    acc = [np.zeros(W) for _ in range(5)]
+    ps = [np.abs(np.fft.fft2(x.astype(np.float64))) ** 2 for x in (th_s, signal - th_s, th_n, noise - th_n)]
+    for y in range(H):
+        for x in range(W):
+            w = np.sqrt(R.convert_to_frequency(x, W) ** 2 + R.convert_to_frequency(y, H) ** 2) * W
+            l0 = max(0, int(np.ceil(w - ring_width)))
+            lf = int(np.floor(w))
+            for l in range(l0, lf):
+                for a, p in zip(acc, ps):
+                    a[l] += p[y, x]
+                acc[4][l] += 1
+    return acc
+
+
+def test_ssnr_rings_match_the_reference_loops():
+    rng = np.random.default_rng(4)
+    H, W = 10, 16
+    s, ts, n, tn = (rng.normal(0, 1, (H, W)).astype(np.float32) for _ in range(4))
+    acc = [np.zeros(W) for _ in range(5)]
+    R.ssnr_rings(s, ts, n, tn, 4, acc)
+    ref = _rings_loops(s, ts, n, tn, 4)
+    for a, b in zip(acc, ref):
+        assert np.allclose(a, b, rtol=1e-10, atol=1e-9)
+    table = R.ssnr_table(acc)
+    assert table.shape == (9, W // 2 + 1)

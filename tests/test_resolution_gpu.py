@@ -50,3 +50,17 @@ def test_half_reconstructions_and_fsc(engine, oracle_lib, method):
     # both halves image the same object: strong correlation at low frequency
     assert curve.shape == (4, c["W"] // 2 + 1)
     assert np.nanmean(curve[1][1:4]) > 0.5
+
+
+def test_ssnr_on_the_engine(engine):
+    c = series_case(W=48, H=8, D=32, n=21, seed=62, noise=0.02)
+    ts = TiltSeries(c["series"], c["angles"])
+    ts.setNormalize(False)
+    ts.setFillType(_abi.FILL_NAN)
+    params = ReconstructionParameters.createOSSARTParameters(c["W"], c["H"], c["D"], 2, 1.0, 0)
+    est = R.ResolutionEstimation(ts, params, seed=5)
+    table = est.SSNR(ring_width=4)
+    assert table.shape == (9, c["W"] // 2 + 1)
+    assert est.recSignal.shape == (c["D"], c["H"], c["W"]) and est.recNoise.shape == est.recSignal.shape
+    # the phantom's reprojections carry far more low-frequency power than the noise series'
+    assert np.all(np.isfinite(table[3][1:5])) and np.nanmean(table[3][1:5]) > np.nanmean(table[6][1:5])

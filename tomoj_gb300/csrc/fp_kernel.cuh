@@ -90,10 +90,11 @@ __device__ __forceinline__ void build_pairs_row(const float* __restrict__ src, f
 }
 
 // The same pairs from a row stored in 16 bits (reduced-precision volume; the slab
-// scale is applied to the finished ray sum).
+// scale is applied to the finished ray sum).  Out of line, like the blended form
+// below: only the FP32 builder sits in the sampling loop's instruction footprint.
 template <int VT>
-__device__ __forceinline__ void build_pairs_row16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W,
-                                                  bool flat) {
+__device__ __noinline__ void build_pairs_row16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W,
+                                               bool flat) {
     const int tid = threadIdx.x;
     if ((W & 3) == 0) {
         for (int m = tid; m < W / 4; m += kThreads) {
@@ -126,8 +127,9 @@ __device__ __forceinline__ void build_pairs_row16(const uint16_t* __restrict__ s
 // weight yf: b = v0 + yf (v1 - v0), then pairs of b as above.  The reference returns
 // the raw voxel of row r (unblended) at the last column, so that slot keeps v0; on
 // the last plane (`flat`) every sample is the raw voxel of row r.
-__device__ __forceinline__ void build_pairs_row_blend(const float* __restrict__ src0, const float* __restrict__ src1,
-                                                      float yf, float2* __restrict__ dst, int W, bool flat) {
+static __device__ __noinline__ void build_pairs_row_blend(const float* __restrict__ src0,
+                                                         const float* __restrict__ src1, float yf,
+                                                         float2* __restrict__ dst, int W, bool flat) {
     const int tid = threadIdx.x;
     if (flat) {
         for (int k = tid; k < W; k += kThreads) dst[k + 2] = make_float2(src0[k], 0.0f);
@@ -344,8 +346,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             if (c + 1 < c_end && use_tma) stage(c + 1);
             const float2* P = pairs + 2;
 #pragma unroll
-            for (int k = 0; k < NR; k++) {
-                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
+            auto one_ray = [&](const int k) {
                 const long long st = s_step[k / QP];
                 const int za = zab[k] & 0xFFFF;
                 const int cnt = (int)((uint32_t)zab[k] >> 16);
@@ -387,6 +388,11 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                     acc[k] += po.s;
 #endif
                 }
+            };
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
+                one_ray(k);
             }
             __syncthreads();
             if (c + 1 < c_end && !use_tma) stage(c + 1);

@@ -16,7 +16,10 @@ shell by shell:
   * frc (:376-454): the same on one pair of images with a circular mask;
   * frcSlices (:275-374): per-slice 2-D FFTs with a cylinder mask; the shell sums
     are not reset between slices, so slice z reports the sums over slices 0..z
-    (reproduced as the reference computes it).
+    (reproduced as the reference computes it);
+  * SSNR (:167-273, 581-697): the series and a Gaussian-noise series of the same
+    geometry are reconstructed and reprojected; per tilt the power spectra of the
+    reprojections and of the residuals accumulate over rings of width ringWidth.
 
 The reference transforms float data with ParallelColt (absent from the reference
 tree); here the transforms are numpy's double-precision FFTs.  The result agrees
@@ -178,9 +181,64 @@ def subseries(ts: TiltSeries, indexes) -> TiltSeries:
     return sub
 
 
+def ssnr_rings(signal, th_signal, noise, th_noise, ring_width, acc):
+    """ResolutionEstimation.addToVectors1D (:581-697) for one tilt: power spectra of the
+    reprojection th and of the residual (exp - th) for the signal and the noise series,
+    each pixel adding to the rings l in [max(0, ceil(|f| W - ringWidth)), floor(|f| W)).
+    acc = [S_S, S_N, N_S, N_N, K] (length W each) is updated in place."""
+    def clean(a):
+        return np.nan_to_num(np.asarray(a, np.float32), nan=0.0)
+
+    sig, th_s, noi, th_n = clean(signal), clean(th_signal), clean(noise), clean(th_noise)
+    sig = sig - th_s
+    noi = noi - th_n
+    H, W = sig.shape
+    ps = [np.abs(np.fft.fft2(x.astype(np.float64))) ** 2 for x in (th_s, sig, th_n, noi)]
+    fy = convert_to_frequency(np.arange(H), H) ** 2
+    fx = convert_to_frequency(np.arange(W), W) ** 2
+    widx = (np.sqrt(fx[None, :] + fy[:, None]) * W).ravel()
+    l0 = np.maximum(0, np.ceil(widx - ring_width)).astype(np.int64)
+    lf = np.floor(widx).astype(np.int64)
+    # each pixel adds to rings l0 .. lf - 1: a difference array over the ring index
+    n = acc[0].size
+    for arr, w in zip(acc, ps + [None]):
+        d = np.zeros(n + 1)
+        weight = np.ones(widx.size) if w is None else w.ravel()
+        ok = lf > l0
+        np.add.at(d, l0[ok], weight[ok])
+        np.add.at(d, np.minimum(lf[ok], n), -weight[ok])
+        arr += np.cumsum(d)[:n]
+    return acc
+
+
+def ssnr_table(acc, pixel_size=1.0):
+    """The SSNR output rows of ResolutionEstimation.SSNR (:206-265): index, frequency,
+    corrected SSNR (dB), signal SNR, signal power and residual power (dB), and the same
+    three for the noise series, up to the Nyquist ring."""
+    S_S, S_N, N_S, N_N, K = (np.array(a, np.float64) for a in acc)
+    n = S_S.size
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s_snr = S_S / S_N
+        n_snr = N_S / N_N
+        S_S, S_N, N_S, N_N = S_S / K, S_N / K, N_S / K, N_N / K
+        imgno = 1 + n  # the reference counts one per ring before writing the table
+        rows = []
+        for i in range(n):
+            w = float(convert_to_frequency(i, n))
+            if w < 0:
+                break
+            ss = s_snr[i] / n_snr[i]
+            rows.append([i, w / pixel_size, 10 * np.log10(ss - 1) if ss > 1 else -1000.0, s_snr[i],
+                         10 * np.log10(S_S[i] / imgno), 10 * np.log10(S_N[i] / imgno), n_snr[i],
+                         10 * np.log10(N_S[i] / imgno), 10 * np.log10(N_N[i] / imgno)])
+    return np.array(rows).T
+
+
 class ResolutionEstimation:
     """ResolutionEstimation on the engine: generateFSCData reconstructs the even and odd
-    halves with `params` (WBP, OS-SART / SIRT or TVM), fsc() compares them."""
+    halves with `params` (WBP, OS-SART / SIRT or TVM), fsc() compares them; SSNR()
+    reconstructs the series and a Gaussian-noise series with the same geometry and
+    compares each projection with its reprojection ring by ring."""
 
     def __init__(self, ts: TiltSeries, params: ReconstructionParameters, seed: int = 0):
         self.ts = ts
@@ -210,3 +268,46 @@ class ResolutionEstimation:
     def fsc(self) -> np.ndarray:
         self.generateFSCData()
         return fsc(self.recFSCeven, self.recFSCodd)
+
+    def _reconstruct_and_reproject(self, ts: TiltSeries):
+        """Reconstruction, each aligned projection and its reprojection."""
+        p = self.params
+        rec = TomoReconstruction2(p.width, p.height, p.depth)
+        proj = p.getProjector(ts, rec)
+        try:
+            if p.reconstructionType in (BP, WBP):
+                rec.WBP(ts, proj, p)
+            else:
+                rec.OSSART(ts, proj, p, seed=self.seed)
+            n = ts.getImageStackSize()
+            exp, th = [], []
+            for i in range(n):
+                proj.clearAllProjections()
+                proj.addProjection(i)
+                proj.project(0, p.height)
+                th.append(proj.getProjection(0))
+                exp.append(proj.getAlignedProjection(i))
+            proj.clearAllProjections()
+            return rec.getVolume(), exp, th
+        finally:
+            proj.close()
+
+    def SSNR(self, ring_width: int = 4, pixel_size: float = 1.0, noise_seed: int = 12345) -> np.ndarray:
+        """ResolutionEstimation.SSNR (:167-273) without the volumetric SSNR: the noise
+        series is N(0, 1) per pixel from a seeded generator (the reference draws it with
+        ImageJ's ImageProcessor.noise(1))."""
+        ts = self.ts
+        self.recSignal, exp_s, th_s = self._reconstruct_and_reproject(ts)
+        rng = np.random.Generator(np.random.PCG64(noise_seed))
+        noise_pixels = rng.normal(0.0, 1.0, ts.pixels.shape).astype(np.float32)
+        tsn = TiltSeries(noise_pixels, ts.tiltAngles)
+        tsn.setNormalize(ts.isNormalized())
+        tsn.setFillType(ts.getFillType())
+        tsn.alignment = _FixedAlignment(ts.transforms(), ts.eulers())
+        self.recNoise, exp_n, th_n = self._reconstruct_and_reproject(tsn)
+        W = ts.getWidth()
+        acc = [np.zeros(W) for _ in range(5)]
+        for i in range(ts.getImageStackSize()):
+            ssnr_rings(exp_s[i], th_s[i], exp_n[i], th_n[i], ring_width, acc)
+        self.ssnr = ssnr_table(acc, pixel_size)
+        return self.ssnr
