@@ -90,11 +90,10 @@ __device__ __forceinline__ void build_pairs_row(const float* __restrict__ src, f
 }
 
 // The same pairs from a row stored in 16 bits (reduced-precision volume; the slab
-// scale is applied to the finished ray sum).  Out of line, like the blended form
-// below: only the FP32 builder sits in the sampling loop's instruction footprint.
+// scale is applied to the finished ray sum).
 template <int VT>
-__device__ __noinline__ void build_pairs_row16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W,
-                                               bool flat) {
+__device__ __forceinline__ void build_pairs_row16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W,
+                                                  bool flat) {
     const int tid = threadIdx.x;
     if ((W & 3) == 0) {
         for (int m = tid; m < W / 4; m += kThreads) {
@@ -127,9 +126,8 @@ __device__ __noinline__ void build_pairs_row16(const uint16_t* __restrict__ src,
 // weight yf: b = v0 + yf (v1 - v0), then pairs of b as above.  The reference returns
 // the raw voxel of row r (unblended) at the last column, so that slot keeps v0; on
 // the last plane (`flat`) every sample is the raw voxel of row r.
-static __device__ __noinline__ void build_pairs_row_blend(const float* __restrict__ src0,
-                                                         const float* __restrict__ src1, float yf,
-                                                         float2* __restrict__ dst, int W, bool flat) {
+__device__ __forceinline__ void build_pairs_row_blend(const float* __restrict__ src0, const float* __restrict__ src1,
+                                                      float yf, float2* __restrict__ dst, int W, bool flat) {
     const int tid = threadIdx.x;
     if (flat) {
         for (int k = tid; k < W; k += kThreads) dst[k + 2] = make_float2(src0[k], 0.0f);
@@ -216,13 +214,15 @@ static __device__ __noinline__ PartialOut full_chunk_call(const float2* __restri
 
 // One CTA's work: projection row j, tilts [g0, g0 + tilts_per_cta) of problem `a`,
 // depth part zp of a.zparts.
-template <int QP, int ZC>
+// BLEND: the fractional-row form (row maps, two staged rows per plane).  A separate
+// instantiation, so that the whole-row kernels compile without any of it.
+template <int QP, int ZC, bool BLEND>
 __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma,
                                         const int zp) {
     constexpr int TGMAX = kFpRays / QP > 0 ? kFpRays / QP : 1;
     constexpr int NR = TGMAX * QP;
     extern __shared__ __align__(16) unsigned char smem[];
-    const Smem L = layout(ZC, a.W, TGMAX, a.two_rows ? 2 : 1);
+    const Smem L = layout(ZC, a.W, TGMAX, BLEND ? 2 : 1);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     float* raw = reinterpret_cast<float*>(smem + L.raw_off);
     float2* pairs = reinterpret_cast<float2*>(smem + L.pair_off);
@@ -233,11 +233,11 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
     const int PW = L.PW;
     const int TG = min(a.tilts_per_cta, a.T - g0);
-    const int r = a.rowmap ? a.rowmap[j] : j - a.row_off;
+    const int r = BLEND ? a.rowmap[j] : j - a.row_off;
     const bool row_in = (r >= 0 && r < H);
-    const float yf = a.rowyf ? a.rowyf[j] : 0.0f;
+    const float yf = BLEND ? a.rowyf[j] : 0.0f;
     // blend rows r and r + 1 (the raw floor voxel rule makes the last row unblended)
-    const bool blend = a.two_rows && yf != 0.0f && r < H - 1;
+    const bool blend = BLEND && yf != 0.0f && r < H - 1;
     // chunks [c_begin, c_end) of the plane stack belong to this depth part
     const int P = a.zparts > 1 ? a.zparts : 1;
     const int nch_all = (D + ZC - 1) / ZC;
@@ -276,16 +276,16 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
         const uint32_t rowb = (uint32_t)(W * vol_elem_bytes(vt));  // bytes of one plane row
         const unsigned char* volb = static_cast<const unsigned char*>(a.vol);
         unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
-        float* raw1 = raw + (size_t)ZC * W;  // row r + 1 of every plane (blended rows only)
+        float* raw1 = BLEND ? raw + (size_t)ZC * W : nullptr;  // row r + 1 of every plane (blended rows)
         auto stage = [&](int c) {  // chunk c -> raw
             const int z0 = c * ZC, zn = min(ZC, D - z0);
             if (use_tma) {
                 if (tid == 0) {
                     fence_proxy_async();
-                    mbar_arrive_expect_tx(bar, (uint32_t)zn * rowb * (blend ? 2u : 1u));
+                    mbar_arrive_expect_tx(bar, (uint32_t)zn * rowb * (BLEND && blend ? 2u : 1u));
                     for (int zz = 0; zz < zn; zz++) {
                         tma_load_1d(rawb + (size_t)zz * rowb, volb + ((size_t)(z0 + zz) * H + r) * rowb, rowb, bar);
-                        if (blend)
+                        if (BLEND && blend)
                             tma_load_1d(raw1 + (size_t)zz * W, volb + ((size_t)(z0 + zz) * H + r + 1) * rowb, rowb,
                                         bar);
                     }
@@ -294,7 +294,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 for (int zz = 0; zz < zn; zz++) {
                     const float* src = reinterpret_cast<const float*>(volb + ((size_t)(z0 + zz) * H + r) * rowb);
                     for (int k = tid; k < W; k += kThreads) raw[(size_t)zz * W + k] = src[k];
-                    if (blend) {
+                    if (BLEND && blend) {
                         const float* s1 = src + (size_t)W;
                         for (int k = tid; k < W; k += kThreads) raw1[(size_t)zz * W + k] = s1[k];
                     }
@@ -330,7 +330,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             }
             for (int zz = 0; zz < zc; zz++) {
                 const bool flat = last_row || (z0 + zz == D - 1);  // raw floor voxel on the last row / plane
-                if (blend)
+                if (BLEND && blend)
                     build_pairs_row_blend(raw + (size_t)zz * W, raw1 + (size_t)zz * W, yf, pairs + (size_t)zz * PW, W,
                                           flat);
                 else if (vt == kVolF32)
@@ -346,7 +346,9 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             if (c + 1 < c_end && use_tma) stage(c + 1);
             const float2* P = pairs + 2;
 #pragma unroll
-            auto one_ray = [&](const int k) {
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
                 const long long st = s_step[k / QP];
                 const int za = zab[k] & 0xFFFF;
                 const int cnt = (int)((uint32_t)zab[k] >> 16);
@@ -388,11 +390,6 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                     acc[k] += po.s;
 #endif
                 }
-            };
-#pragma unroll
-            for (int k = 0; k < NR; k++) {
-                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
-                one_ray(k);
             }
             __syncthreads();
             if (c + 1 < c_end && !use_tma) stage(c + 1);
@@ -484,9 +481,9 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     }
 }
 
-template <int QP, int ZC>
+template <int QP, int ZC, bool BLEND>
 __global__ void __launch_bounds__(kThreads, kFpCtasPerSm) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
-    fp_body<QP, ZC>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
+    fp_body<QP, ZC, BLEND>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
 }
 
 // Batched form: CTA b works on item {problem, first tilt, row, use_tma} of many problems.
@@ -494,12 +491,15 @@ template <int QP, int ZC>
 __global__ void __launch_bounds__(kThreads, kFpCtasPerSm)
     fp_kernel_batch(const FpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
-    fp_body<QP, ZC>(descs[it.x], it.y, it.z, it.w, 0);
+    fp_body<QP, ZC, false>(descs[it.x], it.y, it.z, it.w, 0);
 }
 
 template <int QP, int ZC>
 cudaError_t set_attr_one() {
-    cudaError_t e = cudaFuncSetAttribute(fp_kernel<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaError_t e = cudaFuncSetAttribute(fp_kernel<QP, ZC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMaxSmem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(fp_kernel<QP, ZC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(fp_kernel_batch<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kMaxSmem);
@@ -515,6 +515,12 @@ cudaError_t set_attr_qp() {
     return set_attr_one<QP, 1>();
 }
 
+template <int QP, int ZC>
+void launch_zc(const FpLaunch& a, dim3 grid, size_t smem, int use_tma, cudaStream_t s) {
+    if (a.two_rows) fp_kernel<QP, ZC, true><<<grid, kThreads, smem, s>>>(a, use_tma);
+    else fp_kernel<QP, ZC, false><<<grid, kThreads, smem, s>>>(a, use_tma);
+}
+
 template <int QP>
 cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     const int rows = a.two_rows ? 2 : 1;
@@ -524,11 +530,11 @@ cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     const int use_tma = fp_use_tma(a.W, a.vtype, a.vol);
     dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0, a.zparts > 1 ? a.zparts : 1);
     switch (ZC) {
-        case 16: fp_kernel<QP, 16><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
-        case 8: fp_kernel<QP, 8><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
-        case 4: fp_kernel<QP, 4><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
-        case 2: fp_kernel<QP, 2><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
-        default: fp_kernel<QP, 1><<<grid, kThreads, L.total, s>>>(a, use_tma); break;
+        case 16: launch_zc<QP, 16>(a, grid, L.total, use_tma, s); break;
+        case 8: launch_zc<QP, 8>(a, grid, L.total, use_tma, s); break;
+        case 4: launch_zc<QP, 4>(a, grid, L.total, use_tma, s); break;
+        case 2: launch_zc<QP, 2>(a, grid, L.total, use_tma, s); break;
+        default: launch_zc<QP, 1>(a, grid, L.total, use_tma, s); break;
     }
     count_launch();
     return cudaGetLastError();
