@@ -263,7 +263,7 @@ def run_engine(args, wl):
     def load(pixels):
         _abi.check(lib.tomo_load_series(h, pixels.ctypes.data, 0, _abi.ptr(eul, C.c_double),
                                         _abi.ptr(T, C.c_double), _abi.ptr(stats, C.c_double)))
-        _abi.check(lib.tomo_set_weighting(h, wkind, 0.0, None))
+        _abi.check(lib.tomo_set_weighting(h, wkind, 0.0, None, None))
 
     load(series)
     nvox = W * H * D

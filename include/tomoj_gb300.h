@@ -142,11 +142,15 @@ tomo_status tomo_get_difference(tomo_projector* p, int32_t k, float* out_host);
 int32_t tomo_projection_count(tomo_projector* p);
 
 /* ---- options ------------------------------------------------------------ */
-/* WBP weighting applied before every backprojection of original projections
- * (VoxelProjector3D.java:163-166).  radius: FFTWeighting diameter / w
- * (ReconstructionParameters.java:320).  tilt_axes: per-tilt axis angle in
- * degrees (NULL = 0); only 0 is supported on the device. */
-tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, const double* tilt_axes);
+/* WBP weighting applied before every backprojection (VoxelProjector3D.java:163-166),
+ * replacing new FFTWeighting(ts, radius * w) (ReconstructionParameters.java:320,
+ * FFTWeighting.java:22-24).  tilt_deg: per-tilt ts.getTiltAngle(i) in degrees (NULL =
+ * read from the Euler matrices, which then must have a vertical axis); tilt_axes:
+ * per-tilt ts.getTiltAxis(i) in degrees (NULL = 0).  A zero axis filters rows; any
+ * other axis applies the 2-D mask through 2-D transforms (Radermacher only, w and h
+ * up to 4096). */
+tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, const double* tilt_deg,
+                               const double* tilt_axes);
 /* TVM regularisation run at endOfIteration (TVMProjector3D.java:135-157):
  * ROF denoise with theta, g, dt for `iterations` inner steps; iterations 0 disables. */
 tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int32_t iterations);

@@ -205,7 +205,7 @@ def test_wbp_radermacher_matches_oracle(engine, oracle_lib):
     hd = Handle(engine, c, fill=_abi.FILL_AVG)
     try:
         radius = 0.5
-        _abi.check(engine.tomo_set_weighting(hd.h, _abi.WEIGHT_RADERMACHER, radius, None))
+        _abi.check(engine.tomo_set_weighting(hd.h, _abi.WEIGHT_RADERMACHER, radius, None, None))
         _abi.check(engine.tomo_run_wbp(hd.h, 0, c["H"]))
         got = hd.volume()
         ref = np.zeros_like(c["vol"])
@@ -223,7 +223,7 @@ def test_wbp_radermacher_any_width_matches_oracle(engine, oracle_lib, W):
     hd = Handle(engine, c, fill=_abi.FILL_AVG)
     try:
         radius = 0.45
-        _abi.check(engine.tomo_set_weighting(hd.h, _abi.WEIGHT_RADERMACHER, radius, None))
+        _abi.check(engine.tomo_set_weighting(hd.h, _abi.WEIGHT_RADERMACHER, radius, None, None))
         _abi.check(engine.tomo_run_wbp(hd.h, 0, c["H"]))
         got = hd.volume()
         ref = np.zeros_like(c["vol"])

@@ -110,3 +110,52 @@ def test_ssnr_rings_match_the_reference_loops():
         assert np.allclose(a, b, rtol=1e-10, atol=1e-9)
     table = R.ssnr_table(acc)
     assert table.shape == (9, W // 2 + 1)
+
+
+def _swap_loops(data, cx, cy):
+    h, w = data.shape
+    flat = data.ravel()
+    out = np.zeros(h * w, data.dtype)
+    for y in range(h):
+        yy = y * w
+        yyc = y + cy
+        if yyc >= h:
+            yyc -= h
+        yyc *= w
+        out[yyc + cx:yyc + 2 * cx] = flat[yy:yy + cx]
+        out[yyc:yyc + cx] = flat[yy + cx:yy + 2 * cx]
+    return out.reshape(h, w)
+
+
+@pytest.mark.parametrize("h,w", [(8, 12), (7, 9), (5, 6)])
+def test_swap_quadrant_matches_the_reference_copies(h, w):
+    d = np.arange(h * w, dtype=np.float32).reshape(h, w) + 1
+    out = R.swap_quadrant_2d(d, w // 2, h // 2)
+    assert np.array_equal(out, _swap_loops(d, w // 2, h // 2))
+    if w % 2:
+        assert np.all(out[:, w - 1] == 0)
+
+
+def test_vssnr_image_matches_the_reference_loop():
+    rng = np.random.default_rng(9)
+    H, W = 6, 10
+    s, ts, n, tn = (rng.normal(0, 1, (H, W)).astype(np.float32) for _ in range(4))
+    s[1, 2] = np.nan
+    tn[:] = 0.0  # alpha = 0: ISSNR / 0 = Inf, the SSNR saturates to Inf dB
+    tn[0, 0] = 1.0
+    img = R.vssnr_image(s, ts, n, tn)
+    s0 = np.nan_to_num(s, nan=0.0)
+    ps = [np.abs(np.fft.fft2(x.astype(np.float64))) ** 2 for x in (s0 - ts, ts, n - tn, tn)]
+    ref = np.zeros((H, W), np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for y in range(H):
+            for x in range(W):
+                issnr = ps[1][y, x] / ps[0][y, x]
+                alpha = ps[3][y, x] / ps[2][y, x]
+                aux = issnr / alpha - 1.0
+                v = np.nan if np.isnan(aux) else max(aux, 0.0)
+                ref[y, x] = np.float32(10.0 * np.log10(v + 1.0))
+    ref = _swap_loops(ref, W // 2, H // 2)
+    assert np.array_equal(np.isnan(img), np.isnan(ref))
+    ok = np.isfinite(ref)
+    assert np.array_equal(img[ok], ref[ok]) and np.array_equal(np.isinf(img), np.isinf(ref))

@@ -59,8 +59,11 @@ def test_ssnr_on_the_engine(engine):
     ts.setFillType(_abi.FILL_NAN)
     params = ReconstructionParameters.createOSSARTParameters(c["W"], c["H"], c["D"], 2, 1.0, 0)
     est = R.ResolutionEstimation(ts, params, seed=5)
-    table = est.SSNR(ring_width=4)
+    table = est.SSNR(ring_width=4, computeVSSNR=True)
     assert table.shape == (9, c["W"] // 2 + 1)
+    # volumetric SSNR: the per-tilt SSNR images reconstructed like the data
+    assert est.tsVSSNR.pixels.shape == c["series"].shape
+    assert est.recVSSNR.shape == (c["D"], c["H"], c["W"]) and np.abs(est.recVSSNR).max() > 0
     assert est.recSignal.shape == (c["D"], c["H"], c["W"]) and est.recNoise.shape == est.recSignal.shape
     # the phantom's reprojections carry far more low-frequency power than the noise series'
     assert np.all(np.isfinite(table[3][1:5])) and np.nanmean(table[3][1:5]) > np.nanmean(table[6][1:5])

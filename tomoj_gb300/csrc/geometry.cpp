@@ -3,7 +3,9 @@
 // Compiled with -ffp-contract=off so that a*b+c is rounded twice, as in Java.
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -304,20 +306,11 @@ void weighting_row_filter(int kind, int w, int nproj, const double* sint, const 
 
 namespace tomo {
 
-// The row filter of a non-power-of-two width as a convolution: h[n] = (1/w) sum_k
-// mask[k] e^{2 pi i k n / w} (real for the even masks used here; the real part is
-// kept), zero-padded to M points and transformed by an M-point radix-2 FFT in double.
-void row_filter_spectrum(const float* mask_row, int w, int M, float2* H) {
-    std::vector<double> re((size_t)M, 0.0), im((size_t)M, 0.0);
-    for (int n = 0; n < w; n++) {
-        double acc = 0.0;
-        for (int k = 0; k < w; k++) {
-            const long long kn = ((long long)k * n) % w;
-            acc += (double)mask_row[k] * std::cos(2.0 * M_PI * (double)kn / w);
-        }
-        re[n] = acc / w;
-    }
-    // iterative radix-2 FFT (forward, e^{-2 pi i})
+namespace {
+
+// In-place iterative radix-2 FFT in double, forward (e^{-2 pi i kn/M}); M a power of two.
+void fft_host(std::vector<double>& re, std::vector<double>& im) {
+    const int M = (int)re.size();
     int logM = 0;
     while ((1 << logM) < M) logM++;
     for (int i = 0; i < M; i++) {
@@ -342,7 +335,104 @@ void row_filter_spectrum(const float* mask_row, int w, int M, float2* H) {
                 im[i + k] += ti;
             }
     }
+}
+
+}  // namespace
+
+// The row filter of a non-power-of-two width as a convolution: h[n] = (1/w) sum_k
+// mask[k] e^{2 pi i k n / w} (real for the even masks used here; the real part is
+// kept), zero-padded to M points and transformed by an M-point radix-2 FFT in double.
+void row_filter_spectrum(const float* mask_row, int w, int M, float2* H) {
+    std::vector<double> re((size_t)M, 0.0), im((size_t)M, 0.0);
+    for (int n = 0; n < w; n++) {
+        double acc = 0.0;
+        for (int k = 0; k < w; k++) {
+            const long long kn = ((long long)k * n) % w;
+            acc += (double)mask_row[k] * std::cos(2.0 * M_PI * (double)kn / w);
+        }
+        re[n] = acc / w;
+    }
+    fft_host(re, im);
     for (int m = 0; m < M; m++) H[m] = make_float2((float)re[m], (float)im[m]);
+}
+
+int dft_grid_size(int n) {
+    if ((n & (n - 1)) == 0) return n;
+    int M = 1;
+    while (M < 2 * n - 1) M <<= 1;
+    return M;
+}
+
+// Bluestein tables: chirp c[k] = exp(-i pi k^2 / n) (k^2 reduced mod 2n in integers so
+// the angle stays exact), bspec = M-point spectrum of conj(c) wrapped to negative
+// indices (b[m] = b[M - m] = conj(c[m])), twiddles exp(-2 pi i k / M).  For a power of
+// two n == M only the twiddles are used.
+void dft_row_tables(int n, int M, float2* chirp, float2* bspec, float2* tw) {
+    for (int k = 0; k < M; k++) {
+        const double a = -2.0 * M_PI * k / M;
+        tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    if (M == n) {
+        for (int k = 0; k < n; k++) chirp[k] = make_float2(1.0f, 0.0f);
+        for (int k = 0; k < M; k++) bspec[k] = make_float2(1.0f, 0.0f);
+        return;
+    }
+    std::vector<double> cr(n), ci(n);
+    for (int k = 0; k < n; k++) {
+        const double a = -M_PI * (double)(((long long)k * k) % (2LL * n)) / n;
+        cr[k] = std::cos(a);
+        ci[k] = std::sin(a);
+        chirp[k] = make_float2((float)cr[k], (float)ci[k]);
+    }
+    std::vector<double> re((size_t)M, 0.0), im((size_t)M, 0.0);
+    re[0] = cr[0];
+    im[0] = -ci[0];
+    for (int k = 1; k < n; k++) {
+        re[k] = re[M - k] = cr[k];
+        im[k] = im[M - k] = -ci[k];
+    }
+    fft_host(re, im);
+    for (int m = 0; m < M; m++) bspec[m] = make_float2((float)re[m], (float)im[m]);
+}
+
+// FFTWeighting.createWeightingMask (FFTWeighting.java:31-65) for per-tilt axis angles,
+// stored transposed (column frequency major) for the column pass.
+void weighting_mask_2d(int w, int h, int nproj, const double* tilt_deg, const double* axis_deg, double diameter,
+                       float* maskT) {
+    const double cx = w / 2.0, cy = h / 2.0;
+    std::vector<double> sint(nproj), cosp(nproj), sinp(nproj);
+    for (int p = 0; p < nproj; p++) {
+        sint[p] = std::sin(tilt_deg[p] * (M_PI / 180.0));
+        cosp[p] = std::cos(axis_deg[p] * (M_PI / 180.0));
+        sinp[p] = std::sin(axis_deg[p] * (M_PI / 180.0));
+    }
+    // w * h * nproj sines: rows are split over the host threads
+    auto rows = [&](int ja, int jb) {
+        for (int j = ja; j < jb; j++) {
+            const double cj = (j > cy) ? j - h : j;
+            for (int i = 0; i < w; i++) {
+                const double ci = (i > cx) ? i - w : i;
+                double weight = 0;
+                for (int p = 0; p < nproj; p++) {
+                    const double zj = (ci * sint[p] * cosp[p] + cj * sint[p] * sinp[p]) / w;
+                    double value = diameter * M_PI * zj;
+                    if (value == 0)
+                        value = 1;
+                    else
+                        value = std::sin(value) / value;
+                    weight += value;
+                }
+                if (weight < 0.005) weight = (double)0.005f;
+                weight *= diameter;
+                maskT[(size_t)i * h + j] = (float)(1 / weight);
+            }
+        }
+    };
+    const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), (h + 7) / 8));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++) pool.emplace_back(rows, (int)((long long)h * t / nt), (int)((long long)h * (t + 1) / nt));
+    rows(0, (int)((long long)h / nt));
+    for (auto& th : pool) th.join();
 }
 
 }  // namespace tomo

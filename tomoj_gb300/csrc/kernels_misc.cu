@@ -89,8 +89,15 @@ __device__ void fft_stages(float2* s, const float2* __restrict__ tw, int n, int 
     __syncthreads();
 }
 
+// bad (optional): per-image flag of a non-finite pixel.  The reference's 2-D transform
+// spreads one NaN or Inf over the whole image; a row filter alone would keep it in
+// its row, so rows of a flagged image are written as NaN.
+__device__ __forceinline__ bool image_bad(const int* bad, int row, int rows_per_img) {
+    return bad != nullptr && bad[row / rows_per_img] != 0;
+}
+
 __global__ void row_filter_kernel(float* img, const float* __restrict__ mask, const float2* __restrict__ tw, int rows,
-                                  int n, int logn) {
+                                  int n, int logn, const int* __restrict__ bad, int rows_per_img) {
     extern __shared__ float2 sbuf[];
     float2* a = sbuf;
     float2* b = sbuf + n;
@@ -107,9 +114,10 @@ __global__ void row_filter_kernel(float* img, const float* __restrict__ mask, co
     }
     fft_stages(b, tw, n, logn, true);
     const float inv = 1.0f / (float)n;
+    const bool bad0 = image_bad(bad, r0, rows_per_img), bad1 = row1 && image_bad(bad, r1, rows_per_img);
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        row0[k] = b[k].x * inv;
-        if (row1) row1[k] = b[k].y * inv;
+        row0[k] = bad0 ? __int_as_float(0x7fc00000) : b[k].x * inv;
+        if (row1) row1[k] = bad1 ? __int_as_float(0x7fc00000) : b[k].y * inv;
     }
 }
 
@@ -119,7 +127,7 @@ __global__ void row_filter_kernel(float* img, const float* __restrict__ mask, co
 // convolution with h (spectrum H, M points) equals the circular one on outputs
 // [w, 2w).  Two real rows are packed into one complex sequence as above (h is real).
 __global__ void row_filter_conv_kernel(float* img, const float2* __restrict__ H, const float2* __restrict__ tw, int rows,
-                                       int w, int M, int logM) {
+                                       int w, int M, int logM, const int* __restrict__ bad, int rows_per_img) {
     extern __shared__ float2 sbuf[];
     float2* a = sbuf;
     const int r0 = 2 * blockIdx.x, r1 = r0 + 1;
@@ -141,10 +149,111 @@ __global__ void row_filter_conv_kernel(float* img, const float2* __restrict__ H,
     }
     fft_stages(b, tw, M, logM, true);
     const float inv = 1.0f / (float)M;
+    const bool bad0 = image_bad(bad, r0, rows_per_img), bad1 = row1 && image_bad(bad, r1, rows_per_img);
     for (int k = threadIdx.x; k < w; k += blockDim.x) {
-        row0[k] = b[w + k].x * inv;
-        if (row1) row1[k] = b[w + k].y * inv;
+        row0[k] = bad0 ? __int_as_float(0x7fc00000) : b[w + k].x * inv;
+        if (row1) row1[k] = bad1 ? __int_as_float(0x7fc00000) : b[w + k].y * inv;
     }
+}
+
+// --- 2-D weighting (tilt axis not vertical) ----------------------------------------
+// FFTWeighting.weighting (FFTWeighting.java:87-112) with a mask that depends on both
+// frequencies: forward DFT of every row, transpose, per column (now a row) forward
+// DFT, multiply by the mask, inverse DFT, transpose back, inverse DFT of every row,
+// real part scaled by 1/(w h).  Each transform runs in shared memory: radix-2 when
+// the length is a power of two, otherwise Bluestein's chirp-z algorithm on a radix-2
+// grid of M >= 2n - 1 points:
+//   X[k] = c[k] * sum_j (x[j] c[j]) conj(c[k - j]),  c[j] = exp(-i pi j^2 / n),
+// the convolution done by an M-point FFT with the precomputed spectrum of the
+// wrapped conj(c).  Inverse transforms are conj(DFT(conj(x))).
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// Forward DFT (conjugated on input and output when conj_io: the inverse) of x[0, n)
+// in shared memory, in place; a and b are M-point work buffers.
+__device__ void dft_row(float2* x, float2* a, float2* b, const DftRowPlan& P, bool conj_io) {
+    const int n = P.n, M = P.M, logM = P.logM;
+    const float cs = conj_io ? -1.0f : 1.0f;
+    if (M == n) {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const float2 v = x[k];
+            a[bitrev(k, logM)] = make_float2(v.x, cs * v.y);
+        }
+        fft_stages(a, P.tw, M, logM, false);
+        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = make_float2(a[k].x, cs * a[k].y);
+        __syncthreads();
+        return;
+    }
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        float2 v = make_float2(0.0f, 0.0f);
+        if (k < n) v = cmulf(make_float2(x[k].x, cs * x[k].y), P.chirp[k]);
+        a[bitrev(k, logM)] = v;
+    }
+    fft_stages(a, P.tw, M, logM, false);
+    for (int k = threadIdx.x; k < M; k += blockDim.x) b[bitrev(k, logM)] = cmulf(a[k], P.bspec[k]);
+    fft_stages(b, P.tw, M, logM, true);
+    const float inv = 1.0f / (float)M;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float2 v = cmulf(b[k], P.chirp[k]);
+        x[k] = make_float2(v.x * inv, cs * v.y * inv);
+    }
+    __syncthreads();
+}
+
+// MODE 0: real rows -> spectra; 1: spectra x mask row (row index mod mask_rows),
+// inverse; 2: spectra -> real rows (real part x scale).  One row per CTA.
+template <int MODE>
+__global__ void dft2_rows_kernel(const float* __restrict__ rin, float2* cio, float* rout, const float* __restrict__ mask,
+                                 DftRowPlan P, int mask_rows, float scale) {
+    extern __shared__ float2 sbuf[];
+    float2* x = sbuf;
+    float2* a = sbuf + P.n;
+    float2* b = a + P.M;
+    const size_t r = blockIdx.x;
+    const int n = P.n;
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        x[k] = MODE == 0 ? make_float2(rin[r * n + k], 0.0f) : cio[r * n + k];
+    __syncthreads();
+    dft_row(x, a, b, P, MODE == 2);
+    if (MODE == 1) {
+        const float* m = mask + (size_t)(r % (size_t)mask_rows) * n;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = make_float2(x[k].x * m[k], x[k].y * m[k]);
+        __syncthreads();
+        dft_row(x, a, b, P, true);
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        if (MODE == 2)
+            rout[r * n + k] = x[k].x * scale;
+        else
+            cio[r * n + k] = x[k];
+    }
+}
+
+// [T][R][C] -> [T][C][R], 32 x 32 tiles.
+__global__ void transpose_c_kernel(const float2* __restrict__ in, float2* __restrict__ out, int R, int Cc) {
+    __shared__ float2 tile[32][33];
+    const size_t base = (size_t)blockIdx.z * R * Cc;
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+        const int r = r0 + dy, c = c0 + threadIdx.x;
+        if (r < R && c < Cc) tile[dy][threadIdx.x] = in[base + (size_t)r * Cc + c];
+    }
+    __syncthreads();
+    for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+        const int c = c0 + dy, r = r0 + threadIdx.x;
+        if (r < R && c < Cc) out[base + (size_t)c * R + r] = tile[threadIdx.x][dy];
+    }
+}
+
+// bad[t] = 1 when image t holds a NaN or an Inf.
+__global__ void image_nonfinite_kernel(const float* __restrict__ imgs, size_t npix, int* bad) {
+    const float* im = imgs + (size_t)blockIdx.y * npix;
+    int f = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x)
+        f |= !isfinite(im[i]);
+    f = __reduce_or_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && f) atomicOr(bad + blockIdx.y, 1);
 }
 
 // Sum over rows of the per-row residuals, one thread per tilt, fixed order.
@@ -487,8 +596,15 @@ cudaError_t misc_init_attributes() {
     cudaError_t e = cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          2 * 4096 * (int)sizeof(float2));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(row_filter_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                2 * kRowConvMaxM * (int)sizeof(float2));
+    e = cudaFuncSetAttribute(row_filter_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             2 * kRowConvMaxM * (int)sizeof(float2));
+    if (e != cudaSuccess) return e;
+    const int dft_smem = (kDft2MaxN + 2 * kRowConvMaxM) * (int)sizeof(float2);
+    e = cudaFuncSetAttribute(dft2_rows_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, dft_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(dft2_rows_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dft_smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(dft2_rows_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dft_smem);
 }
 
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s) {
@@ -516,23 +632,54 @@ cudaError_t launch_align(const float* raw, float* out, const double* tinv, const
 }
 
 cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2* tw, int rows, int w,
-                                 cudaStream_t s) {
+                                 const int* bad, int rows_per_img, cudaStream_t s) {
     int logn = 0;
     while ((1 << logn) < w) logn++;
     if ((1 << logn) != w) return cudaErrorInvalidValue;
     const size_t smem = 2 * (size_t)w * sizeof(float2);
-    row_filter_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, mask_row, tw, rows, w, logn);
+    row_filter_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, mask_row, tw, rows, w, logn, bad, rows_per_img);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_filter_conv(float* img, const float2* H, const float2* tw, int rows, int w, int M,
-                                   cudaStream_t s) {
+                                   const int* bad, int rows_per_img, cudaStream_t s) {
     int logM = 0;
     while ((1 << logM) < M) logM++;
     if ((1 << logM) != M || M < 2 * w - 1 || M > kRowConvMaxM) return cudaErrorInvalidValue;
     const size_t smem = 2 * (size_t)M * sizeof(float2);
-    row_filter_conv_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, H, tw, rows, w, M, logM);
+    row_filter_conv_kernel<<<(rows + 1) / 2, 256, smem, s>>>(img, H, tw, rows, w, M, logM, bad, rows_per_img);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_image_nonfinite(const float* imgs, int T, size_t npix, int* bad, cudaStream_t s) {
+    if (T <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int) * (size_t)T, s);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)std::min<size_t>((npix + 255) / 256, 32), T);
+    image_nonfinite_kernel<<<grid, 256, 0, s>>>(imgs, npix, bad);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weighting_2d(float* imgs, int T, int w, int h, const float* maskT, const DftRowPlan& Pw,
+                                const DftRowPlan& Ph, float2* sa, float2* sb, cudaStream_t s) {
+    if (T <= 0) return cudaSuccess;
+    if (Pw.n != w || Ph.n != h || w > kDft2MaxN || h > kDft2MaxN || T > 65535) return cudaErrorInvalidValue;
+    const size_t smw = (size_t)(Pw.n + 2 * Pw.M) * sizeof(float2);
+    const size_t smh = (size_t)(Ph.n + 2 * Ph.M) * sizeof(float2);
+    const float scale = (float)(1.0 / ((double)w * (double)h));
+    const dim3 tb(32, 8);
+    dft2_rows_kernel<0><<<(unsigned)T * h, 256, smw, s>>>(imgs, sa, nullptr, nullptr, Pw, 1, 1.0f);
+    count_launch();
+    transpose_c_kernel<<<dim3((w + 31) / 32, (h + 31) / 32, T), tb, 0, s>>>(sa, sb, h, w);
+    count_launch();
+    dft2_rows_kernel<1><<<(unsigned)T * w, 256, smh, s>>>(nullptr, sb, nullptr, maskT, Ph, w, 1.0f);
+    count_launch();
+    transpose_c_kernel<<<dim3((h + 31) / 32, (w + 31) / 32, T), tb, 0, s>>>(sb, sa, w, h);
+    count_launch();
+    dft2_rows_kernel<2><<<(unsigned)T * h, 256, smw, s>>>(nullptr, sa, imgs, nullptr, Pw, 1, scale);
     count_launch();
     return cudaGetLastError();
 }

@@ -75,6 +75,18 @@ tomo_status alloc_n(tomo_projector* p, T** ptr, size_t n) {
     return dalloc(p, reinterpret_cast<void**>(ptr), n * sizeof(T));
 }
 
+// Frees one of the handle's allocations early (bytes as allocated) and clears *ptr.
+template <class T>
+void free_n(tomo_projector* p, T** ptr, size_t n) {
+    if (!*ptr) return;
+    cudaFree(*ptr);
+    for (auto& a : p->allocs)
+        if (a == (void*)*ptr) a = nullptr;
+    g_in_use -= n * sizeof(T);
+    p->bytes -= n * sizeof(T);
+    *ptr = nullptr;
+}
+
 tomo_status check_status(tomo_projector* p) {
     int st = 0;
     CK(cudaMemcpyAsync(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
@@ -137,24 +149,14 @@ int fp_split(tomo_projector* p, int T, int rows, int tpc) {
     if (need_part <= p->fppart_cap && need_tk <= p->tickets_cap) return P;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 1;
-    auto release = [&](void* q, size_t bytes) {
-        if (!q) return;
-        cudaFree(q);
-        for (auto& a : p->allocs)
-            if (a == q) a = nullptr;
-        g_in_use -= bytes;
-        p->bytes -= bytes;
-    };
     if (need_part > p->fppart_cap) {
-        release(p->d_fppart, sizeof(float) * p->fppart_cap);
-        p->d_fppart = nullptr;
+        free_n(p, &p->d_fppart, p->fppart_cap);
         p->fppart_cap = 0;
         if (alloc_n(p, &p->d_fppart, need_part) != TOMO_OK) return 1;
         p->fppart_cap = need_part;
     }
     if (need_tk > p->tickets_cap) {
-        release(p->d_tickets, sizeof(unsigned) * p->tickets_cap);
-        p->d_tickets = nullptr;
+        free_n(p, &p->d_tickets, p->tickets_cap);
         p->tickets_cap = 0;
         if (alloc_n(p, &p->d_tickets, need_tk) != TOMO_OK) return 1;
         if (cudaMemsetAsync(p->d_tickets, 0, sizeof(unsigned) * need_tk, p->stream) != cudaSuccess) return 1;
@@ -279,10 +281,27 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
 
 tomo_status apply_weighting(tomo_projector* p, float* imgs, int T) {
     if (p->weight_kind == TOMO_WEIGHT_NONE || T <= 0) return TOMO_OK;
-    if (p->conv_M > 0)
-        CK(launch_row_filter_conv(imgs, p->d_convH, p->d_convTw, T * p->g.h, p->g.w, p->conv_M, p->stream));
-    else
-        CK(launch_row_filter_tw(imgs, p->d_mask, p->d_tw, T * p->g.h, p->g.w, p->stream));
+    const Geometry& g = p->g;
+    if (p->weight2d) {
+        for (int t0 = 0; t0 < T; t0 += p->w2chunk) {
+            const int tc = std::min(p->w2chunk, T - t0);
+            CK(launch_weighting_2d(imgs + (size_t)t0 * p->npix, tc, g.w, g.h, p->d_w2mask, p->w2pw, p->w2ph, p->d_w2a,
+                                   p->d_w2b, p->stream));
+        }
+        return TOMO_OK;
+    }
+    // the row filter is the 2-D filter for a vertical axis, except that the 2-D
+    // transform spreads a non-finite pixel over the whole image: flag such images
+    for (int t0 = 0; t0 < T; t0 += p->imgbad_cap) {
+        const int tc = std::min(p->imgbad_cap, T - t0);
+        float* im = imgs + (size_t)t0 * p->npix;
+        CK(launch_image_nonfinite(im, tc, p->npix, p->d_imgbad, p->stream));
+        if (p->conv_M > 0)
+            CK(launch_row_filter_conv(im, p->d_convH, p->d_convTw, tc * g.h, g.w, p->conv_M, p->d_imgbad, g.h,
+                                      p->stream));
+        else
+            CK(launch_row_filter_tw(im, p->d_mask, p->d_tw, tc * g.h, g.w, p->d_imgbad, g.h, p->stream));
+    }
     return TOMO_OK;
 }
 
@@ -923,7 +942,56 @@ tomo_status tomo_get_difference(tomo_projector* p, int32_t k, float* out_host) {
     return get_slot(p, p ? p->d_diff : nullptr, k, out_host, p && p->diffs_valid);
 }
 
-tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, const double* tilt_axes) {
+// FFTWeighting(ts, diameter) (FFTWeighting.java:22-24, 31-81): the mask reads
+// ts.getTiltAngle(i) and ts.getTiltAxis(i).
+tomo_status set_weighting_2d(tomo_projector* p, double diameter, const std::vector<double>& deg,
+                             const double* tilt_axes) {
+    const Geometry& g = p->g;
+    if (g.w > kDft2MaxN || g.h > kDft2MaxN)
+        return fail(TOMO_ERR_UNSUPPORTED, "2-D weighting supports projections up to 4096 x 4096");
+    const int Mw = dft_grid_size(g.w), Mh = dft_grid_size(g.h);
+    const size_t tw_n = (size_t)g.w + 2 * (size_t)Mw, th_n = (size_t)g.h + 2 * (size_t)Mh;
+    std::vector<float2> tab(tw_n + th_n);
+    dft_row_tables(g.w, Mw, tab.data(), tab.data() + g.w, tab.data() + g.w + Mw);
+    dft_row_tables(g.h, Mh, tab.data() + tw_n, tab.data() + tw_n + g.h, tab.data() + tw_n + g.h + Mh);
+    std::vector<float> maskT(p->npix);
+    weighting_mask_2d(g.w, g.h, g.N, deg.data(), tilt_axes, diameter, maskT.data());
+    // scratch for up to 2^24 complex values per buffer (256 MB for both)
+    const int want = (int)std::max<size_t>(1, std::min<size_t>({(size_t)g.N, 65535, ((size_t)1 << 24) / p->npix}));
+    if (!p->d_w2mask) {
+        CKS(alloc_n(p, &p->d_w2mask, p->npix));
+        CKS(alloc_n(p, &p->d_w2tab, tab.size()));
+    }
+    if (p->w2chunk < want) {
+        free_n(p, &p->d_w2a, (size_t)p->w2chunk * p->npix);
+        free_n(p, &p->d_w2b, (size_t)p->w2chunk * p->npix);
+        p->w2chunk = 0;
+        CKS(alloc_n(p, &p->d_w2a, (size_t)want * p->npix));
+        CKS(alloc_n(p, &p->d_w2b, (size_t)want * p->npix));
+        p->w2chunk = want;
+    }
+    CK(cudaMemcpyAsync(p->d_w2mask, maskT.data(), sizeof(float) * p->npix, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_w2tab, tab.data(), sizeof(float2) * tab.size(), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    auto plan = [](int n, int M, const float2* base) {
+        DftRowPlan P;
+        P.n = n;
+        P.M = M;
+        P.logM = 0;
+        while ((1 << P.logM) < M) P.logM++;
+        P.chirp = base;
+        P.bspec = base + n;
+        P.tw = base + n + M;
+        return P;
+    };
+    p->w2pw = plan(g.w, Mw, p->d_w2tab);
+    p->w2ph = plan(g.h, Mh, p->d_w2tab + tw_n);
+    p->weight2d = true;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, const double* tilt_deg,
+                               const double* tilt_axes) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
     if (kind < TOMO_WEIGHT_NONE || kind > TOMO_WEIGHT_HAMMING_RAMP) return fail(TOMO_ERR_INVALID, "unknown filter");
     if (kind == TOMO_WEIGHT_NONE) {
@@ -932,16 +1000,34 @@ tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, c
     }
     if (!p->series_loaded) return fail(TOMO_ERR_STATE, "load the tilt-series before setting the weighting");
     const Geometry& g = p->g;
+    bool tilted = false;
     if (tilt_axes)
-        for (int t = 0; t < g.N; t++)
-            if (tilt_axes[t] != 0.0)
-                return fail(TOMO_ERR_UNSUPPORTED, "weighting with a non-zero tilt-axis angle needs a 2-D filter");
+        for (int t = 0; t < g.N; t++) tilted = tilted || tilt_axes[t] != 0.0;
+    if (tilted && kind != TOMO_WEIGHT_RADERMACHER)
+        return fail(TOMO_ERR_UNSUPPORTED, "ramp filters need a zero tilt-axis angle");
     if (kind == TOMO_WEIGHT_RADERMACHER && !(radius > 0))
         return fail(TOMO_ERR_INVALID, "Radermacher weighting needs a positive radius");
     std::vector<double> sint(g.N), deg(g.N);
     for (int t = 0; t < g.N; t++) {
-        sint[t] = p->euler[9 * t + 6];  // eulerAngles2Matrix row 2 = (sin(theta) cos(phi), ., .)
-        deg[t] = std::atan2(p->euler[9 * t + 6], p->euler[9 * t + 8]) * (180.0 / M_PI);
+        if (tilt_deg) {
+            deg[t] = tilt_deg[t];
+            sint[t] = std::sin(tilt_deg[t] * (M_PI / 180.0));
+        } else {
+            sint[t] = p->euler[9 * t + 6];  // eulerAngles2Matrix(0, theta, 0) row 2 = (sin(theta), 0, cos(theta))
+            deg[t] = std::atan2(p->euler[9 * t + 6], p->euler[9 * t + 8]) * (180.0 / M_PI);
+        }
+    }
+    if (tilted) {
+        CKS(set_weighting_2d(p, radius * g.w, deg, tilt_axes));
+        p->weight_kind = kind;
+        return TOMO_OK;
+    }
+    p->weight2d = false;
+    if (p->imgbad_cap < g.N) {
+        free_n(p, &p->d_imgbad, (size_t)p->imgbad_cap);
+        p->imgbad_cap = 0;
+        CKS(alloc_n(p, &p->d_imgbad, (size_t)g.N));
+        p->imgbad_cap = g.N;
     }
     std::vector<float> mask(g.w);
     weighting_row_filter(kind, g.w, g.N, sint.data(), deg.data(), radius * g.w, mask.data());
@@ -1112,14 +1198,7 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
     const int upd = (update == 0) ? N : std::min(update, N);
     const double factor = (double)(float)(relax / upd);  // float factorimg (TomoReconstruction2.java:646)
     if (p->orders_cap < n_iter) {
-        if (p->d_orders) {
-            cudaFree(p->d_orders);
-            for (auto& a : p->allocs)
-                if (a == p->d_orders) a = nullptr;
-            g_in_use -= sizeof(int) * (size_t)p->orders_cap * N;
-            p->bytes -= sizeof(int) * (size_t)p->orders_cap * N;
-            p->d_orders = nullptr;
-        }
+        free_n(p, &p->d_orders, (size_t)p->orders_cap * N);
         CKS(alloc_n(p, &p->d_orders, (size_t)std::max(n_iter, 1) * N));
         p->orders_cap = std::max(n_iter, 1);
     }

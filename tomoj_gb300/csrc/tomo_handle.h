@@ -63,6 +63,15 @@ struct tomo_projector {
     float2* d_convH = nullptr;   // non-power-of-two widths: spectrum of the circular kernel
     float2* d_convTw = nullptr;  // and twiddles, conv_M points
     int conv_M = 0;
+    int* d_imgbad = nullptr;  // per-image non-finite flags for the row filters
+    int imgbad_cap = 0;
+    // 2-D weighting (tilt axis not vertical): transposed mask, DFT tables, scratch
+    bool weight2d = false;
+    float* d_w2mask = nullptr;
+    float2* d_w2tab = nullptr;
+    float2 *d_w2a = nullptr, *d_w2b = nullptr;
+    int w2chunk = 0;
+    tomo::DftRowPlan w2pw{}, w2ph{};
     float *d_tv_u = nullptr, *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;
     float* d_prev = nullptr;
 

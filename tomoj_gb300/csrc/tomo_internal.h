@@ -206,12 +206,36 @@ int bp_segment_pairs(bool wide);
 
 cudaError_t launch_align(const float* raw, float* out, const double* tinv /*[N][6]*/, const double* stats, int N,
                          int w, int h, int normalize, int fill, const unsigned char* identity, cudaStream_t s);
-cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2* tw, int rows, int w, cudaStream_t s);
+// Row filters: bad (optional, one flag per image of rows_per_img rows) turns every row
+// of a flagged image into NaN, as the reference's 2-D transform does.
+cudaError_t launch_row_filter_tw(float* img, const float* mask_row, const float2* tw, int rows, int w,
+                                 const int* bad, int rows_per_img, cudaStream_t s);
 // Row filter of any width as a circular convolution (spectrum H and twiddles of M points,
 // M a power of two >= 2w - 1, at most kRowConvMaxM).
 constexpr int kRowConvMaxM = 8192;
 cudaError_t launch_row_filter_conv(float* img, const float2* H, const float2* tw, int rows, int w, int M,
-                                   cudaStream_t s);
+                                   const int* bad, int rows_per_img, cudaStream_t s);
+// bad[t] = 1 when image t (npix floats) holds a NaN or an Inf, else 0.
+cudaError_t launch_image_nonfinite(const float* imgs, int T, size_t npix, int* bad, cudaStream_t s);
+// One DFT length for the 2-D weighting: radix-2 when n is a power of two (M == n),
+// otherwise Bluestein on M >= 2n - 1 points.  Device tables: chirp (n), bspec (M),
+// tw (M) as built by dft_row_tables.
+struct DftRowPlan {
+    int n, M, logM;
+    const float2* chirp;
+    const float2* bspec;
+    const float2* tw;
+};
+constexpr int kDft2MaxN = 4096;
+int dft_grid_size(int n);  // M for length n (n <= kDft2MaxN)
+void dft_row_tables(int n, int M, float2* chirp, float2* bspec, float2* tw);
+// FFTWeighting.createWeightingMask (FFTWeighting.java:31-65), transposed: maskT[i * h + j]
+// is the weight of column frequency i, row frequency j.
+void weighting_mask_2d(int w, int h, int nproj, const double* tilt_deg, const double* axis_deg, double diameter,
+                       float* maskT);
+// 2-D weighting of T images (w x h) in place; sa, sb scratch of T*w*h complex each.
+cudaError_t launch_weighting_2d(float* imgs, int T, int w, int h, const float* maskT, const DftRowPlan& Pw,
+                                const DftRowPlan& Ph, float2* sa, float2* sb, cudaStream_t s);
 cudaError_t launch_diff(const float* meas, const int* tilts, const float* th, const float* norm, float* diff,
                         double* errpart, int T, int w, int h, int j0, int j1, double factor, cudaStream_t s);
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s);

@@ -108,7 +108,14 @@ class VoxelProjector3D(Projector):
 
     # --- setters (VoxelProjector3D.java:78-104) ----------------------------------------
     def setWeighting(self, kind: int, radius: float = 0.0):
-        check(self._lib.tomo_set_weighting(self._h, int(kind), float(radius), None))
+        """new FFTWeighting(ts, radius * w) (ReconstructionParameters.java:320): the mask
+        reads every tilt angle and the tilt axis (FFTWeighting.java:67-81)."""
+        ts = self.ts
+        n = ts.getImageStackSize()
+        tilts = np.ascontiguousarray([ts.getTiltAngle(i) for i in range(n)], np.float64)
+        axes = np.full(n, float(ts.getTiltAxis()), np.float64)
+        check(self._lib.tomo_set_weighting(self._h, int(kind), float(radius), _abi.ptr(tilts, C.c_double),
+                                           _abi.ptr(axes, C.c_double)))
         self.weighting = (kind, radius)
 
     def isWeighting(self) -> bool:

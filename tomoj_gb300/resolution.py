@@ -157,9 +157,10 @@ class _FixedAlignment:
     has in the full series (the reference reconstructs a half from the full series through
     getAvailableIndexes, so consecutive transforms of skipped images still compose)."""
 
-    def __init__(self, transforms, eulers):
+    def __init__(self, transforms, eulers, tiltaxis=0.0):
         self._t = [tuple(map(float, t)) for t in transforms]
         self._e = [np.asarray(e, np.float64) for e in eulers]
+        self.tiltaxis = float(tiltaxis)  # ts.getTiltAxis(), read by the WBP weighting
 
     def getTransform(self, index, combine=None):
         return self._t[index]
@@ -175,7 +176,7 @@ def subseries(ts: TiltSeries, indexes) -> TiltSeries:
     sub.setNormalize(ts.isNormalized())
     sub.setFillType(ts.getFillType())
     T, E = ts.transforms(), ts.eulers()
-    sub.alignment = _FixedAlignment(T[idx], E[idx])
+    sub.alignment = _FixedAlignment(T[idx], E[idx], ts.getTiltAxis())
     if ts.stats is not None:
         sub.setStatistics(np.asarray(ts.statistics())[idx])
     return sub
@@ -209,6 +210,37 @@ def ssnr_rings(signal, th_signal, noise, th_noise, ring_width, acc):
         np.add.at(d, np.minimum(lf[ok], n), -weight[ok])
         arr += np.cumsum(d)[:n]
     return acc
+
+
+def swap_quadrant_2d(data: np.ndarray, cx: int, cy: int) -> np.ndarray:
+    """ResolutionEstimation.swapQuadrant2D (:709-721): row y moves to (y + cy) mod h and
+    its halves [0, cx) and [cx, 2 cx) swap; for an odd width the last column stays 0."""
+    h, w = data.shape
+    out = np.zeros_like(data)
+    rows = (np.arange(h) + cy) % h
+    out[rows, cx:2 * cx] = data[:, :cx]
+    out[rows, :cx] = data[:, cx:2 * cx]
+    return out
+
+
+def vssnr_image(signal, th_signal, noise, th_noise) -> np.ndarray:
+    """The volumetric branch of ResolutionEstimation.addToVectors1D (:632-645) for one
+    tilt: per frequency, 10 log10(max(ISSNR / alpha - 1, 0) + 1) with ISSNR the ratio of
+    the reprojection's power to the residual's for the signal series and alpha the same
+    for the noise series, as float, quadrant-swapped to put the origin at the centre."""
+    def clean(a):
+        return np.nan_to_num(np.asarray(a, np.float32), nan=0.0)
+
+    th_s, th_n = clean(th_signal), clean(th_noise)
+    res_s, res_n = clean(signal) - th_s, clean(noise) - th_n
+    ps = [np.abs(np.fft.fft2(x.astype(np.float64))) ** 2 for x in (res_s, th_s, res_n, th_n)]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        issnr = ps[1] / ps[0]
+        alpha = ps[3] / ps[2]
+        ssnr = np.maximum(issnr / alpha - 1.0, 0.0)  # NaN stays NaN, as Math.max
+        img = (10.0 * np.log10(ssnr + 1.0)).astype(np.float32)
+    h, w = img.shape
+    return swap_quadrant_2d(img, w // 2, h // 2)
 
 
 def ssnr_table(acc, pixel_size=1.0):
@@ -246,6 +278,7 @@ class ResolutionEstimation:
         self.seed = seed
         self.recFSCeven = None
         self.recFSCodd = None
+        self.recVSSNR = None
 
     def _reconstruct(self, ts: TiltSeries) -> np.ndarray:
         p = self.params
@@ -292,10 +325,12 @@ class ResolutionEstimation:
         finally:
             proj.close()
 
-    def SSNR(self, ring_width: int = 4, pixel_size: float = 1.0, noise_seed: int = 12345) -> np.ndarray:
-        """ResolutionEstimation.SSNR (:167-273) without the volumetric SSNR: the noise
-        series is N(0, 1) per pixel from a seeded generator (the reference draws it with
-        ImageJ's ImageProcessor.noise(1))."""
+    def SSNR(self, ring_width: int = 4, pixel_size: float = 1.0, noise_seed: int = 12345,
+             computeVSSNR: bool = False) -> np.ndarray:
+        """ResolutionEstimation.SSNR (:167-273): the noise series is N(0, 1) per pixel from
+        a seeded generator (the reference draws it with ImageJ's ImageProcessor.noise(1)).
+        With computeVSSNR the per-tilt 2-D SSNR images form a new tilt-series (same tilt
+        angles, no alignment) reconstructed with the same parameters: recVSSNR."""
         ts = self.ts
         self.recSignal, exp_s, th_s = self._reconstruct_and_reproject(ts)
         rng = np.random.Generator(np.random.PCG64(noise_seed))
@@ -303,11 +338,19 @@ class ResolutionEstimation:
         tsn = TiltSeries(noise_pixels, ts.tiltAngles)
         tsn.setNormalize(ts.isNormalized())
         tsn.setFillType(ts.getFillType())
-        tsn.alignment = _FixedAlignment(ts.transforms(), ts.eulers())
+        tsn.alignment = _FixedAlignment(ts.transforms(), ts.eulers(), ts.getTiltAxis())
         self.recNoise, exp_n, th_n = self._reconstruct_and_reproject(tsn)
         W = ts.getWidth()
         acc = [np.zeros(W) for _ in range(5)]
         for i in range(ts.getImageStackSize()):
             ssnr_rings(exp_s[i], th_s[i], exp_n[i], th_n[i], ring_width, acc)
         self.ssnr = ssnr_table(acc, pixel_size)
+        if computeVSSNR:
+            imgs = np.array([vssnr_image(exp_s[i], th_s[i], exp_n[i], th_n[i])
+                             for i in range(ts.getImageStackSize())], np.float32)
+            self.tsVSSNR = TiltSeries(imgs, ts.tiltAngles)
+            self.recVSSNR = self._reconstruct(self.tsVSSNR)
         return self.ssnr
+
+    def getVSSNR(self):
+        return self.recVSSNR

@@ -107,7 +107,7 @@ class EngineAdapter:
             _abi.check(lib.tomo_load_series(hd, pix.ctypes.data, 0, _abi.ptr(eul, C.c_double),
                                             None if T is None else _abi.ptr(T, C.c_double), None))
             if req.kind == WBP:
-                _abi.check(lib.tomo_set_weighting(hd, req.weighting, 0.5, None))
+                _abi.check(lib.tomo_set_weighting(hd, req.weighting, 0.5, None, None))
             if req.kind == TVM:
                 th, gg, dt, it = req.tvm
                 _abi.check(lib.tomo_set_tvm(hd, th, gg, dt, it))
