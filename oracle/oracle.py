@@ -192,6 +192,21 @@ def weighting_mask(w, h, tilts, axes, diameter):
     return mask
 
 
+def ramp_mask(w, h, tilts_deg, hamming=False):
+    """The engine's ramp / Hamming-ramp WBP filters (not in the reference), as a 2-D mask
+    for weighting_apply: dtheta |k| / w per column frequency k (dtheta / (4 w) at k = 0),
+    times 0.54 + 0.46 cos(2 pi k / w) for Hamming, dtheta the mean tilt spacing in
+    radians; constant along the row frequency."""
+    t = np.asarray(tilts_deg, np.float64)
+    dth = (t.max() - t.min()) * (np.pi / 180.0) / (t.size - 1) if t.size > 1 else np.pi
+    i = np.arange(w)
+    ci = np.where(i > w / 2.0, i - w, i).astype(np.float64)
+    m = np.where(ci == 0, dth / (4.0 * w), dth * np.abs(ci) / w)
+    if hamming:
+        m = m * (0.54 + 0.46 * np.cos(2.0 * np.pi * ci / w))
+    return np.ascontiguousarray(np.broadcast_to(m.astype(np.float32), (h, w)))
+
+
 def weighting_apply(img, mask):
     out = np.array(img, np.float32, copy=True, order="C")
     h, w = out.shape

@@ -87,3 +87,21 @@ def test_two_rank_slabs_equal_single_rank(oracle_lib, tmp_path, update):
         ref_err.append(slabs.error_summary(per, order, c["W"], c["H"]))
     assert np.array_equal(got, ref)
     assert np.allclose(e0, np.array(ref_err), rtol=1e-12)
+
+
+def test_wbp_on_slabs_equals_full_wbp(oracle_lib):
+    # WBP backprojects measurements directly: the slab keeps its halo row's real values
+    # (a NaN halo would void the last row's bilinear reads)
+    from oracle import oracle as O
+    from tomoj_gb300 import slabs
+    c = series_case(W=32, H=9, D=20, n=7, seed=8, misalign=False, noise=0.0)
+    meas = np.array(c["series"], np.float32)
+    ref = np.zeros_like(c["vol"])
+    O.wbp(ref, c["g"], c["eul"], meas, None)
+    got = []
+    for sl in slabs.plan(c["W"], c["H"], c["D"], c["w"], c["h"], 3):
+        g = O.Geom(c["W"], sl.rows, c["D"], c["w"], sl.proj_rows, vc=sl.vol_center, pc=sl.proj_center)
+        v = np.zeros((c["D"], sl.rows, c["W"]), np.float32)
+        O.wbp(v, g, c["eul"], slabs.crop_series(meas, sl, halo_nan=False), None)
+        got.append(v[:, :sl.y1 - sl.y0, :])
+    assert np.array_equal(np.concatenate(got, axis=1), ref)

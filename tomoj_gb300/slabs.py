@@ -41,9 +41,7 @@ class Slab:
         return self.j1 - self.j0
 
 
-def plan(W: int, H: int, D: int, w: int, h: int, world: int, vol_center=None, proj_center=None) -> list[Slab]:
-    """Contiguous, balanced row slabs for `world` ranks (rank r gets slabs[r]).
-    Centres default to TomoJ's ((n - 1) / 2) convention."""
+def _centres(W, H, D, w, h, vol_center, proj_center):
     vc = tuple(vol_center) if vol_center is not None else ((W - 1) / 2.0, (H - 1) / 2.0, (D - 1) / 2.0)
     pc = tuple(proj_center) if proj_center is not None else ((w - 1.0) / 2, (h - 1.0) / 2, (w - 1) / 2.0,
                                                              (h - 1) / 2.0)
@@ -51,28 +49,45 @@ def plan(W: int, H: int, D: int, w: int, h: int, world: int, vol_center=None, pr
     off_bp = pc[3] - vc[1]
     if off_fp != off_bp or off_fp != int(off_fp):
         raise ValueError("slabs need equal, integral row offsets for projection and backprojection")
-    off = int(off_fp)
+    return vc, pc, int(off_fp)
+
+
+def slab(W: int, H: int, D: int, w: int, h: int, y0: int, y1: int, vol_center=None, proj_center=None) -> Slab:
+    """The slab of volume rows [y0, y1) (0 <= y0 <= y1 <= H): its halo, projection rows
+    and centres in slab coordinates."""
+    if not 0 <= y0 <= y1 <= H:
+        raise ValueError("slab rows out of range")
+    vc, pc, off = _centres(W, H, D, w, h, vol_center, proj_center)
+    halo = 1 if y1 < H else 0
+    j0 = min(max(y0 + off, 0), h)
+    j1 = min(max(y1 + halo + off, 0), h)
+    return Slab(y0, y1, halo, j0, j1, (vc[0], vc[1] - y0, vc[2]), (pc[0], pc[1] - j0, pc[2], pc[3] - j0))
+
+
+def plan(W: int, H: int, D: int, w: int, h: int, world: int, vol_center=None, proj_center=None) -> list[Slab]:
+    """Contiguous, balanced row slabs for `world` ranks (rank r gets slabs[r]).
+    Centres default to TomoJ's ((n - 1) / 2) convention."""
+    _centres(W, H, D, w, h, vol_center, proj_center)
     out = []
     base, extra = divmod(H, world)
     y = 0
     for r in range(world):
         n = base + (1 if r < extra else 0)
-        y0, y1 = y, y + n
-        y = y1
-        halo = 1 if y1 < H else 0
-        j0 = min(max(y0 + off, 0), h)
-        j1 = min(max(y1 + halo + off, 0), h)
-        cy = vc[1] - y0
-        out.append(Slab(y0, y1, halo, j0, j1, (vc[0], cy, vc[2]), (pc[0], pc[1] - j0, pc[2], pc[3] - j0)))
+        out.append(slab(W, H, D, w, h, y, y + n, vol_center, proj_center))
+        y += n
     return out
 
 
-def crop_series(series: np.ndarray, slab: Slab) -> np.ndarray:
-    """Rows [j0, j1) of every aligned projection (N, h, w) -> (N, j1 - j0, w).  The halo
-    row's measurements are NaN, so its pixels add nothing to the difference images or
-    to the residual (VoxelProjector3D.difference skips NaN measurements)."""
+def crop_series(series: np.ndarray, slab: Slab, halo_nan: bool = True) -> np.ndarray:
+    """Rows [j0, j1) of every aligned projection (N, h, w) -> (N, j1 - j0, w).  For the
+    iterative methods the halo row's measurements are NaN, so its pixels add nothing to
+    the difference images or to the residual (VoxelProjector3D.difference skips NaN
+    measurements).  For WBP, which backprojects the measurements themselves, pass
+    halo_nan=False: the backprojection's bilinear read of the slab's last row blends in
+    the halo row with weight 0 (ImageJ getInterpolatedValue), and a NaN there would
+    void the sample."""
     out = np.array(series[:, slab.j0:slab.j1, :], np.float32, copy=True, order="C")
-    if slab.halo and slab.j1 > slab.j0:
+    if halo_nan and slab.halo and slab.j1 > slab.j0:
         out[:, -1, :] = np.nan
     return out
 
