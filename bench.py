@@ -383,6 +383,11 @@ def run_engine(args, wl):
         "kernels": {k: {"avg_ms": v["avg_ms"], "launches": v["launches"],
                         "GBs": v["alg"] / (v["avg_ms"] / 1000.0) / 1e9,
                         "compulsory_GBs": v["comp"] / (v["avg_ms"] / 1000.0) / 1e9} for k, v in kernels.items()},
+        # the whole job under the plain-form accounting of a projector that streams the
+        # volume once per tilt: 12 B per voxel-update (4 B FP read + 8 B BP read-write);
+        # above 1 means the fused kernels move less than that per update
+        "job": {"bytes_per_update": 12, "achieved_GBs": value * 12.0 / 1e9 / world,
+                "frac_per_gpu": value * 12.0 / 1e9 / world / peak},
     }
 
     # ---- CPU baseline (rank 0, N=1 only) ----

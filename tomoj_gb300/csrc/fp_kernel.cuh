@@ -57,103 +57,152 @@ __host__ __device__ inline Smem layout(int ZC, int W, int tgmax, int rows = 1) {
     return L;
 }
 
-// Pairs of one plane row: slot k+2 holds the sample at floor(x) = k for k in [-2, W+1]
+// Pairs of a plane row: slot k+2 holds the sample at floor(x) = k for k in [-2, W+1]
 // as (v_k - d_k, d_k), d_k = v_{k+1} - v_k, so that a bilinear sample with fraction f is
 // fma(1 + f, d_k, v_k - d_k).  d = 0 where the reference returns the raw floor voxel
 // (last column, last row, last plane) and outside [0, W-1].
-__device__ __forceinline__ void build_pairs_row(const float* __restrict__ src, float2* __restrict__ dst, int W,
-                                                bool flat) {
-    const int tid = threadIdx.x;
-    if ((W & 3) == 0) {
-        for (int m = tid; m < W / 4; m += kThreads) {
-            const float4 v = *reinterpret_cast<const float4*>(src + 4 * m);
-            const float nx = (4 * m + 4 < W) ? src[4 * m + 4] : v.w;
-            float d0 = v.y - v.x, d1 = v.z - v.y, d2 = v.w - v.z, d3 = nx - v.w;
-            if (flat) d0 = d1 = d2 = d3 = 0.0f;
-            float4* o = reinterpret_cast<float4*>(dst + 4 * m + 2);
-            o[0] = make_float4(v.x - d0, d0, v.y - d1, d1);
-            o[1] = make_float4(v.z - d2, d2, v.w - d3, d3);
-        }
-    } else {
-        for (int k = tid; k < W; k += kThreads) {
-            const float v = src[k];
-            float d = (k + 1 < W) ? src[k + 1] - v : 0.0f;
-            if (flat) d = 0.0f;
-            dst[k + 2] = make_float2(v - d, d);
-        }
-    }
-    if (tid < 4) {
-        const int k = (tid < 2) ? tid - 2 : W + tid - 2;  // -2, -1, W, W+1
-        const float v = src[(tid < 2) ? 0 : W - 1];
-        dst[k + 2] = make_float2(v, 0.0f);
-    }
+//
+// A chunk's rows are converted together: the block is laid out as kThreads / q rows x
+// q groups (q groups per row), so a 512-wide row of 128 float4 groups keeps all 256
+// threads busy instead of half of them.
+
+// Group m of an FP32 row: pairs 4m .. 4m+3 (W % 4 == 0).
+__device__ __forceinline__ void pairs4_f32(const float* __restrict__ src, float2* __restrict__ dst, int W, int m,
+                                           bool flat) {
+    const float4 v = *reinterpret_cast<const float4*>(src + 4 * m);
+    const float nx = (4 * m + 4 < W) ? src[4 * m + 4] : v.w;
+    float d0 = v.y - v.x, d1 = v.z - v.y, d2 = v.w - v.z, d3 = nx - v.w;
+    if (flat) d0 = d1 = d2 = d3 = 0.0f;
+    float4* o = reinterpret_cast<float4*>(dst + 4 * m + 2);
+    o[0] = make_float4(v.x - d0, d0, v.y - d1, d1);
+    o[1] = make_float4(v.z - d2, d2, v.w - d3, d3);
 }
 
-// The same pairs from a row stored in 16 bits (reduced-precision volume; the slab
-// scale is applied to the finished ray sum).
+// Pair k of an FP32 row (any W).
+__device__ __forceinline__ void pair1_f32(const float* __restrict__ src, float2* __restrict__ dst, int W, int k,
+                                          bool flat) {
+    const float v = src[k];
+    float d = (k + 1 < W) ? src[k + 1] - v : 0.0f;
+    if (flat) d = 0.0f;
+    dst[k + 2] = make_float2(v - d, d);
+}
+
+// The same from a row stored in 16 bits (reduced-precision volume; the slab scale is
+// applied to the finished ray sum).
 template <int VT>
-__device__ __forceinline__ void build_pairs_row16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W,
-                                                  bool flat) {
-    const int tid = threadIdx.x;
-    if ((W & 3) == 0) {
-        for (int m = tid; m < W / 4; m += kThreads) {
-            const uint2 u = *reinterpret_cast<const uint2*>(src + 4 * m);
-            const float vx = vol_load16<VT>((uint16_t)(u.x & 0xFFFFu)), vy = vol_load16<VT>((uint16_t)(u.x >> 16));
-            const float vz = vol_load16<VT>((uint16_t)(u.y & 0xFFFFu)), vw = vol_load16<VT>((uint16_t)(u.y >> 16));
-            const float nx = (4 * m + 4 < W) ? vol_load16<VT>(src[4 * m + 4]) : vw;
-            float d0 = vy - vx, d1 = vz - vy, d2 = vw - vz, d3 = nx - vw;
-            if (flat) d0 = d1 = d2 = d3 = 0.0f;
-            float4* o = reinterpret_cast<float4*>(dst + 4 * m + 2);
-            o[0] = make_float4(vx - d0, d0, vy - d1, d1);
-            o[1] = make_float4(vz - d2, d2, vw - d3, d3);
-        }
-    } else {
-        for (int k = tid; k < W; k += kThreads) {
-            const float v = vol_load16<VT>(src[k]);
-            float d = (k + 1 < W) ? vol_load16<VT>(src[k + 1]) - v : 0.0f;
-            if (flat) d = 0.0f;
-            dst[k + 2] = make_float2(v - d, d);
-        }
+__device__ __forceinline__ void pairs4_16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W, int m,
+                                          bool flat) {
+    const uint2 u = *reinterpret_cast<const uint2*>(src + 4 * m);
+    const float vx = vol_load16<VT>((uint16_t)(u.x & 0xFFFFu)), vy = vol_load16<VT>((uint16_t)(u.x >> 16));
+    const float vz = vol_load16<VT>((uint16_t)(u.y & 0xFFFFu)), vw = vol_load16<VT>((uint16_t)(u.y >> 16));
+    const float nx = (4 * m + 4 < W) ? vol_load16<VT>(src[4 * m + 4]) : vw;
+    float d0 = vy - vx, d1 = vz - vy, d2 = vw - vz, d3 = nx - vw;
+    if (flat) d0 = d1 = d2 = d3 = 0.0f;
+    float4* o = reinterpret_cast<float4*>(dst + 4 * m + 2);
+    o[0] = make_float4(vx - d0, d0, vy - d1, d1);
+    o[1] = make_float4(vz - d2, d2, vw - d3, d3);
+}
+
+template <int VT>
+__device__ __forceinline__ void pair1_16(const uint16_t* __restrict__ src, float2* __restrict__ dst, int W, int k,
+                                         bool flat) {
+    const float v = vol_load16<VT>(src[k]);
+    float d = (k + 1 < W) ? vol_load16<VT>(src[k + 1]) - v : 0.0f;
+    if (flat) d = 0.0f;
+    dst[k + 2] = make_float2(v - d, d);
+}
+
+// Pair k of a row blended between volume rows r (src0) and r + 1 (src1) with weight
+// yf: b = v0 + yf (v1 - v0), then pairs of b.  The reference returns the raw voxel of
+// row r (unblended) at the last column, so that slot keeps v0; on the last plane
+// (`flat`) every sample is the raw voxel of row r.
+__device__ __forceinline__ void pair1_blend(const float* __restrict__ src0, const float* __restrict__ src1, float yf,
+                                            float2* __restrict__ dst, int W, int k, bool flat) {
+    const float v0 = src0[k];
+    float2 pr = make_float2(v0, 0.0f);
+    if (!flat && k + 1 < W) {
+        const float b = __fadd_rn(v0, __fmul_rn(yf, __fsub_rn(src1[k], v0)));
+        const float v0n = src0[k + 1];
+        const float bn = __fadd_rn(v0n, __fmul_rn(yf, __fsub_rn(src1[k + 1], v0n)));
+        const float d = __fsub_rn(bn, b);
+        pr = make_float2(__fsub_rn(b, d), d);
     }
-    if (tid < 4) {
-        const int k = (tid < 2) ? tid - 2 : W + tid - 2;  // -2, -1, W, W+1
-        const float v = vol_load16<VT>(src[(tid < 2) ? 0 : W - 1]);
-        dst[k + 2] = make_float2(v, 0.0f);
+    dst[k + 2] = pr;
+}
+
+// Calls fn(zz, m) for every row zz < zc and group m < q, spreading rows over the block.
+template <class Fn>
+__device__ __forceinline__ void for_chunk_groups(int zc, int q, Fn fn) {
+    const int tid = threadIdx.x;
+    if (q <= kThreads) {
+        const int R = kThreads / q;
+        const int r0 = tid / q, m = tid - r0 * q;
+        if (r0 < R)
+            for (int zz = r0; zz < zc; zz += R) fn(zz, m);
+    } else {
+        for (int zz = 0; zz < zc; zz++)
+            for (int m = tid; m < q; m += kThreads) fn(zz, m);
     }
 }
 
-// Pairs of a plane row blended between volume rows r (src0) and r + 1 (src1) with
-// weight yf: b = v0 + yf (v1 - v0), then pairs of b as above.  The reference returns
-// the raw voxel of row r (unblended) at the last column, so that slot keeps v0; on
-// the last plane (`flat`) every sample is the raw voxel of row r.
-__device__ __forceinline__ void build_pairs_row_blend(const float* __restrict__ src0, const float* __restrict__ src1,
-                                                      float yf, float2* __restrict__ dst, int W, bool flat) {
-    const int tid = threadIdx.x;
-    if (flat) {
-        for (int k = tid; k < W; k += kThreads) dst[k + 2] = make_float2(src0[k], 0.0f);
+// All pairs of a staged chunk of zc plane rows.  raw: rows [zc][W] as stored (FP32 or
+// 16-bit), raw1: row r + 1 of every plane (blended form); zflat: the chunk row of the
+// volume's last plane, or -1.
+__device__ __forceinline__ void build_pairs_chunk(const void* raw, const float* raw1, float2* __restrict__ pairs, int W,
+                                                  int PW, int zc, int vt, bool blend, float yf, bool last_row,
+                                                  int zflat) {
+    const float* r32 = static_cast<const float*>(raw);
+    const uint16_t* r16 = static_cast<const uint16_t*>(raw);
+    auto flat = [&](int zz) { return last_row || zz == zflat; };
+    if (blend) {
+        for_chunk_groups(zc, W, [&](int zz, int k) {
+            pair1_blend(r32 + (size_t)zz * W, raw1 + (size_t)zz * W, yf, pairs + (size_t)zz * PW, W, k, flat(zz));
+        });
+    } else if (vt == kVolF32) {
+        if ((W & 3) == 0)
+            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+                pairs4_f32(r32 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
+            });
+        else
+            for_chunk_groups(zc, W, [&](int zz, int k) {
+                pair1_f32(r32 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
+            });
+    } else if (vt == kVolBF16) {
+        if ((W & 3) == 0)
+            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+                pairs4_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
+            });
+        else
+            for_chunk_groups(zc, W, [&](int zz, int k) {
+                pair1_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
+            });
     } else {
-        for (int k = tid; k < W; k += kThreads) {
-            const float v0 = src0[k];
-            const float b = __fadd_rn(v0, __fmul_rn(yf, __fsub_rn(src1[k], v0)));
-            float2 pr;
-            if (k + 1 < W) {
-                const float v0n = src0[k + 1];
-                const float bn = __fadd_rn(v0n, __fmul_rn(yf, __fsub_rn(src1[k + 1], v0n)));
-                const float d = __fsub_rn(bn, b);
-                pr = make_float2(__fsub_rn(b, d), d);
-            } else {
-                pr = make_float2(v0, 0.0f);  // last column: the raw voxel of row r
-            }
-            dst[k + 2] = pr;
-        }
+        if ((W & 3) == 0)
+            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+                pairs4_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
+            });
+        else
+            for_chunk_groups(zc, W, [&](int zz, int k) {
+                pair1_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
+            });
     }
-    if (tid < 4) {
-        // x in [-ACCURACY, 0) samples column 0 with weight 0 (the blended value);
-        // slots past the row are never sampled (x < W)
-        const float v0 = src0[0];
-        const float b0 = flat ? v0 : __fadd_rn(v0, __fmul_rn(yf, __fsub_rn(src1[0], v0)));
-        const int k = (tid < 2) ? tid - 2 : W + tid - 2;  // -2, -1, W, W+1
-        dst[k + 2] = make_float2(tid < 2 ? b0 : src0[W - 1], 0.0f);
+    // slots -2, -1, W, W+1 of every row: the edge values with slope 0.  In the blended
+    // form x in [-ACCURACY, 0) samples column 0 with weight 0 (the blended value) and
+    // slots past the row are never sampled (x < W).
+    for (int e = threadIdx.x; e < zc * 4; e += kThreads) {
+        const int zz = e >> 2, t = e & 3;
+        const int col = (t < 2) ? 0 : W - 1;
+        const size_t o = (size_t)zz * W + col;
+        float v;
+        if (vt == kVolF32)
+            v = r32[o];
+        else if (vt == kVolBF16)
+            v = vol_load16<kVolBF16>(r16[o]);
+        else
+            v = vol_load16<kVolF16>(r16[o]);
+        if (blend && t < 2 && !flat(zz)) v = __fadd_rn(v, __fmul_rn(yf, __fsub_rn(raw1[o], v)));
+        const int k = (t < 2) ? t - 2 : W + t - 2;  // -2, -1, W, W+1
+        pairs[(size_t)zz * PW + k + 2] = make_float2(v, 0.0f);
     }
 }
 
@@ -328,24 +377,11 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             } else {
                 __syncthreads();
             }
-            for (int zz = 0; zz < zc; zz++) {
-                const bool flat = last_row || (z0 + zz == D - 1);  // raw floor voxel on the last row / plane
-                if (BLEND && blend)
-                    build_pairs_row_blend(raw + (size_t)zz * W, raw1 + (size_t)zz * W, yf, pairs + (size_t)zz * PW, W,
-                                          flat);
-                else if (vt == kVolF32)
-                    build_pairs_row(raw + (size_t)zz * W, pairs + (size_t)zz * PW, W, flat);
-                else if (vt == kVolBF16)
-                    build_pairs_row16<kVolBF16>(reinterpret_cast<const uint16_t*>(raw) + (size_t)zz * W,
-                                                pairs + (size_t)zz * PW, W, flat);
-                else
-                    build_pairs_row16<kVolF16>(reinterpret_cast<const uint16_t*>(raw) + (size_t)zz * W,
-                                               pairs + (size_t)zz * PW, W, flat);
-            }
+            build_pairs_chunk(raw, raw1, pairs, W, PW, zc, vt, BLEND && blend, yf, last_row,
+                              D - 1 - z0 < zc ? D - 1 - z0 : -1);
             __syncthreads();
             if (c + 1 < c_end && use_tma) stage(c + 1);
             const float2* P = pairs + 2;
-#pragma unroll
 #pragma unroll
             for (int k = 0; k < NR; k++) {
                 if (k / QP >= TG) break;  // uniform: tilt slot past the batch
