@@ -27,6 +27,11 @@ namespace {
 #define TOMO_BP_MIN_BLOCKS 3
 #endif
 constexpr int kBpThreads = 256;
+#ifndef TOMO_BP_NC
+#define TOMO_BP_NC 1
+#endif
+constexpr int kNC = TOMO_BP_NC;                  // columns per thread
+constexpr int kBpCtaThreads = kBpThreads / kNC;  // threads per CTA
 constexpr int kTX = 64;
 constexpr int kTZ = 64;
 constexpr int kKZ = 16;      // voxels per thread along z
@@ -95,14 +100,18 @@ __device__ __forceinline__ void bp_acc(float& vox, float& comp, float val) {
         bp_add_kahan<SANITIZE, POS>(vox, comp, val);
 }
 
-// One CTA's work: tile (x0, z0) of volume row r of problem `a`.
+// One CTA's work: tile (x0, z0) of volume row r of problem `a`.  The CTA has
+// kBpThreads / kNC threads; thread (tx, tzg) owns the 16 voxels z = z0 + 16*tzg + k of
+// the kNC columns x0 + tx + c * kCX (kCX = kTX / kNC), so the per-tilt position setup
+// and interval test are shared by kNC * 16 voxel-updates.
 template <bool SANITIZE, bool POS, int VT, int SEG>
 __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const int z0, const int r) {
     constexpr int kTC = BpSeg<SEG>::kTC, kSeg = BpSeg<SEG>::kSeg, kRawSeg = BpSeg<SEG>::kRawSeg;
+    constexpr int kThr = kBpCtaThreads, kCX = kTX / kNC;
     __shared__ __align__(16) BpShared<SEG> sh;
     const int tid = threadIdx.x;
-    const int tx = tid & (kTX - 1);
-    const int tzg = tid >> 6;
+    const int tx = tid % kCX;
+    const int tzg = tid / kCX;
     const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
     const int jp = a.bprow ? a.bprow[r] : r + a.row_off;  // projection row seen by this volume row
     if (jp < 0 || jp >= h) return;  // no tilt reaches this row (yy outside [0,h))
@@ -110,26 +119,29 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
     // weight along y); at jp = h - 1 ImageJ blends the row with itself
     const float byf = a.bpyf ? a.bpyf[r] : 0.0f;
     const bool blend = byf != 0.0f && jp < h - 1;
-    const int x = x0 + tx;
     const int zs = z0 + tzg * kKZ;
-    const bool xin = x < W;
 
     const size_t plane = (size_t)H * W;
-    const size_t v0 = ((size_t)zs * H + r) * W + x;  // voxel (x, r, zs); voxel k is at v0 + k * plane
-    const int nk = xin ? min(kKZ, D - zs) : 0;
-    float vox[kKZ], comp[kKZ];
     const float vsc = (VT == kVolF32) ? 1.0f : a.vscale[r];
-    if (VT == kVolF32) {
-        const float* vb = static_cast<const float*>(a.vol) + v0;
+    float vox[kNC][kKZ], comp[kNC][kKZ];
+    int nk[kNC];
 #pragma unroll
-        for (int k = 0; k < kKZ; k++) vox[k] = (k < nk) ? vb[k * plane] : 0.0f;
-    } else {
-        const uint16_t* vb = static_cast<const uint16_t*>(a.vol) + v0;
+    for (int c = 0; c < kNC; c++) {
+        const int x = x0 + tx + c * kCX;
+        nk[c] = (x < W) ? min(kKZ, D - zs) : 0;
+        const size_t v0 = ((size_t)zs * H + r) * W + x;  // voxel (x, r, zs); voxel k is at v0 + k * plane
+        if (VT == kVolF32) {
+            const float* vb = static_cast<const float*>(a.vol) + v0;
 #pragma unroll
-        for (int k = 0; k < kKZ; k++) vox[k] = (k < nk) ? vol_load16<VT>(vb[k * plane]) * vsc : 0.0f;
+            for (int k = 0; k < kKZ; k++) vox[c][k] = (k < nk[c]) ? vb[k * plane] : 0.0f;
+        } else {
+            const uint16_t* vb = static_cast<const uint16_t*>(a.vol) + v0;
+#pragma unroll
+            for (int k = 0; k < kKZ; k++) vox[c][k] = (k < nk[c]) ? vol_load16<VT>(vb[k * plane]) * vsc : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < kKZ; k++) comp[c][k] = 0.0f;
     }
-#pragma unroll
-    for (int k = 0; k < kKZ; k++) comp[k] = 0.0f;
 
     const int xa = x0, xb = min(x0 + kTX - 1, W - 1);
     const int za = z0, zb = min(z0 + kTZ - 1, D - 1);
@@ -153,14 +165,16 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
             sh.seg_start[tid] = s;
             sh.raw_start[tid] = s & ~3;
         }
-        for (int t = tid >> 6; t < tc; t += kBpThreads / kTX) {
-            const int xc = x0 + tx;
-            sh.zint[t][tx] = (xc < W) ? a.zint[(size_t)a.tilts[c0 + t] * W + xc] : 0;
-        }
+        for (int t = tzg; t < tc; t += kThr / kCX)
+#pragma unroll
+            for (int c = 0; c < kNC; c++) {
+                const int xc = x0 + tx + c * kCX;
+                sh.zint[t][tx + c * kCX] = (xc < W) ? a.zint[(size_t)a.tilts[c0 + t] * W + xc] : 0;
+            }
         __syncthreads();
         // --- stage image segments: 128-bit loads of the row, then (value, slope) pairs --
         // one warp per tilt, each lane loading 4 floats at a time
-        for (int t = tid >> 5; t < tc; t += kBpThreads / 32)
+        for (int t = tid >> 5; t < tc; t += kThr / 32)
           for (int v = tid & 31; v < kRawSeg / 4; v += 32) {
             const float* row = a.img + ((size_t)(c0 + t) * h + jp) * w;
             const int k0 = sh.raw_start[t] + 4 * v;
@@ -187,7 +201,7 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
             *reinterpret_cast<float4*>(&sh.raw[t][4 * v]) = q;
         }
         __syncthreads();
-        for (int e = tid; e < tc * kSeg; e += kBpThreads) {
+        for (int e = tid; e < tc * kSeg; e += kThr) {
             const int t = e / kSeg, m = e - t * kSeg;
             const int k = sh.seg_start[t] + m;       // image column of this pair
             const int o = k - sh.raw_start[t];        // offset in the staged floats
@@ -219,85 +233,95 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
         for (int t = 0; t < tc; t++) {
             // the tilt's segment base rides in the high word, so (X >> 32) is the flat pair index
             const long long base = (long long)(t * kSeg - sh.seg_start[t]) << 32;
-            long long X = sh.K[t] + (long long)x * sh.C[t] + (long long)zs * sh.S[t] + base;
             const long long S = sh.S[t];
-            const int zi = sh.zint[t][tx];
-            const int kl = (zi & 0xFFFF) - zs;
-            const int cnt = (int)((uint32_t)zi >> 16);
-            const bool full = xin && kl <= 0 && kl + cnt >= kKZ;
-            if (__all_sync(0xffffffffu, full)) {
-                // two independent position chains (even / odd z)
-                long long X1 = X + S;
-                const long long S2 = 2 * S;
+            const long long Xc0 = sh.K[t] + (long long)(x0 + tx) * sh.C[t] + (long long)zs * sh.S[t] + base;
 #pragma unroll
-                for (int k = 0; k < kKZ; k += 2) {
-                    const float2 p0 = sh.seg[(int)(X >> 32)];
-                    const float2 p1 = sh.seg[(int)(X1 >> 32)];
-                    bp_acc<SANITIZE, POS, VT>(vox[k], comp[k], fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x));
-                    bp_acc<SANITIZE, POS, VT>(vox[k + 1], comp[k + 1],
-                                              fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x));
-                    X += S2;
-                    X1 += S2;
-                }
-            } else {
+            for (int c = 0; c < kNC; c++) {
+                long long X = Xc0 + (long long)(c * kCX) * sh.C[t];
+                const int zi = sh.zint[t][tx + c * kCX];
+                const int kl = (zi & 0xFFFF) - zs;
+                const int cnt = (int)((uint32_t)zi >> 16);
+                const bool full = nk[c] > 0 && kl <= 0 && kl + cnt >= kKZ;
+                if (__all_sync(0xffffffffu, full)) {
+                    // two independent position chains (even / odd z)
+                    long long X1 = X + S;
+                    const long long S2 = 2 * S;
 #pragma unroll
-                for (int k = 0; k < kKZ; k++) {
-                    if ((unsigned)(k - kl) < (unsigned)cnt) {
-                        const float2 p = sh.seg[(int)(X >> 32)];
-                        bp_acc<SANITIZE, POS, VT>(vox[k], comp[k], fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x));
+                    for (int k = 0; k < kKZ; k += 2) {
+                        const float2 p0 = sh.seg[(int)(X >> 32)];
+                        const float2 p1 = sh.seg[(int)(X1 >> 32)];
+                        bp_acc<SANITIZE, POS, VT>(vox[c][k], comp[c][k],
+                                                  fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x));
+                        bp_acc<SANITIZE, POS, VT>(vox[c][k + 1], comp[c][k + 1],
+                                                  fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x));
+                        X += S2;
+                        X1 += S2;
                     }
-                    X += S;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kKZ; k++) {
+                        if ((unsigned)(k - kl) < (unsigned)cnt) {
+                            const float2 p = sh.seg[(int)(X >> 32)];
+                            bp_acc<SANITIZE, POS, VT>(vox[c][k], comp[c][k],
+                                                      fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x));
+                        }
+                        X += S;
+                    }
                 }
             }
         }
         __syncthreads();
     }
 
-    if (VT == kVolF32) {
-        float* vb = static_cast<float*>(a.vol) + v0;
 #pragma unroll
-        for (int k = 0; k < kKZ; k++)
-            if (k < nk) vb[k * plane] = vox[k];
-    } else {
-        // store value / scale (exact: power of two) and feed the row maximum for re-scaling
-        uint16_t* vb = static_cast<uint16_t*>(a.vol) + v0;
-        const float inv = 1.0f / vsc;
-        float m = 0.0f;
-        bool range = false;
+    for (int c = 0; c < kNC; c++) {
+        const size_t v0 = ((size_t)zs * H + r) * W + x0 + tx + c * kCX;
+        if (VT == kVolF32) {
+            float* vb = static_cast<float*>(a.vol) + v0;
 #pragma unroll
-        for (int k = 0; k < kKZ; k++) {
-            if (k < nk) {
-                const float v = vox[k] - comp[k];
-                m = fmaxf(m, fabsf(v));
-                float q = v * inv;
-                if (VT == kVolF16 && fabsf(q) > kF16Max && isfinite(q)) {
-                    range = true;  // reported through the status word; the slab saturates
-                    q = copysignf(kF16Max, q);
+            for (int k = 0; k < kKZ; k++)
+                if (k < nk[c]) vb[k * plane] = vox[c][k];
+        } else {
+            // store value / scale (exact: power of two) and feed the row maximum for re-scaling
+            uint16_t* vb = static_cast<uint16_t*>(a.vol) + v0;
+            const float inv = 1.0f / vsc;
+            float m = 0.0f;
+            bool range = false;
+#pragma unroll
+            for (int k = 0; k < kKZ; k++) {
+                if (k < nk[c]) {
+                    const float v = vox[c][k] - comp[c][k];
+                    m = fmaxf(m, fabsf(v));
+                    float q = v * inv;
+                    if (VT == kVolF16 && fabsf(q) > kF16Max && isfinite(q)) {
+                        range = true;  // reported through the status word; the slab saturates
+                        q = copysignf(kF16Max, q);
+                    }
+                    vb[k * plane] = vol_store16<VT>(q);
                 }
-                vb[k * plane] = vol_store16<VT>(q);
             }
-        }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((tid & 31) == 0 && m > 0.0f) atomicMax(a.vmax + r, __float_as_uint(m));
-        if (range) atomicOr(a.status, (int)kStatusRange);
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((tid & 31) == 0 && m > 0.0f) atomicMax(a.vmax + r, __float_as_uint(m));
+            if (range) atomicOr(a.status, (int)kStatusRange);
+        }
     }
 }
 
 // Reduced storage carries a compensation register per voxel: two CTAs per SM.
 template <int VT>
 struct BpOcc {
-    static constexpr int value = VT == kVolF32 ? TOMO_BP_MIN_BLOCKS : 2;
+    static constexpr int value = kNC == 1 ? (VT == kVolF32 ? TOMO_BP_MIN_BLOCKS : 2) : (VT == kVolF32 ? 4 : 3);
 };
 
 template <bool SANITIZE, bool POS, int VT, int SEG>
-__global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value) bp_separable_kernel(const __grid_constant__ BpLaunch a) {
+__global__ void __launch_bounds__(kBpCtaThreads, BpOcc<VT>::value) bp_separable_kernel(const __grid_constant__ BpLaunch a) {
     bp_body<SANITIZE, POS, VT, SEG>(a, blockIdx.x * kTX, blockIdx.y * kTZ, a.y0 + blockIdx.z);
 }
 
 // Batched form: CTA b works on item {problem, x tile, z tile, row} of many problems.
 template <bool SANITIZE, bool POS, int VT>
-__global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value)
+__global__ void __launch_bounds__(kBpCtaThreads, BpOcc<VT>::value)
     bp_kernel_batch(const BpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
     bp_body<SANITIZE, POS, VT, 96>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
@@ -306,22 +330,22 @@ __global__ void __launch_bounds__(kBpThreads, BpOcc<VT>::value)
 template <int VT>
 void bp_batch_vt(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n, cudaStream_t s) {
     if (sanitize) {
-        if (positivity) bp_kernel_batch<true, true, VT><<<n, kBpThreads, 0, s>>>(descs, items);
-        else bp_kernel_batch<true, false, VT><<<n, kBpThreads, 0, s>>>(descs, items);
+        if (positivity) bp_kernel_batch<true, true, VT><<<n, kBpCtaThreads, 0, s>>>(descs, items);
+        else bp_kernel_batch<true, false, VT><<<n, kBpCtaThreads, 0, s>>>(descs, items);
     } else {
-        if (positivity) bp_kernel_batch<false, true, VT><<<n, kBpThreads, 0, s>>>(descs, items);
-        else bp_kernel_batch<false, false, VT><<<n, kBpThreads, 0, s>>>(descs, items);
+        if (positivity) bp_kernel_batch<false, true, VT><<<n, kBpCtaThreads, 0, s>>>(descs, items);
+        else bp_kernel_batch<false, false, VT><<<n, kBpCtaThreads, 0, s>>>(descs, items);
     }
 }
 
 template <int VT, int SEG>
 void bp_separable_vt(const BpLaunch& a, dim3 grid, cudaStream_t s) {
     if (a.sanitize) {
-        if (a.positivity) bp_separable_kernel<true, true, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
-        else bp_separable_kernel<true, false, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
+        if (a.positivity) bp_separable_kernel<true, true, VT, SEG><<<grid, kBpCtaThreads, 0, s>>>(a);
+        else bp_separable_kernel<true, false, VT, SEG><<<grid, kBpCtaThreads, 0, s>>>(a);
     } else {
-        if (a.positivity) bp_separable_kernel<false, true, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
-        else bp_separable_kernel<false, false, VT, SEG><<<grid, kBpThreads, 0, s>>>(a);
+        if (a.positivity) bp_separable_kernel<false, true, VT, SEG><<<grid, kBpCtaThreads, 0, s>>>(a);
+        else bp_separable_kernel<false, false, VT, SEG><<<grid, kBpCtaThreads, 0, s>>>(a);
     }
 }
 
