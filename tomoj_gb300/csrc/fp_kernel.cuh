@@ -382,9 +382,8 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             __syncthreads();
             if (c + 1 < c_end && use_tma) stage(c + 1);
             const float2* P = pairs + 2;
-#pragma unroll
-            for (int k = 0; k < NR; k++) {
-                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
+            // ray slot k over this chunk: full (unrolled chains), none (skip) or partial
+            auto one = [&](int k) {
                 const long long st = s_step[k / QP];
                 const int za = zab[k] & 0xFFFF;
                 const int cnt = (int)((uint32_t)zab[k] >> 16);
@@ -406,26 +405,15 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 } else if (__all_sync(0xffffffffu, none)) {
                     X[k] += (long long)zc * st;
                 } else {
-#ifdef TOMO_FP_PARTIAL_INLINE
-                    const int lo = za - z0;
-                    long long x = X[k];
-                    float s = 0.0f;
-#pragma unroll 4
-                    for (int zz = 0; zz < zc; zz++) {
-                        const bool in = (unsigned)(zz - lo) < (unsigned)cnt;
-                        float2 p = make_float2(0.0f, 0.0f);
-                        if (in) p = P[(int)(x >> 32)];
-                        s += fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
-                        x += st + pitch;
-                    }
-                    X[k] = x - (long long)zc * pitch;
-                    acc[k] += s;
-#else
                     const PartialOut po = partial_chunk(P, X[k], st + pitch, za - z0, cnt, zc);
                     X[k] = po.x - (long long)zc * pitch;
                     acc[k] += po.s;
-#endif
                 }
+            };
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                if (k / QP >= TG) break;  // uniform: tilt slot past the batch
+                one(k);
             }
             __syncthreads();
             if (c + 1 < c_end && !use_tma) stage(c + 1);
