@@ -124,6 +124,12 @@ tomo_status tomo_get_volume(tomo_projector* p, float* dst, int32_t on_device, in
 tomo_status tomo_fill_volume(tomo_projector* p, float value);
 /* Device pointer of the resident volume [D][H][W] (valid until tomo_destroy). */
 tomo_status tomo_volume_device_ptr(tomo_projector* p, float** out);
+/* Two projectors on one TomoReconstruction2 (the dual-axis drivers ADASIRT / ADOSSART,
+ * TomoReconstruction2.java:880-1100, build projector1 and projector2 on the same rec):
+ * p works in place on owner's volume (same W, H, D; FP32 storage) and on owner's
+ * stream, so their calls run in order; p's own volume is released.  owner must stay
+ * alive while shared.  owner == NULL gives p a private copy of the volume it sees. */
+tomo_status tomo_share_volume(tomo_projector* p, tomo_projector* owner);
 
 /* ---- Projector surface (Projector.java:130-156) ------------------------- */
 tomo_status tomo_add_projection(tomo_projector* p, int32_t index);          /* addProjection(int) */

@@ -278,6 +278,47 @@ def wbp(vol, g: Geom, eulers, meas, mask=None, y0=0, y1=None):
     return vol
 
 
+def ossart_iteration_dual(vol, g1: Geom, eul1, meas1, order1, g2: Geom, eul2, meas2, order2, relax, update):
+    """TomoReconstruction2.osartIterationDual (TomoReconstruction2.java:1282-1428) on one
+    volume: for t = 0, 2, ... while t < n1 - 1, series 1 then series 2 add two projections
+    each (each inner loop stops when t + 1 reaches its series' length); one counter
+    shared by both series triggers, at `update` or at a series' last index, the
+    projection + difference of that series' pending projections and their
+    backprojection (update_step).  `update` is used as given (0 gives factor = inf).
+    Returns err5 over (n1 + n2) projections."""
+    n1, n2 = len(order1), len(order2)
+    factor = float(np.float32(relax / update)) if update else float(np.float32(np.inf))
+    st = {"diff": 0, "som": 0.0, "min": float(np.finfo(np.float32).max), "max": 0.0, "imin": 0, "imax": 0}
+    pend = {1: [], 2: []}
+
+    def add(which, g, eul, meas, order, n, t, i):
+        pend[which].append(int(order[t + i]))
+        st["diff"] += 1
+        if st["diff"] == update or t + i == n - 1:
+            errs = update_step(vol, g, eul, meas, pend[which], factor)
+            for e, v in enumerate(errs):
+                st["som"] += v
+                if v > st["max"]:
+                    st["max"], st["imax"] = v, int(order[t + i - len(errs) + e + 1])
+                elif v < st["min"]:
+                    st["min"], st["imin"] = v, int(order[t + i - len(errs) + e + 1])
+            pend[which] = []
+            st["diff"] = 0
+
+    for t in range(0, n1 - 1, 2):
+        for i in range(2):
+            if t + 1 >= n1:
+                break
+            add(1, g1, eul1, meas1, order1, n1, t, i)
+        for i in range(2):
+            if t + 1 >= n2:
+                break
+            add(2, g2, eul2, meas2, order2, n2, t, i)
+    wh = g1.W * g1.H
+    return np.array([np.sqrt(st["som"] / ((n1 + n2) * wh)), np.sqrt(st["min"] / wh), st["imin"],
+                     np.sqrt(st["max"] / wh), st["imax"]])
+
+
 def fista_step(rec, prev, t):
     _vol(rec)
     _vol(prev)

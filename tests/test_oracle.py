@@ -273,3 +273,21 @@ def test_bgart_collapse_snaps_background_side_to_the_mode(oracle_lib):
     O.bgart_collapse(vol2, k, False)
     expect2 = np.where(v.astype(np.float64) > mode - k * sigma, np.float32(mode), v).reshape(vol.shape)
     assert np.array_equal(vol2, expect2)
+
+
+def test_dual_iteration_flushes_like_the_reference(oracle_lib, monkeypatch):
+    # osartIterationDual with n1 = 5, n2 = 4, update = 3: two projections of each series
+    # in turn, one shared counter; series 1's last projection is never reached (t < n1 - 1)
+    flushed = []
+
+    def record(vol, g, eul, meas, batch, factor, y0=0, y1=None):
+        flushed.append((g.tag, list(batch)))
+        return np.zeros(len(batch))
+
+    monkeypatch.setattr(O, "update_step", record)
+    g1, g2 = O.Geom(4, 2, 4, 4, 2), O.Geom(4, 2, 4, 4, 2)
+    g1.tag, g2.tag = 1, 2
+    o1, o2 = [10, 11, 12, 13, 14], [20, 21, 22, 23]
+    vol = np.zeros((4, 2, 4), np.float32)
+    O.ossart_iteration_dual(vol, g1, None, None, o1, g2, None, None, o2, 1.0, 3)
+    assert flushed == [(2, [20]), (1, [10, 11, 12, 13]), (2, [21, 22, 23])]

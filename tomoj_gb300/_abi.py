@@ -78,6 +78,7 @@ SIGNATURES = {
     "tomo_get_volume": (C.c_int32, [_P, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "tomo_fill_volume": (C.c_int32, [_P, C.c_float]),
     "tomo_volume_device_ptr": (C.c_int32, [_P, C.POINTER(C.c_void_p)]),
+    "tomo_share_volume": (C.c_int32, [_P, _P]),
     "tomo_add_projection": (C.c_int32, [_P, C.c_int32]),
     "tomo_clear_projections": (C.c_int32, [_P]),
     "tomo_project": (C.c_int32, [_P, C.c_int32, C.c_int32]),

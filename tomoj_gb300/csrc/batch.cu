@@ -118,6 +118,8 @@ tomo_status build_plan(tomo_batch* b) {
         if (!g.separable || g.fractional || p->bp_wide || p->bp_generic)
             return handle_fail(TOMO_ERR_UNSUPPORTED,
                                "batched iterations need a vertical tilt axis, scale 1 and whole-row centre offsets");
+        if (p->vol_owner)
+            return handle_fail(TOMO_ERR_UNSUPPORTED, "a handle sharing another handle's volume cannot join a batch");
         const int N = g.N, upd = b->upd[m];
         const int nsub = (N + upd - 1) / upd;
         b->max_nsub = std::max(b->max_nsub, nsub);
@@ -183,7 +185,7 @@ tomo_status build_plan(tomo_batch* b) {
             c.h = g.h;
             c.row_off = g.bp_row_off;
             c.positivity = p->params.positivity;
-            c.sanitize = p->meas_has_inf || p->vol_nonfinite;
+            c.sanitize = p->meas_has_inf || p->vol_flag();
             c.status = p->d_status;
             const int bi = (int)bp.size();
             bp.push_back(c);

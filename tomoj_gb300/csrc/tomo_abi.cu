@@ -376,7 +376,7 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     a.h = g.h;
     a.row_off = g.bp_row_off;
     a.positivity = p->params.positivity;
-    a.sanitize = sanitize || p->vol_nonfinite;
+    a.sanitize = sanitize || p->vol_flag();
     a.status = p->d_status;
     if (to_dist) {
         CK(launch_bp_separable(a, p->stream));
@@ -575,6 +575,31 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
 tomo_status tomo_destroy(tomo_projector* p) {
     if (!p) return TOMO_OK;
     if (p->stream) cudaStreamSynchronize(p->stream);
+    // handles sharing this volume keep it: the allocation passes to the first of them,
+    // which becomes the owner of the others; a sharer leaves its owner
+    if (!p->vol_sharers.empty()) {
+        tomo_projector* q0 = p->vol_sharers.front();
+        for (void*& a : p->allocs)
+            if (a == static_cast<void*>(p->d_vol)) a = nullptr;
+        q0->allocs.push_back(p->d_vol);
+        p->bytes -= sizeof(float) * p->nvox;
+        q0->bytes += sizeof(float) * p->nvox;
+        q0->vol_owner = nullptr;
+        q0->stream = q0->own_stream;
+        q0->vol_nonfinite = p->vol_nonfinite;
+        for (tomo_projector* q : p->vol_sharers) {
+            if (q == q0) continue;
+            q->vol_owner = q0;
+            q->stream = q0->stream;
+            q0->vol_sharers.push_back(q);
+        }
+        p->vol_sharers.clear();
+        p->d_vol = nullptr;
+    }
+    if (p->vol_owner) {
+        auto& v = p->vol_owner->vol_sharers;
+        v.erase(std::remove(v.begin(), v.end(), p), v.end());
+    }
     for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
     for (void* a : p->allocs) cudaFree(a);
     g_in_use -= p->bytes;
@@ -805,7 +830,7 @@ tomo_status tomo_set_volume(tomo_projector* p, const float* src, int32_t on_devi
     CK(launch_scan_nonfinite_vol(p->vol(), p->vtype, p->nvox, p->d_flags, p->stream));
     CK(cudaMemcpyAsync(&flags, p->d_flags, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaStreamSynchronize(p->stream));
-    p->vol_nonfinite = flags != 0;
+    p->vol_flag() = flags != 0;
     return TOMO_OK;
 }
 
@@ -821,7 +846,7 @@ tomo_status tomo_fill_volume(tomo_projector* p, float value) {
     else
         CK(launch_vol_fill(p->vol(), p->vtype, p->d_vscale, p->nvox, p->g.H, value, p->stream));
     CK(cudaStreamSynchronize(p->stream));
-    p->vol_nonfinite = !std::isfinite(value);
+    p->vol_flag() = !std::isfinite(value);
     return TOMO_OK;
 }
 
@@ -830,6 +855,40 @@ tomo_status tomo_volume_device_ptr(tomo_projector* p, float** out) {
     if (p->vtype != kVolF32)
         return fail(TOMO_ERR_UNSUPPORTED, "the volume is stored in 16 bits with slab scales; use tomo_get_volume");
     *out = p->d_vol;
+    return TOMO_OK;
+}
+
+tomo_status tomo_share_volume(tomo_projector* p, tomo_projector* owner) {
+    if (!p || p == owner) return fail(TOMO_ERR_INVALID, "null or self handle");
+    if (p->vtype != kVolF32 || (owner && owner->vtype != kVolF32))
+        return fail(TOMO_ERR_UNSUPPORTED, "volume sharing needs FP32 storage");
+    if (!owner) {
+        if (!p->vol_owner) return TOMO_OK;  // already private
+        float* mine = nullptr;
+        CKS(alloc_n(p, &mine, p->nvox));
+        CK(cudaMemcpyAsync(mine, p->d_vol, sizeof(float) * p->nvox, cudaMemcpyDeviceToDevice, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        p->vol_nonfinite = p->vol_flag();
+        auto& v = p->vol_owner->vol_sharers;
+        v.erase(std::remove(v.begin(), v.end(), p), v.end());
+        p->d_vol = mine;
+        p->vol_owner = nullptr;
+        p->stream = p->own_stream;
+        return TOMO_OK;
+    }
+    if (owner->vol_owner) return fail(TOMO_ERR_INVALID, "the owner shares another handle's volume");
+    if (!p->vol_sharers.empty()) return fail(TOMO_ERR_INVALID, "other handles share this handle's volume");
+    if (p->vol_owner == owner) return TOMO_OK;
+    if (p->vol_owner) CKS(tomo_share_volume(p, nullptr));
+    if (p->g.W != owner->g.W || p->g.H != owner->g.H || p->g.D != owner->g.D)
+        return fail(TOMO_ERR_INVALID, "volume sizes differ");
+    CK(cudaStreamSynchronize(p->stream));
+    CK(cudaStreamSynchronize(owner->stream));
+    if (!p->vol_owner) free_n(p, &p->d_vol, p->nvox);
+    p->d_vol = owner->d_vol;
+    p->vol_owner = owner;
+    p->stream = owner->stream;
+    owner->vol_sharers.push_back(p);
     return TOMO_OK;
 }
 

@@ -18,6 +18,8 @@ struct tomo_projector {
     uint64_t bytes = 0;
 
     float* d_vol = nullptr;        // FP32 volume (precision TOMO_PREC_FP32)
+    tomo_projector* vol_owner = nullptr;  // d_vol belongs to this handle (tomo_share_volume)
+    std::vector<tomo_projector*> vol_sharers;  // handles working on this handle's d_vol
     int vtype = tomo::kVolF32;          // volume storage type (tomo_params.precision)
     uint16_t* d_vol16 = nullptr;   // reduced volume [D][H][W] (BF16 / FP16 bit patterns)
     float* d_vscale = nullptr;     // [H] slab scales of the reduced volume
@@ -84,6 +86,8 @@ struct tomo_projector {
     bool obatch_valid = false;
     bool meas_has_nan = false, meas_has_inf = false;
     bool vol_nonfinite = false;
+    // the flag of the volume this handle works on (the owner's when shared)
+    bool& vol_flag() { return vol_owner ? vol_owner->vol_nonfinite : vol_nonfinite; }
     int weight_kind = TOMO_WEIGHT_NONE;
     float tv_theta = 25.0f, tv_g = 1.0f, tv_dt = 0.1f;
     int tv_iters = 0;

@@ -199,6 +199,16 @@ class VoxelProjector3D(Projector):
         check(self._lib.tomo_cancel(self._h))
 
     # volume plumbing used by TomoReconstruction2
+    def _share_volume(self, owner):
+        """Work on `owner`'s device volume (two projectors on one TomoReconstruction2);
+        None takes a private copy."""
+        check(self._lib.tomo_share_volume(self._h, None if owner is None else owner._h))
+
+    def _shares_with(self, other) -> bool:
+        """Whether this projector can work on `other`'s device volume."""
+        return (isinstance(other, VoxelProjector3D) and getattr(other, "_h", None) is not None
+                and self._params.precision == _abi.PREC_FP32 and other._params.precision == _abi.PREC_FP32)
+
     def _set_volume(self, vol: np.ndarray):
         vol = np.ascontiguousarray(vol, np.float32)
         check(self._lib.tomo_set_volume(self._h, vol.ctypes.data, 0, 0, vol.shape[1]))

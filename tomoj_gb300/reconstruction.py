@@ -29,7 +29,8 @@ class TomoReconstruction2:
         self.centerx = (self.W - 1) / 2.0
         self.centery = (self.H - 1) / 2.0
         self.centerz = (self.D - 1) / 2.0
-        self._proj = None
+        self._proj = None      # the projector holding the volume on the device
+        self._sharers = []     # projectors working on the same device volume
         self.completion = 0.0
 
     # --- container ------------------------------------------------------------------
@@ -49,13 +50,24 @@ class TomoReconstruction2:
         self.centerx, self.centery, self.centerz = float(cx), float(cy), float(cz)
 
     def _attach(self, projector):
+        # projectors built on the same reconstruction work on one volume (the dual-axis
+        # drivers construct two), as the reference's projectors share `rec`
+        owner = self._proj
+        if owner is not None and owner is not projector and projector._shares_with(owner):
+            projector._share_volume(owner)
+            self._sharers.append(projector)
+            return
         self._proj = projector
+        self._sharers = []
         projector._set_volume(self._host)
 
     def _detach(self, projector):
         if self._proj is projector:
             self._host = projector._get_volume()
-            self._proj = None
+            # the engine hands the device volume to the first sharer
+            self._proj = self._sharers.pop(0) if self._sharers else None
+        elif projector in self._sharers:
+            self._sharers.remove(projector)
 
     def getVolume(self) -> np.ndarray:
         if self._proj is not None:
@@ -69,8 +81,8 @@ class TomoReconstruction2:
 
     def interrupt(self):
         self.completion = -1000
-        if self._proj is not None:
-            self._proj.cancel()
+        for p in ([self._proj] if self._proj is not None else []) + self._sharers:
+            p.cancel()
 
     # --- drivers ----------------------------------------------------------------------
     def WBP(self, ts, projector: Projector, params=None, startY=0, endY=None):
@@ -100,33 +112,147 @@ class TomoReconstruction2:
 
     def _ossart_surface(self, ts, projector, params, startY, endY, seed):
         n = ts.getImageStackSize()
-        eul = ts.eulers()
-        upd = n if params.getUpdateNb() == 0 else params.getUpdateNb()
-        factor = float(np.float32(params.getRelaxationCoefficient() / upd))
         out = []
         for it in range(params.getNbIterations()):
             projector.startOfIteration()
-            order = order_shuffle(eul, first_index(seed, it, n))
-            som, errmin, errmax, imin, imax = 0.0, float(np.finfo(np.float32).max), 0.0, 0, 0
-            batch = []
-            for t in range(n):
-                projector.addProjection(int(order[t]))
-                batch.append(int(order[t]))
-                if len(batch) == upd or t == n - 1:
-                    err = projector.projectAndDifference(factor, startY, endY)
-                    for e, v in enumerate(err):
-                        som += v
-                        if v > errmax:
-                            errmax, imax = v, order[t - len(err) + e + 1]
-                        elif v < errmin:
-                            errmin, imin = v, order[t - len(err) + e + 1]
-                    projector.backproject(startY, endY)
-                    projector.clearAllProjections()
-                    batch = []
+            out.append(self.osartIteration(projector, ts, params, startY, endY, first_index(seed, it, n)))
             projector.endOfIteration()
-            wh = self.W * self.H
-            out.append([np.sqrt(som / (n * wh)), np.sqrt(errmin / wh), imin, np.sqrt(errmax / wh), imax])
         return np.array(out)
+
+    def osartIteration(self, projector, ts, params, startY, endY, first):
+        """One iteration through the Projector surface (TomoReconstruction2.osartIteration,
+        :640-733); `first` is orderShuffleART's first index.  Returns [average, min, argmin,
+        max, argmax]."""
+        n = ts.getImageStackSize()
+        order = order_shuffle(ts.eulers(), first)
+        upd = n if params.getUpdateNb() == 0 else params.getUpdateNb()
+        factor = float(np.float32(params.getRelaxationCoefficient() / upd))
+        som, errmin, errmax, imin, imax = 0.0, float(np.finfo(np.float32).max), 0.0, 0, 0
+        pending = 0
+        projector.clearAllProjections()
+        for t in range(n):
+            projector.addProjection(int(order[t]))
+            pending += 1
+            if pending == upd or t == n - 1:
+                err = projector.projectAndDifference(factor, startY, endY)
+                for e, v in enumerate(err):
+                    som += v
+                    if v > errmax:
+                        errmax, imax = v, order[t - len(err) + e + 1]
+                    elif v < errmin:
+                        errmin, imin = v, order[t - len(err) + e + 1]
+                projector.backproject(startY, endY)
+                projector.clearAllProjections()
+                pending = 0
+        wh = self.W * self.H
+        return [np.sqrt(som / (n * wh)), np.sqrt(errmin / wh), imin, np.sqrt(errmax / wh), imax]
+
+    def osartIterationDual(self, projector1, ts1, projector2, ts2, params, startY, endY, first1, first2):
+        """TomoReconstruction2.osartIterationDual (:1282-1428): the two series alternate two
+        projections at a time with one update counter shared by both projectors; the loop
+        runs t < n1 - 1 (the last projection of an odd-length first series is not used) and
+        a projector's pending projections are flushed when the shared counter reaches
+        `update` or at its series' last index."""
+        n1, n2 = ts1.getImageStackSize(), ts2.getImageStackSize()
+        upd = params.getUpdateNb()  # used as given: 0 is not replaced by the series length here
+        factor = float(np.float32(params.getRelaxationCoefficient() / upd)) if upd else float(np.float32(np.inf))
+        projector1.clearAllProjections()
+        projector2.clearAllProjections()
+        idx = (order_shuffle(ts1.eulers(), first1), order_shuffle(ts2.eulers(), first2))
+        state = {"diff": 0, "som": 0.0, "min": float(np.finfo(np.float32).max), "max": 0.0, "imin": 0, "imax": 0}
+
+        def step(proj, ts, order, t, i):
+            proj.addProjection(int(order[t + i]))
+            state["diff"] += 1
+            if state["diff"] == upd or t + i == ts.getImageStackSize() - 1:
+                err = proj.projectAndDifference(factor, startY, endY)
+                for e, v in enumerate(err):
+                    state["som"] += v
+                    if v > state["max"]:
+                        state["max"], state["imax"] = v, int(order[t + i - len(err) + e + 1])
+                    elif v < state["min"]:
+                        state["min"], state["imin"] = v, int(order[t + i - len(err) + e + 1])
+                proj.backproject(startY, endY)
+                proj.clearAllProjections()
+                state["diff"] = 0
+
+        for t in range(0, n1 - 1, 2):
+            for i in range(2):
+                if t + 1 >= n1 or self.completion < 0:
+                    break
+                step(projector1, ts1, idx[0], t, i)
+            for i in range(2):
+                if t + 1 >= n2 or self.completion < 0:
+                    break
+                step(projector2, ts2, idx[1], t, i)
+        wh = self.W * self.H
+        return [np.sqrt(state["som"] / ((n1 + n2) * wh)), np.sqrt(state["min"] / wh), state["imin"],
+                np.sqrt(state["max"] / wh), state["imax"]]
+
+    def _until_diverging(self, iteration, n_iter):
+        """The dual-axis drivers' loop: stop once the average residual grows by more than
+        10 % over the previous iteration's.  Returns the average of every iteration run."""
+        out, err0 = [], float("inf")
+        for i in range(n_iter):
+            if self.completion < 0:
+                break
+            err = iteration(i)
+            out.append(err[0])
+            if err[0] > err0 * 1.1:
+                self.completion = -1000
+            else:
+                err0 = err[0]
+        return out
+
+    def ADASIRT(self, ts1, projector1, ts2, projector2, params, startY=0, endY=None, seed=0):
+        """TomoReconstruction2.ADASIRT (:880-999): alternate whole iterations of the two
+        series on one volume.  As the reference, projector1.endOfIteration() runs after
+        both halves (projector2's never does).  Iteration i orders series 1 and 2 with
+        first indexes first_index(seed, 2i, n1) and first_index(seed, 2i + 1, n2)."""
+        endY = self.H if endY is None else endY
+        self.completion = 0.0
+        n1, n2 = ts1.getImageStackSize(), ts2.getImageStackSize()
+
+        def iteration(i):
+            projector1.startOfIteration()
+            self.osartIteration(projector1, ts1, params, startY, endY, first_index(seed, 2 * i, n1))
+            projector1.endOfIteration()
+            projector2.startOfIteration()
+            err = self.osartIteration(projector2, ts2, params, startY, endY, first_index(seed, 2 * i + 1, n2))
+            projector1.endOfIteration()
+            return err
+
+        return self._until_diverging(iteration, params.getNbIterations())
+
+    def ADOSSART(self, ts1, projector1, ts2, projector2, params, startY=0, endY=None, seed=0):
+        """TomoReconstruction2.ADOSSART (:1001-1100): iterations of osartIterationDual, then
+        both projectors' endOfIteration."""
+        endY = self.H if endY is None else endY
+        self.completion = 0.0
+        n1, n2 = ts1.getImageStackSize(), ts2.getImageStackSize()
+
+        def iteration(i):
+            err = self.osartIterationDual(projector1, ts1, projector2, ts2, params, startY, endY,
+                                          first_index(seed, 2 * i, n1), first_index(seed, 2 * i + 1, n2))
+            projector1.endOfIteration()
+            projector2.endOfIteration()
+            return err
+
+        return self._until_diverging(iteration, params.getNbIterations())
+
+    def ADASIRT2Single(self, ts, projector, params, startY=0, endY=None, seed=0):
+        """TomoReconstruction2.ADASIRT2Single (:1102-1181): osartIteration + endOfIteration
+        with the dual drivers' stop rule."""
+        endY = self.H if endY is None else endY
+        self.completion = 0.0
+        n = ts.getImageStackSize()
+
+        def iteration(i):
+            err = self.osartIteration(projector, ts, params, startY, endY, first_index(seed, i, n))
+            projector.endOfIteration()
+            return err
+
+        return self._until_diverging(iteration, params.getNbIterations())
 
 
 def order_shuffle(eulers, first: int) -> np.ndarray:
