@@ -256,10 +256,6 @@ __device__ __forceinline__ PartialOut full_chunk_inl(const float2* __restrict__ 
     }
     return PartialOut{x0, a0 + a1};
 }
-template <int ZC>
-static __device__ __noinline__ PartialOut full_chunk_call(const float2* __restrict__ P, long long x, long long step) {
-    return full_chunk_inl<ZC>(P, x, step);
-}
 
 // One CTA's work: projection row j, tilts [g0, g0 + tilts_per_cta) of problem `a`,
 // depth part zp of a.zparts.
@@ -391,11 +387,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 const bool none = (cnt == 0) || (za + cnt <= z0) || (za >= z0 + zc);
                 if (__all_sync(0xffffffffu, full) && zc == ZC) {
                     if (ZC >= 2) {
-#ifdef TOMO_FP_FULL_NOINLINE
-                        const PartialOut fo = full_chunk_call<ZC>(P, X[k], st + pitch);
-#else
                         const PartialOut fo = full_chunk_inl<ZC>(P, X[k], st + pitch);
-#endif
                         X[k] = fo.x - (long long)ZC * pitch;
                         acc[k] += fo.s;
                     } else {
