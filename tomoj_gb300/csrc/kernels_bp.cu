@@ -52,7 +52,8 @@ struct BpShared {
     float raw[kTC][kRawSeg];
     int seg_start[kTC];
     int raw_start[kTC];
-    long long K[kTC], C[kTC], S[kTC];
+    long long C[kTC], S[kTC];
+    long long AZ[kTC][4];  // position of (x0, z0 + 16 g) with the segment base, per tilt and z-group g
     int zint[kTC][kTX];
 };
 
@@ -108,6 +109,7 @@ template <bool SANITIZE, bool POS, int VT, int SEG>
 __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const int z0, const int r) {
     constexpr int kTC = BpSeg<SEG>::kTC, kSeg = BpSeg<SEG>::kSeg, kRawSeg = BpSeg<SEG>::kRawSeg;
     constexpr int kThr = kBpCtaThreads, kCX = kTX / kNC;
+    static_assert(kThr / kCX == 4 && 4 * kKZ == kTZ, "four z-groups of 16 voxels per tile");
     __shared__ __align__(16) BpShared<SEG> sh;
     const int tid = threadIdx.x;
     const int tx = tid % kCX;
@@ -153,7 +155,6 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
         if (tid < tc) {
             const int tilt = a.tilts[c0 + tid];
             const BpTilt b = a.btilt[tilt];
-            sh.K[tid] = b.K;
             sh.C[tid] = b.C;
             sh.S[tid] = b.S;
             const long long p00 = b.K + (long long)xa * b.C + (long long)za * b.S;
@@ -164,6 +165,10 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
             const int s = (int)(mn >> 32);
             sh.seg_start[tid] = s;
             sh.raw_start[tid] = s & ~3;
+            // the tilt's segment base rides in the high word, so (X >> 32) is the flat pair index
+            const long long base = (long long)(tid * kSeg - s) << 32;
+#pragma unroll
+            for (int g = 0; g < 4; g++) sh.AZ[tid][g] = p00 + (long long)(g * kKZ) * b.S + base;
         }
         for (int t = tzg; t < tc; t += kThr / kCX)
 #pragma unroll
@@ -231,10 +236,8 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
         __syncthreads();
         // --- accumulate the chunk's tilts in update order ----------------------------------
         for (int t = 0; t < tc; t++) {
-            // the tilt's segment base rides in the high word, so (X >> 32) is the flat pair index
-            const long long base = (long long)(t * kSeg - sh.seg_start[t]) << 32;
             const long long S = sh.S[t];
-            const long long Xc0 = sh.K[t] + (long long)(x0 + tx) * sh.C[t] + (long long)zs * sh.S[t] + base;
+            const long long Xc0 = sh.AZ[t][tzg] + (long long)(unsigned)tx * sh.C[t];
 #pragma unroll
             for (int c = 0; c < kNC; c++) {
                 long long X = Xc0 + (long long)(c * kCX) * sh.C[t];
