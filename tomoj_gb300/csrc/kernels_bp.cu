@@ -24,7 +24,7 @@ namespace tomo {
 namespace {
 
 #ifndef TOMO_BP_MIN_BLOCKS
-#define TOMO_BP_MIN_BLOCKS 3
+#define TOMO_BP_MIN_BLOCKS 4
 #endif
 constexpr int kBpThreads = 256;
 #ifndef TOMO_BP_NC
@@ -311,10 +311,14 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
     }
 }
 
-// Reduced storage carries a compensation register per voxel: two CTAs per SM.
+// Reduced storage carries a compensation register per voxel: fewer CTAs per SM.
 template <int VT>
 struct BpOcc {
-    static constexpr int value = kNC == 1 ? (VT == kVolF32 ? TOMO_BP_MIN_BLOCKS : 2) : (VT == kVolF32 ? 4 : 3);
+#ifndef TOMO_BP_MIN_BLOCKS_16
+#define TOMO_BP_MIN_BLOCKS_16 3
+#endif
+    static constexpr int value =
+        kNC == 1 ? (VT == kVolF32 ? TOMO_BP_MIN_BLOCKS : TOMO_BP_MIN_BLOCKS_16) : (VT == kVolF32 ? 4 : 3);
 };
 
 template <bool SANITIZE, bool POS, int VT, int SEG>
