@@ -136,3 +136,14 @@ def test_shared_volume_survives_its_owner(engine, dual):
     finally:
         p1.close()
         p2.close()
+
+
+def test_a_sharer_follows_its_owners_stream(engine, dual):
+    from tomoj_gb300 import _abi
+    rec, p1, p2 = projectors(dual)
+    try:
+        assert engine.tomo_set_stream(p2.handle, None) == _abi.ERR_STATE
+        assert engine.tomo_set_stream(p1.handle, None) == _abi.OK
+    finally:
+        p2.close()
+        p1.close()

@@ -610,8 +610,11 @@ tomo_status tomo_destroy(tomo_projector* p) {
 
 tomo_status tomo_set_stream(tomo_projector* p, void* stream) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (p->vol_owner)
+        return fail(TOMO_ERR_STATE, "this handle works on another handle's volume: set the owner's stream");
     CK(cudaStreamSynchronize(p->stream));
     p->stream = stream ? static_cast<cudaStream_t>(stream) : p->own_stream;
+    for (tomo_projector* q : p->vol_sharers) q->stream = p->stream;  // one volume, one stream
     return TOMO_OK;
 }
 
