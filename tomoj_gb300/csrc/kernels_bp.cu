@@ -123,7 +123,9 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
     const bool blend = byf != 0.0f && jp < h - 1;
     const int zs = z0 + tzg * kKZ;
 
-    const size_t plane = (size_t)H * W;
+    // voxel k of a thread sits k * H * W elements after its first; tomo_create keeps
+    // 16 * H * W below 2^32, so the offsets are 32-bit products of a uniform value
+    const unsigned plane = (unsigned)H * (unsigned)W;
     const float vsc = (VT == kVolF32) ? 1.0f : a.vscale[r];
     float vox[kNC][kKZ], comp[kNC][kKZ];
     int nk[kNC];

@@ -476,6 +476,9 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
         return fail(TOMO_ERR_INVALID, "dimensions must be positive");
     if (geom->D > 65535 || geom->w > 4096 || geom->W > 65535)
         return fail(TOMO_ERR_UNSUPPORTED, "D <= 65535, W <= 65535 and w <= 4096 are supported");
+    // the backprojector addresses a thread's 16 voxels with 32-bit offsets of k * H * W
+    if ((uint64_t)geom->W * (uint64_t)geom->H * 16u >= (1ull << 32))
+        return fail(TOMO_ERR_UNSUPPORTED, "W * H must be below 2^28");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
