@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <thread>
 #include <utility>
 #include <vector>
@@ -407,7 +408,7 @@ void weighting_mask_2d(int w, int h, int nproj, const double* tilt_deg, const do
         sinp[p] = std::sin(axis_deg[p] * (M_PI / 180.0));
     }
     // w * h * nproj sines: rows are split over the host threads
-    auto rows = [&](int ja, int jb) {
+    parallel_ranges(h, 8, [&](int ja, int jb) {
         for (int j = ja; j < jb; j++) {
             const double cj = (j > cy) ? j - h : j;
             for (int i = 0; i < w; i++) {
@@ -427,11 +428,16 @@ void weighting_mask_2d(int w, int h, int nproj, const double* tilt_deg, const do
                 maskT[(size_t)i * h + j] = (float)(1 / weight);
             }
         }
-    };
-    const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), (h + 7) / 8));
+    });
+}
+
+void parallel_ranges(int n, int min_per_thread, const std::function<void(int, int)>& fn) {
+    if (n <= 0) return;
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int nt = std::max(1, std::min({hw, 16, (n + min_per_thread - 1) / std::max(1, min_per_thread)}));
     std::vector<std::thread> pool;
-    for (int t = 1; t < nt; t++) pool.emplace_back(rows, (int)((long long)h * t / nt), (int)((long long)h * (t + 1) / nt));
-    rows(0, (int)((long long)h / nt));
+    for (int t = 1; t < nt; t++) pool.emplace_back(fn, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+    fn(0, (int)((long long)n / nt));
     for (auto& th : pool) th.join();
 }
 

@@ -677,10 +677,13 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
         std::vector<FpRay> rays((size_t)N * g.w);
         std::vector<BpTilt> bt(N);
         std::vector<int32_t> zint((size_t)N * g.W);
-        for (int t = 0; t < N; t++) {
-            build_fp_tables(g, &p->euler[9 * t], &ft[t], &rays[(size_t)t * g.w]);
-            build_bp_tables(g, &p->euler[9 * t], &bt[t], &zint[(size_t)t * g.W]);
-        }
+        // tilts are independent: their tables are built on the host threads
+        parallel_ranges(N, 4, [&](int t0, int t1) {
+            for (int t = t0; t < t1; t++) {
+                build_fp_tables(g, &p->euler[9 * t], &ft[t], &rays[(size_t)t * g.w]);
+                build_bp_tables(g, &p->euler[9 * t], &bt[t], &zint[(size_t)t * g.W]);
+            }
+        });
         CK(cudaMemcpyAsync(p->d_ftilt, ft.data(), sizeof(FpTilt) * N, cudaMemcpyHostToDevice, p->stream));
         CK(cudaMemcpyAsync(p->d_rays, rays.data(), sizeof(FpRay) * rays.size(), cudaMemcpyHostToDevice, p->stream));
         CK(cudaMemcpyAsync(p->d_btilt, bt.data(), sizeof(BpTilt) * N, cudaMemcpyHostToDevice, p->stream));

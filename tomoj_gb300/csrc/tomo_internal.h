@@ -11,6 +11,7 @@
 // exact double arithmetic and shipped as per-ray / per-column z intervals.
 #pragma once
 #include <atomic>
+#include <functional>
 #include <cstddef>
 #include <cstdint>
 
@@ -90,6 +91,9 @@ void build_generic_fp_tilt(const double* R, GenericFpTilt* out);
 // h = IDFT_w(mask_row), zero-padded: the row filter as a convolution.
 void row_filter_spectrum(const float* mask_row, int w, int M, float2* H);
 void order_shuffle(int n, const double* euler, int first, int* out);
+// fn(begin, end) over [0, n) split into contiguous ranges on up to 16 host threads,
+// at least min_per_thread items each (the calling thread takes the first range).
+void parallel_ranges(int n, int min_per_thread, const std::function<void(int, int)>& fn);
 int first_index(uint64_t seed, int iteration, int nproj);
 void weighting_row_filter(int kind, int w, int nproj, const double* sint, const double* tilts_deg, double diameter,
                           float* mask_row);
