@@ -62,6 +62,10 @@ def test_invalid_arguments_are_rejected(engine):
     out = np.zeros(3, np.int32)
     assert engine.tomo_order_shuffle(3, _abi.ptr(e, C.c_double), 5, _abi.ptr(out, C.c_int32)) == -1
     assert b"first index" in engine.tomo_last_error()
+    # a thread's 16 voxels are addressed with 32-bit offsets: 16 * W * H must stay below 2^32
+    g = _abi.make_geom(65535, 4097, 8, 64, 8, 3)
+    assert engine.tomo_create(C.byref(g), None, C.byref(h)) == _abi.ERR_UNSUPPORTED
+    assert b"2^28" in engine.tomo_last_error()
 
 
 @pytest.mark.parametrize("first", [0, 7, 30, 60])
