@@ -148,6 +148,14 @@ tomo_status tomo_get_difference(tomo_projector* p, int32_t k, float* out_host);
 int32_t tomo_projection_count(tomo_projector* p);
 
 /* ---- options ------------------------------------------------------------ */
+/* VoxelProjector3D setters (VoxelProjector3D.java:78-104): positivity constraint,
+ * long-object compensation, and the projection / reconstruction scale (the geometry
+ * tables are rebuilt when a series is loaded).  setNbRaysPerPixels has no engine
+ * call: the Joseph projector of the reference ignores it (projectJosephPartial reads
+ * one ray per pixel; projectPartial resets it to 1, VoxelProjector3D.java:471). */
+tomo_status tomo_set_positivity(tomo_projector* p, int32_t enabled);
+tomo_status tomo_set_long_object(tomo_projector* p, int32_t enabled);
+tomo_status tomo_set_scale(tomo_projector* p, double scale);
 /* WBP weighting applied before every backprojection (VoxelProjector3D.java:163-166),
  * replacing new FFTWeighting(ts, radius * w) (ReconstructionParameters.java:320,
  * FFTWeighting.java:22-24).  tilt_deg: per-tilt ts.getTiltAngle(i) in degrees (NULL =

@@ -90,6 +90,9 @@ SIGNATURES = {
     "tomo_get_norm": (C.c_int32, [_P, C.c_int32, _f32p]),
     "tomo_get_difference": (C.c_int32, [_P, C.c_int32, _f32p]),
     "tomo_projection_count": (C.c_int32, [_P]),
+    "tomo_set_positivity": (C.c_int32, [_P, C.c_int32]),
+    "tomo_set_long_object": (C.c_int32, [_P, C.c_int32]),
+    "tomo_set_scale": (C.c_int32, [_P, C.c_double]),
     "tomo_set_weighting": (C.c_int32, [_P, C.c_int32, C.c_double, _f64p, _f64p]),
     "tomo_set_tvm": (C.c_int32, [_P, C.c_float, C.c_float, C.c_float, C.c_int32]),
     "tomo_set_fista": (C.c_int32, [_P, C.c_int32]),

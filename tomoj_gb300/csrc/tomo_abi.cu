@@ -621,15 +621,11 @@ tomo_status tomo_set_stream(tomo_projector* p, void* stream) {
     return TOMO_OK;
 }
 
-tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pixels_on_device, const double* euler,
-                             const double* transforms, const double* stats) {
-    if (!p || !pixels || !euler) return fail(TOMO_ERR_INVALID, "null argument");
+// Geometry tables of the loaded Euler matrices and the handle's geometry (scale,
+// centres): the kernel family (separable, fractional rows, generic) and its tables.
+static tomo_status setup_geometry(tomo_projector* p) {
     Geometry& g = p->g;
     const int N = g.N;
-    CK(cudaMemcpyAsync(p->d_raw, pixels, sizeof(float) * N * p->npix,
-                       pixels_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, p->stream));
-    p->euler.assign(euler, euler + 9 * (size_t)N);
-    // geometry tables
     bool integral = true, vertical = true;
     for (int t = 0; t < N; t++) {
         integral = integral && tilt_is_separable(&p->euler[9 * t], g);
@@ -703,6 +699,18 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
         CK(cudaMemcpyAsync(p->d_euler, p->euler.data(), sizeof(double) * 9 * N, cudaMemcpyHostToDevice, p->stream));
         CK(cudaStreamSynchronize(p->stream));
     }
+    return TOMO_OK;
+}
+
+tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pixels_on_device, const double* euler,
+                             const double* transforms, const double* stats) {
+    if (!p || !pixels || !euler) return fail(TOMO_ERR_INVALID, "null argument");
+    Geometry& g = p->g;
+    const int N = g.N;
+    CK(cudaMemcpyAsync(p->d_raw, pixels, sizeof(float) * N * p->npix,
+                       pixels_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, p->stream));
+    p->euler.assign(euler, euler + 9 * (size_t)N);
+    CKS(setup_geometry(p));
     // alignment: Tinv = AffineTransform.createInverse (general case)
     std::vector<double> tinv((size_t)N * 6), st((size_t)N * 2);
     std::vector<unsigned char> ident(N);
@@ -740,6 +748,36 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
     p->batch.clear();
     p->batch_uploaded = false;
     p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_positivity(tomo_projector* p, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    p->params.positivity = enabled ? 1 : 0;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_long_object(tomo_projector* p, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    p->params.long_object = enabled ? 1 : 0;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_scale(tomo_projector* p, double scale) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (!(scale > 0) || !std::isfinite(scale)) return fail(TOMO_ERR_INVALID, "scale must be positive");
+    const double old = p->g.scale;
+    p->g.scale = scale;
+    if (!p->series_loaded) return TOMO_OK;
+    const tomo_status st = setup_geometry(p);
+    if (st != TOMO_OK) {
+        const std::string why = tomo_last_error();
+        p->g.scale = old;
+        setup_geometry(p);
+        return fail(st, why);
+    }
+    p->fprow_j0 = -1;
+    p->diffs_valid = p->projected = false;
     return TOMO_OK;
 }
 

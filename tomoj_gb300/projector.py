@@ -107,6 +107,21 @@ class VoxelProjector3D(Projector):
                                          None if stats is None else _abi.ptr(stats, C.c_double)))
 
     # --- setters (VoxelProjector3D.java:78-104) ----------------------------------------
+    def setPositivityConstraint(self, enabled: bool):
+        check(self._lib.tomo_set_positivity(self._h, int(bool(enabled))))
+
+    def setLongObjectCompensation(self, enabled: bool):
+        check(self._lib.tomo_set_long_object(self._h, int(bool(enabled))))
+
+    def setScale(self, value: float):
+        """Projection width / reconstruction width (VoxelProjector3D.setScale)."""
+        check(self._lib.tomo_set_scale(self._h, float(value)))
+
+    def setNbRaysPerPixels(self, n: float):
+        """Kept for the reference's interface: its Joseph projector reads one ray per
+        pixel whatever this value (VoxelProjector3D.java:471, 671-821)."""
+        self.nbRaysPerPixels = float(n)
+
     def setWeighting(self, kind: int, radius: float = 0.0):
         """new FFTWeighting(ts, radius * w) (ReconstructionParameters.java:320): the mask
         reads every tilt angle and the tilt axis (FFTWeighting.java:67-81)."""
