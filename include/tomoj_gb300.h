@@ -156,6 +156,11 @@ int32_t tomo_projection_count(tomo_projector* p);
 tomo_status tomo_set_positivity(tomo_projector* p, int32_t enabled);
 tomo_status tomo_set_long_object(tomo_projector* p, int32_t enabled);
 tomo_status tomo_set_scale(tomo_projector* p, double scale);
+/* Projector.setVolumeCenters(cx, cy, cz) / setProjectionCenter(...) (Projector.java:52-108):
+ * vol_center {cx, cy, cz}, proj_center {centerX, centerY, projectionCenterX,
+ * projectionCenterY}; NULL or NaN entries keep their value.  Rebuilds the geometry
+ * tables of a loaded series. */
+tomo_status tomo_set_centers(tomo_projector* p, const double* vol_center, const double* proj_center);
 /* WBP weighting applied before every backprojection (VoxelProjector3D.java:163-166),
  * replacing new FFTWeighting(ts, radius * w) (ReconstructionParameters.java:320,
  * FFTWeighting.java:22-24).  tilt_deg: per-tilt ts.getTiltAngle(i) in degrees (NULL =

@@ -85,3 +85,28 @@ def test_set_scale_rejects_nonpositive(engine):
         assert engine.tomo_set_scale(hd, -1.0) == _abi.ERR_INVALID
     finally:
         engine.tomo_destroy(hd)
+
+
+def test_set_centers_equals_creation_centres(engine):
+    # volume centre off by 1.5 columns / 0.5 planes, tilt axis 2 pixels right of the
+    # projection centre: blended rows and shifted tables, as a handle created with them
+    vol, eul, series = make_series(2.0)
+    vc = np.array([(W - 1) / 2.0 + 1.5, (H - 1) / 2.0, (D - 1) / 2.0 - 0.5])
+    pc = np.array([(w - 1) / 2.0, (h - 1) / 2.0, (w - 1) / 2.0 + 2.0, (h - 1) / 2.0])
+    g = _abi.make_geom(W, H, D, w, h, n, vol_center=tuple(vc), proj_center=tuple(pc), scale=2.0)
+    p = _abi.make_params()
+    ref_h = C.c_void_p()
+    _abi.check(engine.tomo_create(C.byref(g), C.byref(p), C.byref(ref_h)))
+    hd = handle(engine, 2.0)
+    try:
+        load(engine, ref_h, eul, series)
+        load(engine, hd, eul, series)
+        _abi.check(engine.tomo_set_centers(hd, _abi.ptr(np.ascontiguousarray(vc), C.c_double),
+                                           _abi.ptr(np.ascontiguousarray(pc), C.c_double)))
+        v_ref, n_ref = run(engine, ref_h, vol)
+        v, nm = run(engine, hd, vol)
+        assert np.array_equal(v, v_ref)
+        assert np.array_equal(nm, n_ref)
+    finally:
+        engine.tomo_destroy(ref_h)
+        engine.tomo_destroy(hd)

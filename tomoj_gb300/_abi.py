@@ -93,6 +93,7 @@ SIGNATURES = {
     "tomo_set_positivity": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_long_object": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_scale": (C.c_int32, [_P, C.c_double]),
+    "tomo_set_centers": (C.c_int32, [_P, _f64p, _f64p]),
     "tomo_set_weighting": (C.c_int32, [_P, C.c_int32, C.c_double, _f64p, _f64p]),
     "tomo_set_tvm": (C.c_int32, [_P, C.c_float, C.c_float, C.c_float, C.c_int32]),
     "tomo_set_fista": (C.c_int32, [_P, C.c_int32]),

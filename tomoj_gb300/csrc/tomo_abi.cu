@@ -781,6 +781,30 @@ tomo_status tomo_set_scale(tomo_projector* p, double scale) {
     return TOMO_OK;
 }
 
+tomo_status tomo_set_centers(tomo_projector* p, const double* vol_center, const double* proj_center) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    Geometry& g = p->g;
+    double vc[3], pc[4];
+    std::memcpy(vc, g.vc, sizeof(vc));
+    std::memcpy(pc, g.pc, sizeof(pc));
+    for (int k = 0; k < 3; k++)
+        if (vol_center && !std::isnan(vol_center[k])) g.vc[k] = vol_center[k];
+    for (int k = 0; k < 4; k++)
+        if (proj_center && !std::isnan(proj_center[k])) g.pc[k] = proj_center[k];
+    if (!p->series_loaded) return TOMO_OK;
+    const tomo_status st = setup_geometry(p);
+    if (st != TOMO_OK) {
+        const std::string why = tomo_last_error();
+        std::memcpy(g.vc, vc, sizeof(vc));
+        std::memcpy(g.pc, pc, sizeof(pc));
+        setup_geometry(p);
+        return fail(st, why);
+    }
+    p->fprow_j0 = -1;
+    p->diffs_valid = p->projected = false;
+    return TOMO_OK;
+}
+
 tomo_status tomo_set_fill(tomo_projector* p, int32_t fill) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
     if (fill < TOMO_FILL_NONE || fill > TOMO_FILL_NAN) return fail(TOMO_ERR_INVALID, "unknown fill type");

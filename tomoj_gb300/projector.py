@@ -117,6 +117,44 @@ class VoxelProjector3D(Projector):
         """Projection width / reconstruction width (VoxelProjector3D.setScale)."""
         check(self._lib.tomo_set_scale(self._h, float(value)))
 
+    def setVolumeCenters(self, cx, cy=None, cz=None):
+        """Projector.setVolumeCenters(rec) or (cx, cy, cz) (Projector.java:60-65, 104-108)."""
+        if cy is None:
+            cx, cy, cz = cx.centers()
+        vc = np.ascontiguousarray([cx, cy, cz], np.float64)
+        check(self._lib.tomo_set_centers(self._h, _abi.ptr(vc, C.c_double), None))
+
+    def setProjectionCenter(self, pcx, pcy=None):
+        """Projector.setProjectionCenter(ts) (all four centres) or (pcx, pcy) (the tilt-axis
+        position on the projections only) (Projector.java:52-58, 99-102)."""
+        if pcy is None:
+            ts = pcx
+            pc = [ts.getCenterX(), ts.getCenterY(), ts.getProjectionCenterX(), ts.getProjectionCenterY()]
+        else:
+            pc = [np.nan, np.nan, pcx, pcy]
+        pc = np.ascontiguousarray(pc, np.float64)
+        check(self._lib.tomo_set_centers(self._h, None, _abi.ptr(pc, C.c_double)))
+
+    def getTiltSeries(self):
+        return self.ts
+
+    def getReconstruction(self):
+        return self.rec
+
+    def getWeightingFilter(self):
+        return self.weighting
+
+    def setWeightingFilter(self, weighting):
+        """None or a (kind, radius) pair (Projector.setWeightingFilter)."""
+        if weighting is None:
+            check(self._lib.tomo_set_weighting(self._h, _abi.WEIGHT_NONE, 0.0, None, None))
+            self.weighting = None
+        else:
+            self.setWeighting(*weighting)
+
+    def getCompletion(self) -> float:
+        return float(getattr(self.rec, "completion", 0.0))
+
     def setNbRaysPerPixels(self, n: float):
         """Kept for the reference's interface: its Joseph projector reads one ray per
         pixel whatever this value (VoxelProjector3D.java:471, 671-821)."""
