@@ -110,3 +110,16 @@ def test_set_centers_equals_creation_centres(engine):
     finally:
         engine.tomo_destroy(ref_h)
         engine.tomo_destroy(hd)
+
+
+def test_project_volume_matches_oracle(engine, oracle_lib):
+    from tomoj_gb300.reconstruction import project_volume
+    vol = P.ellipsoid_phantom(32, 8, 24, 4, 3)
+    projs, angles = project_volume(vol, -30.0, 30.0, 7.5)
+    assert angles.size == 9 and projs.shape == (9, 8, 32)
+    g = O.Geom(32, 8, 24, 32, 8)
+    for i, a in enumerate(angles):
+        ref, _ = O.project(vol, g, O.euler_tilt_y(a))
+        assert np.array_equal(np.isnan(projs[i]), np.isnan(ref))
+        ok = ~np.isnan(ref)
+        assert np.allclose(projs[i][ok], ref[ok], rtol=1e-5, atol=1e-5)

@@ -357,3 +357,35 @@ class ReconstructionParameters:
         if self.fista:
             proj.setFista(True)
         return proj
+
+
+def project_volume(volume: np.ndarray, tilt_angle_start=-60.0, tilt_angle_end=60.0, tilt_angle_increment=2.0,
+                   center=None) -> tuple[np.ndarray, np.ndarray]:
+    """Project_Volume (TomoJ_Base/.../plugins/Project_Volume.java:41-70): a tilt-series of
+    the volume [D][H][W] at angles start, start + increment, ... <= end about the vertical
+    axis, projections W x H, through VoxelProjector3D.  center = (cx, cy, cz) of the tilt
+    axis in the volume (default (n - 1) / 2).  The reference sizes its angle array as
+    (int)((end - start + 1) / increment), one short when the increment does not divide
+    end - start + 1; every angle of the loop is kept here.  Returns (projections, angles)."""
+    from .tiltseries import TiltSeries
+    vol = np.ascontiguousarray(volume, np.float32)
+    D, H, W = vol.shape
+    angles = []
+    a = float(tilt_angle_start)
+    while a <= tilt_angle_end:
+        angles.append(a)
+        a += tilt_angle_increment
+    angles = np.array(angles)
+    ts = TiltSeries(np.zeros((angles.size, H, W), np.float32), angles)
+    ts.setNormalize(False)  # the blank series is never compared with the projections
+    rec = TomoReconstruction2(W, H, D, vol)
+    if center is not None:
+        rec.setCenter(*center)
+    proj = VoxelProjector3D(ts, rec)
+    try:
+        for i in range(angles.size):
+            proj.addProjection(i)
+        proj.project(0, H)
+        return np.array([proj.getProjection(i) for i in range(angles.size)], np.float32), angles
+    finally:
+        proj.close()
