@@ -336,6 +336,27 @@ def run_engine(args, wl):
     e2e_value = updates_per_step * e2e_steps * world / e2e_s
     phase = {k: v / e2e_steps for k, v in phase.items()}
 
+    # ---- the same job with its OS-SART iterations on two row streams (opt-in engine
+    # option: the forward projection of one row range overlaps the backprojection of
+    # the other; bitwise the same volume) ----
+    row_leg = None
+    if not args.no_extra:
+        _abi.check(lib.tomo_set_row_streams(h, 2))
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        ra, rb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ra.record(stream)
+        for _ in range(args.steps):
+            step()
+        rb.record(stream)
+        torch.cuda.synchronize()
+        rms = ra.elapsed_time(rb)
+        _abi.check(lib.tomo_set_row_streams(h, 1))
+        row_leg = {"row_streams": 2, "ms_per_step": rms / args.steps,
+                   "voxel_updates_per_s": updates_per_step * args.steps / (rms / 1000.0),
+                   "speedup_vs_one_stream": (ms / args.steps) / (rms / args.steps)}
+
     # ---- roofline of the dominant kernel ----
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
@@ -416,7 +437,7 @@ def run_engine(args, wl):
             "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps, "phases_s": phase},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-            "batched": batched, "serving": serving, "precision": precision,
+            "row_streams": row_leg, "batched": batched, "serving": serving, "precision": precision,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)

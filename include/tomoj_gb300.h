@@ -154,6 +154,11 @@ int32_t tomo_projection_count(tomo_projector* p);
  * call: the Joseph projector of the reference ignores it (projectJosephPartial reads
  * one ray per pixel; projectPartial resets it to 1, VoxelProjector3D.java:471). */
 tomo_status tomo_set_positivity(tomo_projector* p, int32_t enabled);
+/* OS-SART iterations over K (1..4) row ranges on K streams: volume rows are
+ * independent with a vertical tilt axis, so the forward projection of one range can
+ * overlap the backprojection of another.  Used for whole-row centre offsets, scale 1
+ * geometry, FP32 storage and no long-object compensation; otherwise one stream. */
+tomo_status tomo_set_row_streams(tomo_projector* p, int32_t k);
 tomo_status tomo_set_long_object(tomo_projector* p, int32_t enabled);
 tomo_status tomo_set_scale(tomo_projector* p, double scale);
 /* Projector.setVolumeCenters(cx, cy, cz) / setProjectionCenter(...) (Projector.java:52-108):

@@ -90,6 +90,7 @@ SIGNATURES = {
     "tomo_get_norm": (C.c_int32, [_P, C.c_int32, _f32p]),
     "tomo_get_difference": (C.c_int32, [_P, C.c_int32, _f32p]),
     "tomo_projection_count": (C.c_int32, [_P]),
+    "tomo_set_row_streams": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_positivity": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_long_object": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_scale": (C.c_int32, [_P, C.c_double]),

@@ -279,6 +279,40 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
     return TOMO_OK;
 }
 
+// Forward projection + difference of projection rows [j0, j1) only (separable FP32
+// geometry), on p->stream, no depth split and no residual reduction: one row range
+// of a row-stream iteration.
+tomo_status run_fp_range(tomo_projector* p, const int* d_tilts, int T, int j0, int j1, double factor, int slot0) {
+    const Geometry& g = p->g;
+    if (j0 >= j1) return TOMO_OK;
+    FpLaunch a{};
+    a.vol = p->vol();
+    a.vtype = p->vtype;
+    a.meas = p->d_meas;
+    a.tilts = d_tilts;
+    a.T = T;
+    a.ftilt = p->d_ftilt;
+    a.rays = p->d_rays;
+    a.proj = p->d_proj + (size_t)slot0 * p->npix;
+    a.norm = p->d_norm + (size_t)slot0 * p->npix;
+    a.diff = p->d_diff + (size_t)slot0 * p->npix;
+    a.errpart = p->d_errpart + (size_t)slot0 * g.h;
+    a.factor = factor;
+    a.j0 = j0;
+    a.j1 = j1;
+    a.tilts_per_cta = auto_tilts_per_cta(p, T, j1 - j0);
+    a.zparts = 1;
+    a.W = g.W;
+    a.H = g.H;
+    a.D = g.D;
+    a.w = g.w;
+    a.h = g.h;
+    a.row_off = g.fp_row_off;
+    a.status = p->d_status;
+    CK(launch_fp_separable(a, p->stream));
+    return TOMO_OK;
+}
+
 tomo_status apply_weighting(tomo_projector* p, float* imgs, int T) {
     if (p->weight_kind == TOMO_WEIGHT_NONE || T <= 0) return TOMO_OK;
     const Geometry& g = p->g;
@@ -606,6 +640,10 @@ tomo_status tomo_destroy(tomo_projector* p) {
     for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
     for (void* a : p->allocs) cudaFree(a);
     g_in_use -= p->bytes;
+    for (cudaEvent_t e : p->rs_ev) cudaEventDestroy(e);
+    for (cudaStream_t q : p->rs)
+        if (q) cudaStreamDestroy(q);
+    if (p->rs_reduce) cudaStreamDestroy(p->rs_reduce);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     delete p;
     return TOMO_OK;
@@ -748,6 +786,17 @@ tomo_status tomo_load_series(tomo_projector* p, const float* pixels, int32_t pix
     p->batch.clear();
     p->batch_uploaded = false;
     p->diffs_valid = p->projected = p->obatch_valid = false;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_row_streams(tomo_projector* p, int32_t k) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (k < 1 || k > 4) return fail(TOMO_ERR_INVALID, "1 to 4 row streams");
+    for (int i = 1; i < k; i++)
+        if (!p->rs[i]) CK(cudaStreamCreateWithFlags(&p->rs[i], cudaStreamNonBlocking));
+    if (k > 1 && !p->rs[0]) CK(cudaStreamCreateWithFlags(&p->rs[0], cudaStreamNonBlocking));
+    if (k > 1 && !p->rs_reduce) CK(cudaStreamCreateWithFlags(&p->rs_reduce, cudaStreamNonBlocking));
+    p->row_streams = k;
     return TOMO_OK;
 }
 
@@ -1357,7 +1406,89 @@ tomo_status tomo_run_ossart(tomo_projector* p, int32_t n_iter, double relax, int
             if (T > 0) fp_split(p, T, j1 - j0, auto_tilts_per_cta(p, T, j1 - j0));
         if (g.separable && g.fractional) CKS(ensure_fp_rowmap(p, j0));
     }
+    // row streams: integral separable FP32 geometry without long-object compensation
+    // (its norm maximum couples the rows of a projection)
+    const int K = (p->row_streams > 1 && g.separable && !g.fractional && !p->bp_generic && p->vtype == kVolF32 &&
+                   !p->params.long_object && g.fp_row_off == g.bp_row_off)
+                      ? p->row_streams
+                      : 1;
+    int rj0 = 0, rj1 = 0;
+    fp_rows(p, y0, &rj0, &rj1);
+    const int ry0 = std::max(0, y0), ry1 = std::min(g.H, y1);
+    if (K > 1) {
+        const size_t need = 1 + (size_t)nsub * K + K + 1;
+        while (p->rs_ev.size() < need) {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            p->rs_ev.push_back(e);
+        }
+    }
+    auto body_rows = [&](const int* d_ord) -> tomo_status {
+        CKS(start_iteration(p));
+        cudaStream_t main = p->stream;
+        struct Restore {  // the handle's stream comes back on every exit path
+            tomo_projector* p;
+            cudaStream_t s;
+            ~Restore() { p->stream = s; }
+        } restore{p, main};
+        if (rj0 > 0) {
+            // rows the reference leaves untouched stay zero, for every slot of the iteration
+            for (int b = 0; b < N; b++) {
+                const size_t o = (size_t)b * p->npix, n = sizeof(float) * (size_t)std::min(rj0, g.h) * g.w;
+                CK(cudaMemsetAsync(p->d_proj + o, 0, n, main));
+                CK(cudaMemsetAsync(p->d_norm + o, 0, n, main));
+                CK(cudaMemsetAsync(p->d_diff + o, 0, n, main));
+            }
+            CK(cudaMemsetAsync(p->d_errpart, 0, sizeof(double) * (size_t)N * g.h, main));
+        }
+        cudaEvent_t* ev = p->rs_ev.data();
+        CK(cudaEventRecord(ev[0], main));
+        CK(cudaStreamWaitEvent(p->rs_reduce, ev[0], 0));
+        // volume rows [yb[k], yb[k+1]) and the projection rows they see
+        std::vector<int> yb(K + 1), jb(K + 1);
+        for (int k = 0; k <= K; k++) {
+            yb[k] = ry0 + (int)((long long)(ry1 - ry0) * k / K);
+            jb[k] = std::min(std::max(yb[k] + g.fp_row_off, rj0), rj1);
+        }
+        jb[0] = rj0;
+        jb[K] = rj1;
+        tomo_status st = TOMO_OK;
+        for (int s = 0, q = 0; s < N && st == TOMO_OK; s += upd, q++) {
+            const int T = std::min(upd, N - s);
+            for (int k = 0; k < K && st == TOMO_OK; k++) {
+                p->stream = p->rs[k];
+                if (q == 0) CK(cudaStreamWaitEvent(p->stream, ev[0], 0));
+                if (p->profile && k == 0)
+                    CK(cudaEventRecordWithFlags(p->ev[4 * q + 0], p->stream, cudaEventRecordExternal));
+                st = run_fp_range(p, d_ord + s, T, jb[k], jb[k + 1], factor, s);
+                if (p->profile && k == 0)
+                    CK(cudaEventRecordWithFlags(p->ev[4 * q + 1], p->stream, cudaEventRecordExternal));
+                CK(cudaEventRecord(ev[1 + (size_t)q * K + k], p->stream));
+            }
+            for (int k = 0; k < K; k++) CK(cudaStreamWaitEvent(p->rs_reduce, ev[1 + (size_t)q * K + k], 0));
+            CK(launch_reduce_err(p->d_errpart + (size_t)s * g.h, p->d_err + s, T, g.h, p->rs_reduce));
+            for (int k = 0; k < K && st == TOMO_OK; k++) {
+                p->stream = p->rs[k];
+                st = run_bp(p, p->d_diff + (size_t)s * p->npix, d_ord + s, T, yb[k], yb[k + 1], p->meas_has_inf,
+                            true);
+                if (p->profile && k == 0)
+                    CK(cudaEventRecordWithFlags(p->ev[4 * q + 2], p->stream, cudaEventRecordExternal));
+            }
+        }
+        p->stream = main;
+        const size_t j = 1 + (size_t)nsub * K;
+        for (int k = 0; k < K; k++) {
+            CK(cudaEventRecord(ev[j + k], p->rs[k]));
+            CK(cudaStreamWaitEvent(main, ev[j + k], 0));
+        }
+        CK(cudaEventRecord(ev[j + K], p->rs_reduce));
+        CK(cudaStreamWaitEvent(main, ev[j + K], 0));
+        CKS(st);
+        CKS(end_iteration(p));
+        return TOMO_OK;
+    };
     auto body = [&](const int* d_ord) -> tomo_status {
+        if (K > 1) return body_rows(d_ord);
         CKS(start_iteration(p));
         for (int s = 0, k = 0; s < N; s += upd, k++) {
             const int T = std::min(upd, N - s);

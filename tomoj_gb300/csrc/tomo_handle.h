@@ -107,6 +107,12 @@ struct tomo_projector {
     void* bp_target() const { return bayes ? static_cast<void*>(d_dist) : vol(); }
     std::atomic<int> cancel{0};
     int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+    // row streams: K row ranges of an OS-SART iteration run on K streams (rows are
+    // independent), so that forward and backprojections of different rows overlap
+    int row_streams = 1;
+    cudaStream_t rs[4] = {};
+    cudaStream_t rs_reduce = nullptr;
+    std::vector<cudaEvent_t> rs_ev;  // fork, per-(subset, range) forward-done, joins
     int sms = 0;            // multiprocessors of the device
     // forward-projector depth split scratch (partial ray sums, per-group tickets)
     float* d_fppart = nullptr;
