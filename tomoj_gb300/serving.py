@@ -25,6 +25,7 @@ import ctypes as C
 import heapq
 import queue
 import threading
+from concurrent.futures import ThreadPoolExecutor
 import time
 from dataclasses import dataclass, field
 
@@ -77,16 +78,26 @@ class Result:
 
 
 class EngineAdapter:
-    """The engine calls the server needs (a fake with the same methods tests the scheduling on CPU)."""
+    """The engine calls the server needs (a fake with the same methods tests the scheduling on CPU).
 
-    def __init__(self):
+    The active requests iterate as `split` batches (alternate members), each on its own
+    stream and driven from its own host thread, so that one batch's forward projections
+    run beside another's backprojections."""
+
+    def __init__(self, split: int = 2):
         self.lib = _abi.load()
-        b = C.c_void_p()
-        _abi.check(self.lib.tomo_batch_create(C.byref(b)))
-        self.batch = b
+        self.batches = []
+        for _ in range(max(1, split)):
+            b = C.c_void_p()
+            _abi.check(self.lib.tomo_batch_create(C.byref(b)))
+            self.batches.append(b)
+        self.pool = ThreadPoolExecutor(max_workers=len(self.batches)) if len(self.batches) > 1 else None
 
     def close(self):
-        self.lib.tomo_batch_destroy(self.batch)
+        if self.pool is not None:
+            self.pool.shutdown()
+        for b in self.batches:
+            self.lib.tomo_batch_destroy(b)
 
     def create(self, req: Request):
         """Handle with the request's series loaded; None if HBM is short (TOMO_ERR_NOMEM)."""
@@ -120,18 +131,35 @@ class EngineAdapter:
         _abi.check(self.lib.tomo_run_wbp(hd, 0, req.H))
 
     def set_members(self, handles):
-        arr = (C.c_void_p * max(len(handles), 1))(*[h.value for h in handles])
-        _abi.check(self.lib.tomo_batch_set(self.batch, arr, len(handles)))
+        k = len(self.batches)
+        for i, b in enumerate(self.batches):
+            part = handles[i::k]
+            arr = (C.c_void_p * max(len(part), 1))(*[h.value for h in part])
+            _abi.check(self.lib.tomo_batch_set(b, arr, len(part)))
 
     def iterate(self, handles, reqs, iteration):
-        M = len(handles)
+        M, k = len(handles), len(self.batches)
         relax = np.array([r.relax for r in reqs], np.float64)
         upd = np.array([0 if r.kind in (SIRT, TVM) else r.update for r in reqs], np.int32)
         first = np.array([self.lib.tomo_first_index(r.seed, it, len(r.angles)) for r, it in zip(reqs, iteration)],
                          np.int32)
         err = np.zeros((M, 5))
-        _abi.check(self.lib.tomo_batch_iteration(self.batch, _abi.ptr(relax, C.c_double), _abi.ptr(upd, C.c_int32),
-                                                 _abi.ptr(first, C.c_int32), 1, _abi.ptr(err, C.c_double)))
+
+        def run(i):
+            idx = np.arange(i, M, k)
+            if idx.size == 0:
+                return
+            r, u, f = (np.ascontiguousarray(x[idx]) for x in (relax, upd, first))
+            e = np.zeros((idx.size, 5))
+            _abi.check(self.lib.tomo_batch_iteration(self.batches[i], _abi.ptr(r, C.c_double),
+                                                     _abi.ptr(u, C.c_int32), _abi.ptr(f, C.c_int32), 1,
+                                                     _abi.ptr(e, C.c_double)))
+            err[idx] = e
+
+        if self.pool is None:
+            run(0)
+        else:
+            list(self.pool.map(run, range(k)))
         return err
 
     def read_volume(self, hd, req: Request):
