@@ -39,7 +39,7 @@ typedef int32_t tomo_status;
 #define TOMO_ERR_CUDA (-2)        /* CUDA runtime error (message in tomo_last_error) */
 #define TOMO_ERR_NOMEM (-3)       /* admission control: not enough free HBM under the limit */
 #define TOMO_ERR_STATE (-4)       /* call out of order (e.g. backproject with no projection) */
-#define TOMO_ERR_UNSUPPORTED (-5) /* geometry or option not supported by this build */
+#define TOMO_ERR_UNSUPPORTED (-5) /* geometry or option not supported by the engine */
 #define TOMO_ERR_CANCELLED (-6)   /* tomo_cancel() was called */
 #define TOMO_ERR_DEVICE (-7)      /* a kernel reported an error status (bounded wait expired) */
 

@@ -1,6 +1,6 @@
 """FP64 numpy twin of the CPU oracle.
 
-TEST INFRASTRUCTURE ONLY (checker for tests/ and bench.py's precision report).
+TEST INFRASTRUCTURE ONLY (the reference for tests/ and bench.py's precision report).
 
 Same algorithm and quirks as oracle/tomo_oracle.c (which follows the reference's
 float/double operation order), but every value is stored and computed in

@@ -1,7 +1,7 @@
 """ctypes front-end of the C oracle (oracle/tomo_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU legs of bench.py as the checker / CPU baseline, never by the engine.
+CPU legs of bench.py to check the engine and as the CPU baseline, never by the engine.
 
 Parity status: unpinned (the reference ships no golden vectors and cannot be
 run without a JDK); see tomo_oracle.c's header.

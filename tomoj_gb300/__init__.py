@@ -1,1 +1,1 @@
-"""GB300-native projection/backprojection engine for TomoJ."""
+"""GB300-native projection/backprojection engine for TomoJ: the Projector surface on CUDA kernels."""
