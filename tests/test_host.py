@@ -148,3 +148,22 @@ def test_unalign_is_inverse_of_oracle_alignment(oracle_lib):
     shift = np.array([1.0, 0.0, 0.0, 1.0, 2.0, 1.0])  # integer shifts round-trip exactly
     back = O.align(P.unalign(img, shift), shift, fill=O.FILL_NAN)
     assert np.array_equal(back[inner], img[inner])
+
+
+def test_reconstruction_type_codes_follow_the_reference():
+    # ReconstructionParameters.java:13-15, AdvancedReconstructionParameters.java:10-13
+    from tomoj_gb300 import reconstruction as R
+    assert (R.BP, R.WBP, R.OSSART, R.TVM, R.BAYESIAN, R.COMPRESSED_SENSING, R.BGART) == (0, 1, 2, 3, 4, 5, 6)
+
+
+def test_compressed_sensing_projector_is_refused():
+    from tomoj_gb300 import reconstruction as R
+    params = R.ReconstructionParameters.createCompressedSensingParameters(8, 2, 8, 2, 1.0, 0.95, 3, 3.0, 0.0)
+    assert params.reconstructionType == R.COMPRESSED_SENSING and params.updateNb == 0
+    ts = TiltSeries(np.zeros((3, 2, 8), np.float32), np.array([-10.0, 0.0, 10.0]))
+    with pytest.raises(NotImplementedError):
+        params.getProjector(ts, R.TomoReconstruction2(8, 2, 8))
+    p = R.ReconstructionParameters.createBgARTParameters(8, 2, 8, 3, 0.5, 2, 1.5, False, True)
+    assert (p.reconstructionType, p.bgartK, p.bgartMedian, p.bgartDarkBG, p.updateNb) == (R.BGART, 1.5, False, True, 2)
+    b = R.ReconstructionParameters.createBayesianParameters(8, 2, 8, 4, 0.3, 0.02)
+    assert (b.reconstructionType, b.relaxationCoefficient, b.getRegularizationWeight()) == (R.BAYESIAN, 0.3, 0.02)

@@ -16,7 +16,9 @@ import numpy as np
 from . import _abi
 from .projector import Projector, VoxelProjector3D, first_index
 
-BP, WBP, OSSART, TVM = 0, 1, 2, 10
+# ReconstructionParameters (:13-15) and AdvancedReconstructionParameters (:10-13) types
+BP, WBP, OSSART = 0, 1, 2
+TVM, BAYESIAN, COMPRESSED_SENSING, BGART = 3, 4, 5, 6
 
 
 class TomoReconstruction2:
@@ -283,6 +285,9 @@ class ReconstructionParameters:
         # TVM (AdvancedReconstructionParameters)
         self.tvmTheta, self.tvmG, self.tvmDt, self.tvmIterations = 25.0, 1.0, 0.1, 5
         self.regularizationWeight = 0.1
+        # BgART and compressed sensing (AdvancedReconstructionParameters)
+        self.bgartK, self.bgartMedian, self.bgartDarkBG = 0.0, True, True
+        self.waveletPercentageOfZeros, self.waveletType, self.waveletDegree, self.waveletShift = 0.95, 3, 3.0, 0.0
         # volume storage precision (engine option; the reference stores float32)
         self.precision = _abi.PREC_FP32
 
@@ -321,6 +326,48 @@ class ReconstructionParameters:
         p.updateNb = 0
         return p
 
+    @staticmethod
+    def createBayesianParameters(width, height, depth, nbIterations, regularizationAlpha, regularizationWeight):
+        """AdvancedReconstructionParameters.createBayesianParameters (:135-144): the
+        relaxation coefficient carries alpha."""
+        p = ReconstructionParameters(width, height, depth)
+        p.reconstructionType = BAYESIAN
+        p.nbIterations = nbIterations
+        p.relaxationCoefficient = regularizationAlpha
+        p.regularizationWeight = regularizationWeight
+        p.updateNb = 0
+        return p
+
+    @staticmethod
+    def createBgARTParameters(width, height, depth, nbIterations, relaxationCoefficient, updateNb, bgartK,
+                              bgartMedian, bgartDarkBG):
+        """AdvancedReconstructionParameters.createBgARTParameters (:145-156)."""
+        p = ReconstructionParameters(width, height, depth)
+        p.reconstructionType = BGART
+        p.nbIterations = nbIterations
+        p.relaxationCoefficient = relaxationCoefficient
+        p.updateNb = updateNb
+        p.bgartK, p.bgartMedian, p.bgartDarkBG = float(bgartK), bool(bgartMedian), bool(bgartDarkBG)
+        return p
+
+    @staticmethod
+    def createCompressedSensingParameters(width, height, depth, nbIterations, relaxationCoefficient,
+                                          waveletPercentageOfZeros, waveletType, waveletDegree, waveletShift):
+        """AdvancedReconstructionParameters.createCompressedSensingParameters (:157-168); its
+        projector needs the fractional spline wavelet library, which the engine does not
+        provide (getProjector raises)."""
+        p = ReconstructionParameters(width, height, depth)
+        p.reconstructionType = COMPRESSED_SENSING
+        p.nbIterations = nbIterations
+        p.relaxationCoefficient = relaxationCoefficient
+        p.waveletPercentageOfZeros, p.waveletType = waveletPercentageOfZeros, waveletType
+        p.waveletDegree, p.waveletShift = waveletDegree, waveletShift
+        p.updateNb = 0
+        return p
+
+    def getRegularizationWeight(self):
+        return self.regularizationWeight
+
     def getNbIterations(self):
         return self.nbIterations
 
@@ -344,9 +391,29 @@ class ReconstructionParameters:
         self.precision = _abi.precision_code(v)
 
     def getProjector(self, ts, rec) -> VoxelProjector3D:
-        """ReconstructionParameters.getProjector (ReconstructionParameters.java:313-333)."""
+        """ReconstructionParameters.getProjector (ReconstructionParameters.java:313-333) and
+        AdvancedReconstructionParameters.getProjector (AdvancedReconstructionParameters.java:171-221)."""
+        from .projector import BayesianVoxelProjector3D, BgARTVoxelProjector3D
         scale = ts.getWidth() / float(rec.getWidth()) if self.rescaleData else 1.0
-        pos = self.positivityConstraint if self.reconstructionType in (OSSART, TVM) else False
+        kind = self.reconstructionType
+        if kind == COMPRESSED_SENSING:
+            raise NotImplementedError("CompressedSensingProjector needs the fractional spline wavelet library, "
+                                      "which is not part of the engine")
+        if kind == BAYESIAN:
+            proj = BayesianVoxelProjector3D(ts, rec, None, positivity=self.positivityConstraint,
+                                            long_object=self.longObjectCompensation, scale=scale,
+                                            precision=self.precision)
+            proj.setRegularizationAlpha(self.relaxationCoefficient)
+            proj.setRegularizationLambda(self.regularizationWeight)
+            return proj
+        if kind == BGART:
+            # BgARTVoxelProjector3D keeps the projector defaults (no positivity / long object)
+            proj = BgARTVoxelProjector3D(ts, rec, None, self.bgartK, self.bgartDarkBG, self.bgartMedian, scale=scale,
+                                         precision=self.precision)
+            if self.fista:
+                proj.setFista(True)
+            return proj
+        pos = self.positivityConstraint if kind in (OSSART, TVM) else False
         proj = VoxelProjector3D(ts, rec, None, positivity=pos, long_object=self.longObjectCompensation, scale=scale,
                                 precision=self.precision)
         if self.reconstructionType == WBP:
