@@ -196,6 +196,20 @@ tomo_status tomo_set_bayesian(tomo_projector* p, double lambda, double alpha, in
  * FP32 volumes only. */
 tomo_status tomo_set_bgart(tomo_projector* p, double k, int32_t dark_bg, int32_t do_median, double bg_value,
                            int32_t enabled);
+/* CompressedSensingProjector (TomoJ_AdvancedReconstruction/.../projectors/
+ * CompressedSensingProjector.java:34-155; the reference's setters setWaveletType,
+ * setWaveletDegree, setWaveletShift, setSoftThresholdingPercentageOfZeros and
+ * setWaveletsIterations): after every iteration the volume goes through the
+ * separable 3-D fractional spline wavelet transform (wavelet_type 0 orthonormal,
+ * 3 B-spline, 6 dual; degree > -0.5; shift), is soft-thresholded at the level that
+ * zeroes fraction_zeros of the coefficients, and is transformed back.
+ * levels = {x, y, z} transform levels, or NULL for the reference's default (the
+ * same count on every axis, from the width).  Every level's line length must be
+ * even (TOMO_ERR_UNSUPPORTED otherwise).  FP32 volumes only. */
+tomo_status tomo_set_compressed_sensing(tomo_projector* p, int32_t wavelet_type, double degree, double shift,
+                                       double fraction_zeros, const int32_t* levels, int32_t enabled);
+/* The soft threshold of the last wavelet filter (synchronises the handle's stream). */
+tomo_status tomo_compressed_sensing_threshold(tomo_projector* p, double* out);
 
 /* ---- drivers (TomoReconstruction2) --------------------------------------- */
 /* WBP(ts, projector, params, y0, y1) with update 0 (TomoReconstruction2.java:499-538). */

@@ -156,13 +156,12 @@ def test_reconstruction_type_codes_follow_the_reference():
     assert (R.BP, R.WBP, R.OSSART, R.TVM, R.BAYESIAN, R.COMPRESSED_SENSING, R.BGART) == (0, 1, 2, 3, 4, 5, 6)
 
 
-def test_compressed_sensing_projector_is_refused():
+def test_advanced_parameter_factories_fill_their_fields():
     from tomoj_gb300 import reconstruction as R
-    params = R.ReconstructionParameters.createCompressedSensingParameters(8, 2, 8, 2, 1.0, 0.95, 3, 3.0, 0.0)
+    params = R.ReconstructionParameters.createCompressedSensingParameters(8, 2, 8, 2, 1.0, 0.9, 0, 2.0, 0.25)
     assert params.reconstructionType == R.COMPRESSED_SENSING and params.updateNb == 0
-    ts = TiltSeries(np.zeros((3, 2, 8), np.float32), np.array([-10.0, 0.0, 10.0]))
-    with pytest.raises(NotImplementedError):
-        params.getProjector(ts, R.TomoReconstruction2(8, 2, 8))
+    assert (params.waveletPercentageOfZeros, params.waveletType, params.waveletDegree, params.waveletShift) == \
+        (0.9, 0, 2.0, 0.25)
     p = R.ReconstructionParameters.createBgARTParameters(8, 2, 8, 3, 0.5, 2, 1.5, False, True)
     assert (p.reconstructionType, p.bgartK, p.bgartMedian, p.bgartDarkBG, p.updateNb) == (R.BGART, 1.5, False, True, 2)
     b = R.ReconstructionParameters.createBayesianParameters(8, 2, 8, 4, 0.3, 0.02)

@@ -100,6 +100,9 @@ SIGNATURES = {
     "tomo_set_fista": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_bayesian": (C.c_int32, [_P, C.c_double, C.c_double, C.c_int32]),
     "tomo_set_bgart": (C.c_int32, [_P, C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_int32]),
+    "tomo_set_compressed_sensing": (C.c_int32, [_P, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                                C.POINTER(C.c_int32), C.c_int32]),
+    "tomo_compressed_sensing_threshold": (C.c_int32, [_P, _f64p]),
     "tomo_run_wbp": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "tomo_run_ossart": (C.c_int32, [_P, C.c_int32, C.c_double, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
                                     C.c_int32, _f64p]),

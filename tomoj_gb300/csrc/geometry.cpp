@@ -340,6 +340,8 @@ void fft_host(std::vector<double>& re, std::vector<double>& im) {
 
 }  // namespace
 
+void fft_host_forward(std::vector<double>& re, std::vector<double>& im) { fft_host(re, im); }
+
 // The row filter of a non-power-of-two width as a convolution: h[n] = (1/w) sum_k
 // mask[k] e^{2 pi i k n / w} (real for the even masks used here; the real part is
 // kept), zero-padded to M points and transformed by an M-point radix-2 FFT in double.

@@ -461,6 +461,7 @@ tomo_status end_iteration(tomo_projector* p) {
     if (p->bgart)
         CK(launch_bgart_collapse(p->d_vol, p->nvox, p->bg_k, p->bg_dark, p->bg_value, p->d_bgscratch, p->stream));
     CKS(tv_denoise(p));
+    if (p->cs) CK(launch_wavelet_filter(p->wav, p->d_vol, p->stream));
     if (p->fista) {
         const double t_1 = p->fista_t;
         p->fista_t = (1 + std::sqrt(1 + 4 * p->fista_t * p->fista_t)) / 2;
@@ -645,6 +646,7 @@ tomo_status tomo_destroy(tomo_projector* p) {
         if (q) cudaStreamDestroy(q);
     if (p->rs_reduce) cudaStreamDestroy(p->rs_reduce);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
+    if (p->wav) wavelet_plan_destroy(p->wav);
     delete p;
     return TOMO_OK;
 }
@@ -1299,6 +1301,64 @@ tomo_status tomo_set_bgart(tomo_projector* p, double k, int32_t dark_bg, int32_t
         CK(launch_bgart_collapse(p->d_vol, p->nvox, k, p->bg_dark, bg_value, p->d_bgscratch, p->stream));
         CK(cudaStreamSynchronize(p->stream));
     }
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_compressed_sensing(tomo_projector* p, int32_t wavelet_type, double degree, double shift,
+                                       double fraction_zeros, const int32_t* levels, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    if (!enabled) {
+        p->cs = false;
+        return TOMO_OK;
+    }
+    if (p->vtype != kVolF32)
+        return fail(TOMO_ERR_UNSUPPORTED, "the wavelet filter needs the FP32 volume (precision TOMO_PREC_FP32)");
+    const Geometry& g = p->g;
+    int it[3];
+    if (levels) {
+        for (int a = 0; a < 3; a++) it[a] = levels[a];
+    } else {
+        // findBestWaveletsIteration (CompressedSensingProjector.java:127-151): every axis
+        // from the width
+        int n = 1;
+        for (long long s = 64; s < g.W; s *= 2) n++;
+        it[0] = it[1] = it[2] = n;
+    }
+    const char* why = nullptr;
+    WaveletPlan* plan = wavelet_plan_create(g.W, g.H, g.D, it, wavelet_type, degree, shift, fraction_zeros, &why);
+    if (!plan) {
+        const bool sizes = std::strstr(why, "levels") != nullptr;
+        return fail(sizes ? TOMO_ERR_UNSUPPORTED : TOMO_ERR_INVALID, why);
+    }
+    CK(cudaStreamSynchronize(p->stream));
+    const size_t tb = wavelet_plan_table_bytes(plan);
+    tomo_status st = TOMO_OK;
+    if (!p->d_wbuf) st = alloc_n(p, &p->d_wbuf, p->nvox);
+    if (st == TOMO_OK && !p->d_wstate) st = dalloc(p, &p->d_wstate, wavelet_plan_state_bytes());
+    if (st == TOMO_OK && p->d_wtab && p->wtab_bytes < tb) free_n(p, reinterpret_cast<char**>(&p->d_wtab), p->wtab_bytes);
+    if (st == TOMO_OK && !p->d_wtab) {
+        st = dalloc(p, &p->d_wtab, tb);
+        if (st == TOMO_OK) p->wtab_bytes = tb;
+    }
+    if (st != TOMO_OK) {
+        wavelet_plan_destroy(plan);
+        return st;
+    }
+    cudaError_t e = wavelet_plan_bind(plan, p->d_wtab, p->d_wbuf, p->d_wstate, p->stream);
+    if (e != cudaSuccess) {
+        wavelet_plan_destroy(plan);
+        CK(e);
+    }
+    if (p->wav) wavelet_plan_destroy(p->wav);
+    p->wav = plan;
+    p->cs = true;
+    return TOMO_OK;
+}
+
+tomo_status tomo_compressed_sensing_threshold(tomo_projector* p, double* out) {
+    if (!p || !out) return fail(TOMO_ERR_INVALID, "null argument");
+    if (!p->wav) return fail(TOMO_ERR_STATE, "no wavelet filter set (tomo_set_compressed_sensing)");
+    CK(wavelet_read_threshold(p->wav, out, p->stream));
     return TOMO_OK;
 }
 

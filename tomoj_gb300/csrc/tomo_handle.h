@@ -103,6 +103,13 @@ struct tomo_projector {
     int bg_dark = 1, bg_median = 1;
     void* d_bgscratch = nullptr;
     float* d_bgtmp = nullptr;
+    // CompressedSensingProjector: wavelet soft threshold after every iteration
+    bool cs = false;
+    tomo::WaveletPlan* wav = nullptr;
+    double* d_wbuf = nullptr;
+    void* d_wtab = nullptr;
+    size_t wtab_bytes = 0;
+    void* d_wstate = nullptr;
     // volume a backprojection of differences adds to
     void* bp_target() const { return bayes ? static_cast<void*>(d_dist) : vol(); }
     std::atomic<int> cancel{0};

@@ -12,6 +12,7 @@
 #pragma once
 #include <atomic>
 #include <functional>
+#include <vector>
 #include <cstddef>
 #include <cstdint>
 
@@ -94,6 +95,8 @@ void order_shuffle(int n, const double* euler, int first, int* out);
 // fn(begin, end) over [0, n) split into contiguous ranges on up to 16 host threads,
 // at least min_per_thread items each (the calling thread takes the first range).
 void parallel_ranges(int n, int min_per_thread, const std::function<void(int, int)>& fn);
+// In-place radix-2 FFT in double (forward, e^{-2 pi i kn/M}); M a power of two.
+void fft_host_forward(std::vector<double>& re, std::vector<double>& im);
 int first_index(uint64_t seed, int iteration, int nproj);
 void weighting_row_filter(int kind, int w, int nproj, const double* sint, const double* tilts_deg, double diameter,
                           float* mask_row);
@@ -278,6 +281,24 @@ constexpr size_t kBgScratchBytes = 16 + 256 * 8 + 3 * 8;
 cudaError_t launch_bgart_collapse(float* vol, size_t n, double k, int dark_bg, double bg_value, void* scratch,
                                   cudaStream_t s);
 cudaError_t launch_bgart_median(float* vol, float* tmp, int W, int H, int D, cudaStream_t s);
+
+// Compressed sensing (CompressedSensingProjector.endOfIteration, kernels_wavelet.cu): FP64
+// separable fractional spline wavelet transform of the volume, soft threshold at the level
+// that zeroes the requested fraction of coefficients, inverse transform, back into the FP32
+// volume.  The threshold search runs kWaveletThresholdPasses histogram rounds at most.
+constexpr int kWaveletThresholdPasses = 16;
+struct WaveletPlan;
+// nullptr (with *why) when the parameters or sizes are not supported
+WaveletPlan* wavelet_plan_create(int W, int H, int D, const int iters[3], int type, double alpha, double tau,
+                                 double fraction_zeros, const char** why);
+size_t wavelet_plan_table_bytes(const WaveletPlan* P);
+size_t wavelet_plan_state_bytes();
+// uploads the tables into d_tables (wavelet_plan_table_bytes) and binds the FP64 buffer
+// (W * H * D doubles) and the state (wavelet_plan_state_bytes)
+cudaError_t wavelet_plan_bind(WaveletPlan* P, void* d_tables, double* d_buf, void* d_state, cudaStream_t s);
+void wavelet_plan_destroy(WaveletPlan* P);
+cudaError_t launch_wavelet_filter(const WaveletPlan* P, float* vol, cudaStream_t s);
+cudaError_t wavelet_read_threshold(const WaveletPlan* P, double* out, cudaStream_t s);
 
 // Reduced-precision volume storage (kernels_vol.cu).  `src`/`dst` float buffers are
 // laid out [D][rows][W] and cover volume rows [y0, y0 + rows).

@@ -310,6 +310,83 @@ class BgARTVoxelProjector3D(VoxelProjector3D):
         check(self._lib.tomo_set_bgart(self._h, self.k, int(self.darkBG), int(self.doMedian), self.bgValue, 1))
 
 
+class CompressedSensingProjector(VoxelProjector3D):
+    """CompressedSensingProjector (TomoJ_AdvancedReconstruction/.../projectors/
+    CompressedSensingProjector.java:16-201): after every iteration the volume goes through
+    the separable 3-D fractional spline wavelet transform, is soft-thresholded at the level
+    that zeroes softThresholdingPercentageOfZeros of the coefficients and is transformed
+    back.  The wavelet filters are restated from the published fractional spline wavelets
+    (the reference calls a third-party library for them)."""
+
+    WAVELET_ORTHONORMAL, WAVELET_BSPLINE, WAVELET_DUAL = 0, 3, 6
+
+    def __init__(self, ts, rec, weighting=None, **kw):
+        super().__init__(ts, rec, weighting, **kw)
+        self.waveletDegree = 3.0
+        self.waveletShift = 0.0
+        self.waveletType = self.WAVELET_BSPLINE
+        self.softThresholdingPercentageOfZeros = 0.95
+        self.iters = self.findBestWaveletsIteration(rec)
+        self._apply()
+
+    @staticmethod
+    def findBestWaveletsIteration(rec):
+        """CompressedSensingProjector.java:127-151: levels from 64 doubling up to the width,
+        the same count on all three axes (the reference sizes every axis from the width)."""
+        n, s = 1, 64
+        while s < rec.getWidth():
+            s *= 2
+            n += 1
+        return [n, n, n]
+
+    def _apply(self):
+        lv = (C.c_int32 * 3)(*[int(v) for v in self.iters])
+        check(self._lib.tomo_set_compressed_sensing(self._h, int(self.waveletType), float(self.waveletDegree),
+                                                    float(self.waveletShift),
+                                                    float(self.softThresholdingPercentageOfZeros), lv, 1))
+
+    def getLastThreshold(self) -> float:
+        """The soft threshold of the last end-of-iteration filter."""
+        out = C.c_double()
+        check(self._lib.tomo_compressed_sensing_threshold(self._h, C.byref(out)))
+        return out.value
+
+    def getWaveletDegree(self):
+        return self.waveletDegree
+
+    def setWaveletDegree(self, v):
+        self.waveletDegree = float(v)
+        self._apply()
+
+    def getWaveletShift(self):
+        return self.waveletShift
+
+    def setWaveletShift(self, v):
+        self.waveletShift = float(v)
+        self._apply()
+
+    def getWaveletType(self):
+        return self.waveletType
+
+    def setWaveletType(self, v):
+        self.waveletType = int(v)
+        self._apply()
+
+    def getSoftThresholdingPercentageOfZeros(self):
+        return self.softThresholdingPercentageOfZeros
+
+    def setSoftThresholdingPercentageOfZeros(self, v):
+        self.softThresholdingPercentageOfZeros = float(v)
+        self._apply()
+
+    def getWaveletsIterations(self):
+        return list(self.iters)
+
+    def setWaveletsIterations(self, x, y=None, z=None):
+        self.iters = list(x) if y is None else [int(x), int(y), int(z)]
+        self._apply()
+
+
 def first_index(seed: int, iteration: int, nproj: int) -> int:
     """Deterministic replacement of orderShuffleART's Math.random() first index."""
     return int(_abi.load().tomo_first_index(int(seed), int(iteration), int(nproj)))

@@ -353,9 +353,7 @@ class ReconstructionParameters:
     @staticmethod
     def createCompressedSensingParameters(width, height, depth, nbIterations, relaxationCoefficient,
                                           waveletPercentageOfZeros, waveletType, waveletDegree, waveletShift):
-        """AdvancedReconstructionParameters.createCompressedSensingParameters (:157-168); its
-        projector needs the fractional spline wavelet library, which the engine does not
-        provide (getProjector raises)."""
+        """AdvancedReconstructionParameters.createCompressedSensingParameters (:157-168)."""
         p = ReconstructionParameters(width, height, depth)
         p.reconstructionType = COMPRESSED_SENSING
         p.nbIterations = nbIterations
@@ -393,12 +391,19 @@ class ReconstructionParameters:
     def getProjector(self, ts, rec) -> VoxelProjector3D:
         """ReconstructionParameters.getProjector (ReconstructionParameters.java:313-333) and
         AdvancedReconstructionParameters.getProjector (AdvancedReconstructionParameters.java:171-221)."""
-        from .projector import BayesianVoxelProjector3D, BgARTVoxelProjector3D
+        from .projector import BayesianVoxelProjector3D, BgARTVoxelProjector3D, CompressedSensingProjector
         scale = ts.getWidth() / float(rec.getWidth()) if self.rescaleData else 1.0
         kind = self.reconstructionType
         if kind == COMPRESSED_SENSING:
-            raise NotImplementedError("CompressedSensingProjector needs the fractional spline wavelet library, "
-                                      "which is not part of the engine")
+            # CompressedSensingProjector keeps the projector defaults (no positivity / long object)
+            proj = CompressedSensingProjector(ts, rec, None, scale=scale, precision=self.precision)
+            proj.waveletType, proj.waveletDegree = int(self.waveletType), float(self.waveletDegree)
+            proj.waveletShift = float(self.waveletShift)
+            proj.softThresholdingPercentageOfZeros = float(self.waveletPercentageOfZeros)
+            proj._apply()
+            if self.fista:
+                proj.setFista(True)
+            return proj
         if kind == BAYESIAN:
             proj = BayesianVoxelProjector3D(ts, rec, None, positivity=self.positivityConstraint,
                                             long_object=self.longObjectCompensation, scale=scale,
