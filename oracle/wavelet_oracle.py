@@ -16,7 +16,8 @@ T. Blu, "Fractional splines and wavelets", SIAM Review 42(1), 2000; T. Blu and M
 * refinement filter of the (alpha, tau) fractional B-spline, for w in (-pi, pi]:
   H(w) = sqrt(2) |cos(w/2)|^(alpha+1) exp(-i tau w);
 * autocorrelation A(w) = |2 sin(w/2)|^(2 alpha+2) sum_k |w + 2 pi k|^-(2 alpha+2)
-  (A(0) = 1), summed over |k| <= 256 with an integral estimate of the tail;
+  (A(0) = 1), summed over |k| <= 256 with the tail from its integral and the first
+  Euler-Maclaurin correction;
 * ORTHONORMAL (type 0): analysis = synthesis, Ho(w) = H(w) sqrt(A(w) / A(2w)),
   Go(w) = exp(-i w) conj(Ho(w + pi));
 * BSPLINE (type 3): synthesis H and G(w) = exp(-i w) conj(H(w + pi)) A(w + pi);
@@ -48,9 +49,11 @@ def autocorrelation(w: np.ndarray, alpha: float) -> np.ndarray:
     wn = w[nz]
     k = np.arange(1, _TAIL_K + 1, dtype=np.float64)[:, None]
     s = np.abs(wn) ** -p + np.sum(np.abs(wn + 2 * np.pi * k) ** -p + np.abs(wn - 2 * np.pi * k) ** -p, axis=0)
-    # tail sum_{k > K} |w +- 2 pi k|^-p ~ integral from K + 1/2
+    # tail sum_{k > K} f(k), f(t) = |w +- 2 pi t|^-p: integral from K + 1/2 plus the
+    # midpoint-rule Euler-Maclaurin term f'(K + 1/2) / 24
     a = 2 * np.pi * (_TAIL_K + 0.5)
     s += ((a + wn) ** (1 - p) + (a - wn) ** (1 - p)) / (2 * np.pi * (p - 1))
+    s -= 2 * np.pi * p / 24 * ((a + wn) ** (-p - 1) + (a - wn) ** (-p - 1))
     out[nz] = np.abs(2 * np.sin(wn / 2)) ** p * s
     return out
 

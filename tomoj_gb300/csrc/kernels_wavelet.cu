@@ -8,7 +8,8 @@
 // Filters: the published fractional spline wavelets of Unser and Blu, the third-party
 // library the reference calls (Fractional_Splines_Wavelets 1.0).  H(w) = sqrt(2)
 // |cos(w/2)|^(alpha+1) exp(-i tau w) on (-pi, pi]; A(w) = |2 sin(w/2)|^(2 alpha+2)
-// sum_k |w + 2 pi k|^-(2 alpha+2) (|k| <= 256 plus an integral estimate of the tail).
+// sum_k |w + 2 pi k|^-(2 alpha+2) (|k| <= 256, the tail from its integral and the first
+// Euler-Maclaurin correction).
 // Orthonormal: Ho = H sqrt(A(w)/A(2w)), Go = e^{-iw} conj(Ho(w+pi)); B-spline: synthesis
 // H, e^{-iw} conj(H(w+pi)) A(w+pi), analysis H A(w)/A(2w), e^{-iw} conj(H(w+pi))/A(2w);
 // dual: the B-spline pair exchanged.  All filter values are computed on the host in
@@ -275,8 +276,10 @@ double autocorr(double w, double alpha) {
     double s = std::pow(std::fabs(w), -p);
     for (int k = 1; k <= kWavTailK; k++)
         s += std::pow(std::fabs(w + 2.0 * M_PI * k), -p) + std::pow(std::fabs(w - 2.0 * M_PI * k), -p);
+    // the tail k > K: integral from K + 1/2 plus the midpoint-rule Euler-Maclaurin term
     const double a = 2.0 * M_PI * (kWavTailK + 0.5);
     s += (std::pow(a + w, 1.0 - p) + std::pow(a - w, 1.0 - p)) / (2.0 * M_PI * (p - 1.0));
+    s -= 2.0 * M_PI * p / 24.0 * (std::pow(a + w, -p - 1.0) + std::pow(a - w, -p - 1.0));
     return std::pow(std::fabs(2.0 * std::sin(w / 2.0)), p) * s;
 }
 
