@@ -15,7 +15,7 @@
 // dual: the B-spline pair exchanged.  All filter values are computed on the host in
 // double; the device does only FFTs (radix 2, Bluestein for other lengths) and products.
 //
-// A level along an axis of length n runs one CTA per pair of lines: DFT_n, the two analysis
+// A level along an axis of length n runs a group of threads per pair of lines: DFT_n, the two analysis
 // products folded to n/2 frequencies, two inverse DFT_{n/2} into [low | high].  The
 // synthesis inverts it.  Levels act on the low-pass corner: x, y, z forward and z, y, x
 // backward.  The threshold search runs on the device (fixed number of histogram passes,
@@ -56,7 +56,9 @@ struct WavDft {
 struct WavLines {
     double* buf;
     int n;
-    int nu;
+    int nu, nv;
+    int groups;  // line pairs per CTA (a power of two; blockDim.x / groups threads each)
+    int stride;  // shared-memory entries per group: n + Bluestein scratch
     long long es, su, sv;  // element stride along a line, strides of the line indices u, v
     WavDft full, half;
     const double2* lo;  // analysis: conj(filter) / 2; synthesis: filter
@@ -70,10 +72,16 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
+// The threads of one line pair: index within the group, group size.  Every group of a CTA
+// runs the same lengths, so the barriers below are reached by all threads together.
+struct Grp {
+    int t, nt;
+};
+
 // In-place radix-2 DFT of s[0, n) (natural order in and out), n = 2^logn >= 2, unnormalised;
 // inverse uses e^{+2 pi i kn/n}.  Ends with a barrier.
-__device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict__ tw, bool inverse) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+__device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict__ tw, bool inverse, Grp g) {
+    for (int k = g.t; k < n; k += g.nt) {
         const int r = (int)(__brev((unsigned)k) >> (32 - logn));
         if (k < r) {
             const double2 t = s[k];
@@ -85,7 +93,7 @@ __device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict_
     for (int lg = 1; lg <= logn; lg++) {
         const int half = 1 << (lg - 1);
         const int step = kWavTwN >> lg;
-        for (int j = threadIdx.x; j < (n >> 1); j += blockDim.x) {
+        for (int j = g.t; j < (n >> 1); j += g.nt) {
             const int pos = j & (half - 1);
             const int i0 = ((j >> (lg - 1)) << lg) + pos;
             double2 w = tw[pos * step];
@@ -100,22 +108,23 @@ __device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict_
 }
 
 // DFT of x[0, n) in place (a: Bluestein scratch of P.M entries); unnormalised.
-__device__ void dft_any(double2* x, double2* a, const WavDft& P, const double2* __restrict__ tw, bool inverse) {
+__device__ void dft_any(double2* x, double2* a, const WavDft& P, const double2* __restrict__ tw, bool inverse,
+                        Grp g) {
     if (P.n <= 1) return;
     if (P.logn >= 0) {
-        fft_pow2(x, P.n, P.logn, tw, inverse);
+        fft_pow2(x, P.n, P.logn, tw, inverse, g);
         return;
     }
     // inverse DFT = conj(DFT(conj(x)))
     const double cs = inverse ? -1.0 : 1.0;
-    for (int k = threadIdx.x; k < P.M; k += blockDim.x)
+    for (int k = g.t; k < P.M; k += g.nt)
         a[k] = k < P.n ? cmul(make_double2(x[k].x, cs * x[k].y), P.chirp[k]) : make_double2(0.0, 0.0);
     __syncthreads();
-    fft_pow2(a, P.M, P.logM, tw, false);
-    for (int k = threadIdx.x; k < P.M; k += blockDim.x) a[k] = cmul(a[k], P.bspec[k]);
+    fft_pow2(a, P.M, P.logM, tw, false, g);
+    for (int k = g.t; k < P.M; k += g.nt) a[k] = cmul(a[k], P.bspec[k]);
     __syncthreads();
-    fft_pow2(a, P.M, P.logM, tw, true);
-    for (int k = threadIdx.x; k < P.n; k += blockDim.x) {
+    fft_pow2(a, P.M, P.logM, tw, true, g);
+    for (int k = g.t; k < P.n; k += g.nt) {
         const double2 v = cmul(a[k], P.chirp[k]);
         x[k] = make_double2(v.x, cs * v.y);
     }
@@ -130,43 +139,51 @@ __device__ void dft_any(double2* x, double2* a, const WavDft& P, const double2* 
 template <bool SYN>
 __global__ void __launch_bounds__(kWavThreads) wav_lines_kernel(const WavLines L) {
     extern __shared__ double2 wsm[];
-    double2* x = wsm;
-    double2* a = wsm + L.n;
+    const int nt = blockDim.x / L.groups;
+    const int gi = threadIdx.x / nt;
+    const Grp g{(int)threadIdx.x - gi * nt, nt};
+    double2* x = wsm + (size_t)gi * L.stride;
+    double2* a = x + L.n;
     const int npair = (L.nu + 1) >> 1;
-    const int u0 = 2 * (int)(blockIdx.x % (unsigned)npair);
+    // pair index over (u pairs, v); a group past the end computes on zeros and stores nothing
+    const long long pidx = (long long)blockIdx.x * L.groups + gi;
+    const bool live = pidx < (long long)npair * L.nv;
+    const int u0 = live ? 2 * (int)(pidx % npair) : 0;
     const int u1 = u0 + 1 < L.nu ? u0 + 1 : u0;
-    const int v = (int)(blockIdx.x / (unsigned)npair);
+    const int v = live ? (int)(pidx / npair) : 0;
     double* line0 = L.buf + (long long)u0 * L.su + (long long)v * L.sv;
     double* line1 = L.buf + (long long)u1 * L.su + (long long)v * L.sv;
     const int n = L.n, m = n >> 1;
-    for (int j = threadIdx.x; j < n; j += blockDim.x)
-        x[j] = make_double2(line0[(long long)j * L.es], u1 != u0 ? line1[(long long)j * L.es] : 0.0);
+    for (int j = g.t; j < n; j += g.nt)
+        x[j] = live ? make_double2(line0[(long long)j * L.es], u1 != u0 ? line1[(long long)j * L.es] : 0.0)
+                    : make_double2(0.0, 0.0);
     __syncthreads();
     double scale;
     if (!SYN) {
-        dft_any(x, a, L.full, L.tw, false);
-        for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        dft_any(x, a, L.full, L.tw, false, g);
+        for (int k = g.t; k < m; k += g.nt) {
             const double2 x0 = x[k], x1 = x[k + m];
             x[k] = cadd(cmul(x0, L.lo[k]), cmul(x1, L.lo[k + m]));
             x[k + m] = cadd(cmul(x0, L.hi[k]), cmul(x1, L.hi[k + m]));
         }
         __syncthreads();
-        dft_any(x, a, L.half, L.tw, true);
-        dft_any(x + m, a, L.half, L.tw, true);
+        dft_any(x, a, L.half, L.tw, true, g);
+        dft_any(x + m, a, L.half, L.tw, true, g);
         scale = 1.0 / m;
     } else {
-        dft_any(x, a, L.half, L.tw, false);
-        dft_any(x + m, a, L.half, L.tw, false);
-        for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        dft_any(x, a, L.half, L.tw, false, g);
+        dft_any(x + m, a, L.half, L.tw, false, g);
+        for (int k = g.t; k < m; k += g.nt) {
             const double2 c = x[k], d = x[k + m];
             x[k] = cadd(cmul(c, L.lo[k]), cmul(d, L.hi[k]));
             x[k + m] = cadd(cmul(c, L.lo[k + m]), cmul(d, L.hi[k + m]));
         }
         __syncthreads();
-        dft_any(x, a, L.full, L.tw, true);
+        dft_any(x, a, L.full, L.tw, true, g);
         scale = 1.0 / n;
     }
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    if (!live) return;
+    for (int j = g.t; j < n; j += g.nt) {
         line0[(long long)j * L.es] = x[j].x * scale;
         if (u1 != u0) line1[(long long)j * L.es] = x[j].y * scale;
     }
@@ -305,6 +322,7 @@ struct WaveletPlan {
         long long es = 0, su = 0, sv = 0;
         Dft full, half;
         size_t lo = 0, hi = 0;
+        int groups = 1, stride = 0;
         size_t smem = 0;
     };
     int W = 0, H = 0, D = 0;
@@ -452,7 +470,11 @@ WaveletPlan* wavelet_plan_create(int W, int H, int D, const int iters[3], int ty
         q.full = make_dft(*P, cache, q.n);
         q.half = make_dft(*P, cache, q.n / 2);
         make_filters(*P, q.n, type, alpha, tau, syn, q.lo, q.hi);
-        q.smem = sizeof(double2) * ((size_t)q.n + std::max(dft_scratch(q.full), dft_scratch(q.half)));
+        // enough line pairs per CTA that a butterfly stage has work for every thread
+        q.groups = 1;
+        while (q.groups < 32 && (long long)q.groups * q.n < 2 * kWavThreads) q.groups <<= 1;
+        q.stride = q.n + (int)std::max(dft_scratch(q.full), dft_scratch(q.half));
+        q.smem = sizeof(double2) * (size_t)q.groups * q.stride;
         P->smem_max = std::max(P->smem_max, q.smem);
         P->passes.push_back(q);
     };
@@ -519,6 +541,9 @@ cudaError_t launch_wavelet_filter(const WaveletPlan* P, float* vol, cudaStream_t
         L.buf = P->d_buf;
         L.n = q.n;
         L.nu = q.nu;
+        L.nv = q.nv;
+        L.groups = q.groups;
+        L.stride = q.stride;
         L.es = q.es;
         L.su = q.su;
         L.sv = q.sv;
@@ -527,7 +552,8 @@ cudaError_t launch_wavelet_filter(const WaveletPlan* P, float* vol, cudaStream_t
         L.lo = P->d_tables + q.lo;
         L.hi = P->d_tables + q.hi;
         L.tw = P->d_tables;
-        const unsigned grid = (unsigned)((long long)((q.nu + 1) / 2) * q.nv);
+        const long long pairs = (long long)((q.nu + 1) / 2) * q.nv;
+        const unsigned grid = (unsigned)((pairs + q.groups - 1) / q.groups);
         if (q.syn)
             wav_lines_kernel<true><<<grid, kWavThreads, q.smem, s>>>(L);
         else
