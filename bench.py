@@ -357,6 +357,28 @@ def run_engine(args, wl):
                    "voxel_updates_per_s": updates_per_step * args.steps / (rms / 1000.0),
                    "speedup_vs_one_stream": (ms / args.steps) / (rms / args.steps)}
 
+    # ---- the compressed-sensing end-of-iteration filter on the same volume (FP64 wavelet
+    # transform, threshold search, soft threshold, inverse; default levels from the width) ----
+    cs_leg = None
+    if not args.no_extra:
+        _abi.check(lib.tomo_set_compressed_sensing(h, 3, 3.0, 0.0, 0.95, None, 1))
+        _abi.check(lib.tomo_end_iteration(h))
+        ca, cb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 3
+        ca.record(stream)
+        for _ in range(reps):
+            _abi.check(lib.tomo_end_iteration(h))
+        cb.record(stream)
+        torch.cuda.synchronize()
+        cms = ca.elapsed_time(cb) / reps
+        _abi.check(lib.tomo_set_compressed_sensing(h, 0, 0.0, 0.0, 0.0, None, 0))
+        levels = 1
+        while 64 << (levels - 1) < W:
+            levels += 1
+        cs_leg = {"wavelet": "B-spline, degree 3", "levels": [levels] * 3, "fraction_zeros": 0.95,
+                  "ms_per_filter": cms, "voxels_per_s": nvox / (cms / 1000.0),
+                  "vs_one_plain_iteration": cms / (ms / args.steps / (1 + wl["n_iter"]))}
+
     # ---- roofline of the dominant kernel ----
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
@@ -437,7 +459,7 @@ def run_engine(args, wl):
             "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps, "phases_s": phase},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-            "row_streams": row_leg, "batched": batched, "serving": serving, "precision": precision,
+            "row_streams": row_leg, "compressed_sensing": cs_leg, "batched": batched, "serving": serving, "precision": precision,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)
