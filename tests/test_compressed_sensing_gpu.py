@@ -112,3 +112,26 @@ def test_compressed_sensing_refusals(engine):
         assert set_cs(engine, hb, 3, 3.0, 0.0, 0.9, None) == _abi.ERR_UNSUPPORTED
     finally:
         engine.tomo_destroy(hb)
+
+
+def test_long_lines_and_a_second_handle(engine):
+    # 3072-voxel lines (Bluestein over 8192 points: 180 KB of shared memory per CTA), then a
+    # handle with short lines is set up before the first filters again
+    W, H, D = 3072, 2, 4
+    vol = np.random.default_rng(8).standard_normal((D, H, W)).astype(np.float32)
+    big = handle(engine, W, H, D)
+    small = handle(engine, 32, 6, 20)
+    try:
+        _abi.check(engine.tomo_set_volume(big, vol.ctypes.data, 0, 0, H))
+        _abi.check(set_cs(engine, big, WO.ORTHONORMAL, 3.0, 0.0, 0.9, (1, 1, 1)))
+        _abi.check(set_cs(engine, small, WO.BSPLINE, 3.0, 0.0, 0.9, None))
+        _abi.check(engine.tomo_end_iteration(small))
+        _abi.check(engine.tomo_end_iteration(big))
+        got = np.empty_like(vol)
+        _abi.check(engine.tomo_get_volume(big, got.ctypes.data, 0, 0, H))
+    finally:
+        engine.tomo_destroy(small)
+        engine.tomo_destroy(big)
+    ref = vol.copy()
+    WO.cs_filter(ref, 0.9, WO.ORTHONORMAL, 3.0, 0.0, (1, 1, 1))
+    assert rel_l2(got, ref) <= 1e-6, rel_l2(got, ref)

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "tomo_internal.h"
@@ -504,13 +505,20 @@ cudaError_t wavelet_plan_bind(WaveletPlan* P, void* d_tables, double* d_buf, voi
     P->d_state = static_cast<WavState*>(d_state);
     cudaError_t e = cudaMemcpyAsync(d_tables, P->tables.data(), wavelet_plan_table_bytes(P), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
-    if (P->smem_max > 48 * 1024) {
-        e = cudaFuncSetAttribute(wav_lines_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)P->smem_max);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(wav_lines_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)P->smem_max);
-        if (e != cudaSuccess) return e;
+    {
+        // the limit is per kernel, shared by every handle: only ever raised
+        static std::mutex mu;
+        static size_t attr = 48 * 1024;
+        std::lock_guard<std::mutex> lock(mu);
+        if (P->smem_max > attr) {
+            e = cudaFuncSetAttribute(wav_lines_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)P->smem_max);
+            if (e != cudaSuccess) return e;
+            e = cudaFuncSetAttribute(wav_lines_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)P->smem_max);
+            if (e != cudaSuccess) return e;
+            attr = P->smem_max;
+        }
     }
     return cudaStreamSynchronize(s);
 }
