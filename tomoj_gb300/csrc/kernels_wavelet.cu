@@ -97,10 +97,18 @@ __device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict_
         for (int j = g.t; j < (n >> 1); j += g.nt) {
             const int pos = j & (half - 1);
             const int i0 = ((j >> (lg - 1)) << lg) + pos;
-            double2 w = tw[pos * step];
-            if (inverse) w.y = -w.y;
             const double2 a = s[i0];
-            const double2 b = cmul(s[i0 + half], w);
+            double2 b = s[i0 + half];
+            if (pos != 0) {
+                if (lg == 2) {
+                    // twiddle -i (forward) or +i (inverse): a swap and a sign
+                    b = inverse ? make_double2(-b.y, b.x) : make_double2(b.y, -b.x);
+                } else {
+                    double2 w = tw[pos * step];
+                    if (inverse) w.y = -w.y;
+                    b = cmul(b, w);
+                }
+            }
             s[i0] = cadd(a, b);
             s[i0 + half] = csub(a, b);
         }
