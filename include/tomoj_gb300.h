@@ -92,6 +92,9 @@ const char* tomo_last_error(void);
  * (admission control; 0 = no limit besides free HBM). */
 tomo_status tomo_set_memory_limit(uint64_t bytes);
 uint64_t tomo_memory_in_use(void);
+/* Free and total bytes of the current device (ProjectorGPU.computeMaximumSizeForVolume
+ * sizes a volume from them, ProjectorGPU.java:162-166). */
+tomo_status tomo_device_memory(uint64_t* free_bytes, uint64_t* total_bytes);
 /* Number of kernels this library launched since load (all handles). */
 uint64_t tomo_kernel_launches(void);
 

@@ -67,6 +67,7 @@ SIGNATURES = {
     "tomo_last_error": (C.c_char_p, []),
     "tomo_set_memory_limit": (C.c_int32, [C.c_uint64]),
     "tomo_memory_in_use": (C.c_uint64, []),
+    "tomo_device_memory": (C.c_int32, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "tomo_kernel_launches": (C.c_uint64, []),
     "tomo_create": (C.c_int32, [C.POINTER(Geom), C.POINTER(Params), C.POINTER(_P)]),
     "tomo_destroy": (C.c_int32, [_P]),

@@ -502,6 +502,14 @@ tomo_status tomo_set_memory_limit(uint64_t bytes) {
     return TOMO_OK;
 }
 uint64_t tomo_memory_in_use(void) { return g_in_use.load(); }
+tomo_status tomo_device_memory(uint64_t* free_bytes, uint64_t* total_bytes) {
+    if (!free_bytes || !total_bytes) return fail(TOMO_ERR_INVALID, "null argument");
+    size_t f = 0, t = 0;
+    CK(cudaMemGetInfo(&f, &t));
+    *free_bytes = f;
+    *total_bytes = t;
+    return TOMO_OK;
+}
 uint64_t tomo_kernel_launches(void) { return g_launches.load(); }
 
 tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_projector** out) {

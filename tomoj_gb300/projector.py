@@ -387,6 +387,85 @@ class CompressedSensingProjector(VoxelProjector3D):
         self._apply()
 
 
+class VoxelProjector3DGPU(VoxelProjector3D):
+    """VoxelProjector3DGPU / ProjectorGPU (TomoJ_GPU/.../projectors/ProjectorGPU.java:70-403):
+    the reference's OpenCL projector surface over the same engine handle.  The engine keeps
+    the whole volume on the device, so the slab calls act on rows of it:
+
+    * initForBP(startY, endY, updateNb) zeroes rows [startY, endY): the reference
+      backprojects into a new zero buffer (:175-193);
+    * initForIterative(startY, endY, update, kernelType, errorVolume[, other]) uploads those
+      rows from the reconstruction's host copy (:211-216), or, with `other`, works on
+      other's device volume (:217-235);
+    * copyInGPUBuffer uploads rows, updateFromGPU(startY, endY[, usableStartY, usableEndY])
+      downloads the usable rows into the reconstruction's host copy (:297-330);
+    * releaseCL_Memory frees the device memory and leaves the host copy as the last
+      updateFromGPU left it (:376-403);
+    * computeMaximumSizeForVolume is 40 % of the device memory (:162-166).
+
+    Kernel choices (setKernelToUse, setUseImage3D, kernelType) pick among OpenCL kernels of
+    one computation and are recorded only.  The debugging error volume (errorVolume =
+    True) is not provided."""
+
+    SEPARATE_PROJ_DIFF, ONE_KERNEL_PROJ_DIFF, ONE_KERNEL_PROJ_DIFF_WITH_ALIGNMENT = 0, 1, 2
+
+    def __init__(self, ts, rec, device=None, weightingFilter=None, **kw):
+        super().__init__(ts, rec, weightingFilter, **kw)
+        self.device = device
+        self.kernelusage = self.SEPARATE_PROJ_DIFF
+        self.useImage3D = False
+        self.currentStartY, self.currentEndY = 0, rec.getHeight()
+
+    def setKernelToUse(self, kernelusage: int):
+        self.kernelusage = int(kernelusage)
+
+    def setUseImage3D(self, useImage3D: bool):
+        self.useImage3D = bool(useImage3D)
+
+    def computeMaximumSizeForVolume(self) -> int:
+        free, total = C.c_uint64(), C.c_uint64()
+        check(self._lib.tomo_device_memory(C.byref(free), C.byref(total)))
+        return int(0.4 * total.value)
+
+    def _slab(self, startY, endY):
+        if not 0 <= startY <= endY <= self.rec.getHeight():
+            raise ValueError(f"rows [{startY}, {endY}) outside the volume")
+        self.currentStartY, self.currentEndY = int(startY), int(endY)
+
+    def initForBP(self, startY: int, endY: int, updateNb: int):
+        self._slab(startY, endY)
+        zeros = np.zeros((self.rec.getSizez(), endY - startY, self.rec.getWidth()), np.float32)
+        check(self._lib.tomo_set_volume(self._h, zeros.ctypes.data, 0, startY, endY))
+        self.kernelusage = self.SEPARATE_PROJ_DIFF
+
+    def initForIterative(self, startY: int, endY: int, update: int, kernelType: int, errorVolume: bool = False,
+                         other=None):
+        if errorVolume:
+            raise NotImplementedError("the debugging error volume of the OpenCL projector is not provided")
+        self._slab(startY, endY)
+        self.kernelusage = int(kernelType)
+        if other is not None:
+            self._share_volume(other)
+            return
+        self.copyInGPUBuffer(startY, endY)
+
+    def copyInGPUBuffer(self, startY: int, endY: int):
+        rows = np.ascontiguousarray(self.rec._host[:, startY:endY, :])
+        check(self._lib.tomo_set_volume(self._h, rows.ctypes.data, 0, startY, endY))
+
+    def updateFromGPU(self, startY: int, endY: int, usableStartY=None, usableEndY=None):
+        a = startY if usableStartY is None else int(usableStartY)
+        b = endY if usableEndY is None else int(usableEndY)
+        out = np.empty((self.rec.getSizez(), b - a, self.rec.getWidth()), np.float32)
+        check(self._lib.tomo_get_volume(self._h, out.ctypes.data, 0, a, b))
+        self.rec._host[:, a:b, :] = out
+
+    def releaseCL_Memory(self):
+        host = self.rec._host
+        self.close()
+        self.rec._host = host
+
+
 def first_index(seed: int, iteration: int, nproj: int) -> int:
     """Deterministic replacement of orderShuffleART's Math.random() first index."""
     return int(_abi.load().tomo_first_index(int(seed), int(iteration), int(nproj)))
