@@ -83,3 +83,44 @@ def test_bgart_parameters_equal_a_hand_built_projector(engine, case, median, dar
     assert np.array_equal(out[0][1], out[1][1])
     assert not np.array_equal(out[0][0], start)
 
+
+
+def test_thread_manager_runs_the_parameters(engine, case):
+    # ReconstructionThreadManager.reconstruct: the same volume as driving the projector by
+    # hand; a second call on the same sizes adds iterations to the same volume
+    c = case
+    params = R.ReconstructionParameters.createOSSARTParameters(W, H, D, 2, 0.9, 4)
+    mgr = R.ReconstructionThreadManager(None, tilt_series(c))
+    mgr.seed = 3
+    try:
+        rec = mgr.reconstruct(params)
+        first = rec.getVolume().copy()
+        errs = mgr.getReconstructionDissimilarities()
+        assert len(errs) == 2 and mgr.getNumberofsteps() == n * 2 * 2
+        assert mgr.reconstruct(params) is rec
+        second = rec.getVolume().copy()
+        proj5 = mgr.getProjection(5)
+    finally:
+        mgr.close()
+    ts = tilt_series(c)
+    ref = R.TomoReconstruction2(W, H, D)
+    p = params.getProjector(ts, ref)
+    try:
+        ref_errs = ref.OSSART(ts, p, params, seed=3)
+        assert np.array_equal(ref.getVolume(), first)
+        assert np.array_equal(np.asarray(errs), np.asarray(ref_errs))
+        ref.OSSART(ts, p, params, seed=3)
+        assert np.array_equal(ref.getVolume(), second)
+        p.addProjection(5)
+        p.project(0, H)
+        assert np.array_equal(p.getProjection(0), proj5)
+        p.clearAllProjections()
+    finally:
+        p.close()
+    wbp = R.ReconstructionParameters.createWBPParameters(W, H, D, 0.5)
+    mgr = R.ReconstructionThreadManager(None, tilt_series(c))
+    try:
+        rec = mgr.reconstruct(wbp)
+        assert mgr.getReconstructionDissimilarities() is None and np.any(rec.getVolume())
+    finally:
+        mgr.close()

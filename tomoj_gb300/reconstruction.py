@@ -290,6 +290,8 @@ class ReconstructionParameters:
         self.waveletPercentageOfZeros, self.waveletType, self.waveletDegree, self.waveletShift = 0.95, 3, 3.0, 0.0
         # volume storage precision (engine option; the reference stores float32)
         self.precision = _abi.PREC_FP32
+        # shifts of the volume centre (ReconstructionParameters.getReconstructionCenterModifiers)
+        self.reconstructionCenterModifiers = None
 
     @staticmethod
     def createOSSARTParameters(width, height, depth, nbIterations, relaxationCoefficient, updateNb):
@@ -365,6 +367,24 @@ class ReconstructionParameters:
 
     def getRegularizationWeight(self):
         return self.regularizationWeight
+
+    def getWidth(self):
+        return self.width
+
+    def getHeight(self):
+        return self.height
+
+    def getDepth(self):
+        return self.depth
+
+    def getReconstructionType(self):
+        return self.reconstructionType
+
+    def getReconstructionCenterModifiers(self):
+        return self.reconstructionCenterModifiers
+
+    def setReconstructionCenterModifiers(self, dx, dy, dz):
+        self.reconstructionCenterModifiers = (float(dx), float(dy), float(dz))
 
     def getNbIterations(self):
         return self.nbIterations
@@ -461,3 +481,106 @@ def project_volume(volume: np.ndarray, tilt_angle_start=-60.0, tilt_angle_end=60
         return np.array([proj.getProjection(i) for i in range(angles.size)], np.float32), angles
     finally:
         proj.close()
+
+
+class ReconstructionThreadManager:
+    """ReconstructionThreadManager (TomoJ_Base/.../tomography/ReconstructionThreadManager.java):
+    the reference's driver from a ReconstructionParameters to a reconstruction.
+    reconstruct() makes or reuses the volume (createRec2, :169-196: reused when the sizes
+    match, so further calls add iterations) and runs doCPUrec (:218-255): the parameters'
+    projector, then WBP for BP / WBP, OSSART for OSSART, regularization for the other
+    types.  The run is synchronous (the reference runs it on a worker thread behind a
+    progress window).  The debugging error volumes (saveErrorVolume) are not provided.
+    The projector stays open for getProjection until the next reconstruction or close()."""
+
+    def __init__(self, parentWindow=None, ts=None, other=None):
+        self.parentWindow = parentWindow if other is None else other.parentWindow
+        self.ts = ts
+        self.rec2 = None
+        self.projector = None
+        self.errors = None
+        self.numberofsteps = 0.0
+        self._thprojs = None
+        self.seed = 0  # orderShuffleART's first-index seed
+
+    def reconstruct(self, parameters, showProgressWindow=False):
+        self.createRec2(parameters)
+        self.performReconstruction(parameters, showProgressWindow)
+        return self.rec2
+
+    def createRec2(self, parameters):
+        self._thprojs = None
+        w, h, d = parameters.getWidth(), parameters.getHeight(), parameters.getDepth()
+        r = self.rec2
+        if r is None or (r.getWidth(), r.getHeight(), r.getSizez()) != (w, h, d):
+            self.close()
+            self.rec2 = TomoReconstruction2(w, h, d)
+            mod = parameters.getReconstructionCenterModifiers()
+            if mod is not None:
+                c = self.rec2.centers()
+                self.rec2.setCenter(c[0] + mod[0], c[1] + mod[1], c[2] + mod[2])
+
+    def performReconstruction(self, parameters, showProgressWindow=False):
+        self._thprojs = None
+        self.rec2.completion = 0.0
+        n = self.ts.getImageStackSize()
+        self.numberofsteps = n * parameters.getNbIterations() * 2 if parameters.getReconstructionType() > WBP else n
+        self.errors = self.doCPUrec(parameters, False, False)
+
+    def doRec(self, parameters, saveErrorVol=False, saveForAll=False, time=None):
+        return self.doCPUrec(parameters, saveErrorVol, saveForAll)
+
+    def doCPUrec(self, params, saveError=False, saveForAll=False):
+        if saveError or saveForAll:
+            raise NotImplementedError("the debugging error volume is not provided")
+        self.close()
+        self.projector = params.getProjector(self.ts, self.rec2)
+        kind = params.getReconstructionType()
+        if kind in (BP, WBP):
+            self.rec2.WBP(self.ts, self.projector, params, 0, self.rec2.getHeight())
+            return None
+        if kind == OSSART:
+            return self.rec2.OSSART(self.ts, self.projector, params, 0, self.rec2.getHeight(), seed=self.seed)
+        return self.rec2.regularization(self.ts, self.projector, params, 0, self.rec2.getHeight(), seed=self.seed)
+
+    def getProjection(self, index: int) -> np.ndarray:
+        """The projection of the reconstruction at tilt `index` (cached, :257-270)."""
+        if self._thprojs is None:
+            self._thprojs = {}
+        if index not in self._thprojs:
+            p = self.projector
+            p.addProjection(index)
+            p.project(0, self.rec2.getHeight())
+            self._thprojs[index] = p.getProjection(0).copy()
+            p.clearAllProjections()
+        return self._thprojs[index]
+
+    def close(self):
+        if self.projector is not None:
+            self.projector.close()
+            self.projector = None
+
+    def setRec2(self, rec2):
+        self._thprojs = None
+        self.close()
+        self.rec2 = rec2
+
+    def resetRec2(self):
+        self.setRec2(None)
+
+    def getRec2(self):
+        return self.rec2
+
+    def setTiltSeries(self, ts):
+        self.ts = ts
+
+    def getNumberofsteps(self):
+        return self.numberofsteps
+
+    def getReconstructionDissimilarities(self):
+        return self.errors
+
+    def getCompletion(self):
+        if self.rec2 is not None and self.numberofsteps:
+            return self.rec2.completion / self.numberofsteps * 100
+        return -123456789
