@@ -320,12 +320,13 @@ class CompressedSensingProjector(VoxelProjector3D):
 
     WAVELET_ORTHONORMAL, WAVELET_BSPLINE, WAVELET_DUAL = 0, 3, 6
 
-    def __init__(self, ts, rec, weighting=None, **kw):
+    def __init__(self, ts, rec, weighting=None, waveletType=3, waveletDegree=3.0, waveletShift=0.0,
+                 softThresholdingPercentageOfZeros=0.95, **kw):
         super().__init__(ts, rec, weighting, **kw)
-        self.waveletDegree = 3.0
-        self.waveletShift = 0.0
-        self.waveletType = self.WAVELET_BSPLINE
-        self.softThresholdingPercentageOfZeros = 0.95
+        self.waveletDegree = float(waveletDegree)
+        self.waveletShift = float(waveletShift)
+        self.waveletType = int(waveletType)
+        self.softThresholdingPercentageOfZeros = float(softThresholdingPercentageOfZeros)
         self.iters = self.findBestWaveletsIteration(rec)
         self._apply()
 

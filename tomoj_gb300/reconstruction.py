@@ -416,11 +416,8 @@ class ReconstructionParameters:
         kind = self.reconstructionType
         if kind == COMPRESSED_SENSING:
             # CompressedSensingProjector keeps the projector defaults (no positivity / long object)
-            proj = CompressedSensingProjector(ts, rec, None, scale=scale, precision=self.precision)
-            proj.waveletType, proj.waveletDegree = int(self.waveletType), float(self.waveletDegree)
-            proj.waveletShift = float(self.waveletShift)
-            proj.softThresholdingPercentageOfZeros = float(self.waveletPercentageOfZeros)
-            proj._apply()
+            proj = CompressedSensingProjector(ts, rec, None, self.waveletType, self.waveletDegree, self.waveletShift,
+                                              self.waveletPercentageOfZeros, scale=scale, precision=self.precision)
             if self.fista:
                 proj.setFista(True)
             return proj
