@@ -561,7 +561,10 @@ def run_serving_leg(args):
     """BASELINE config 5, bounded to args.serve_requests requests: Poisson arrivals (4/s) of
     series of {512,1024,2048}^2 x {128,256,512} with {41,61,121} tilts, WBP 30 % / SIRT 40 % /
     OS-SART 20 % / TVM 10 %, 5-50 iterations; continuous batching with HBM admission."""
+    import torch
     from tomoj_gb300.serving import EngineAdapter, Server, summarize, synthetic_requests
+    # admission is by free HBM: hand back what earlier legs left in torch's allocator cache
+    torch.cuda.empty_cache()
     reqs = synthetic_requests(args.serve_requests, seed=42)
     eng = EngineAdapter()
     try:
