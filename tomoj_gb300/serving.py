@@ -32,6 +32,17 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _abi
+
+
+def _release_torch_cache() -> bool:
+    """Admission is by free HBM: blocks that torch's allocator keeps cached in this process
+    count as used.  When torch is loaded with CUDA, hand them back; True if it was."""
+    import sys
+    torch = sys.modules.get("torch")
+    if torch is None or not torch.cuda.is_initialized():
+        return False
+    torch.cuda.empty_cache()
+    return True
 from .tiltseries import euler_angles_to_matrix
 
 WBP, SIRT, OSSART, TVM = "WBP", "SIRT", "OS-SART", "TVM"
@@ -108,7 +119,9 @@ class EngineAdapter:
         p = _abi.make_params(fill=fill)
         hd = C.c_void_p()
         rc = lib.tomo_create(C.byref(g), C.byref(p), C.byref(hd))
-        if rc == -3:
+        if rc == _abi.ERR_NOMEM and _release_torch_cache():
+            rc = lib.tomo_create(C.byref(g), C.byref(p), C.byref(hd))
+        if rc == _abi.ERR_NOMEM:
             return None
         _abi.check(rc)
         try:
