@@ -13,7 +13,7 @@
 // Orthonormal: Ho = H sqrt(A(w)/A(2w)), Go = e^{-iw} conj(Ho(w+pi)); B-spline: synthesis
 // H, e^{-iw} conj(H(w+pi)) A(w+pi), analysis H A(w)/A(2w), e^{-iw} conj(H(w+pi))/A(2w);
 // dual: the B-spline pair exchanged.  All filter values are computed on the host in
-// double; the device does only FFTs (radix 2, Bluestein for other lengths) and products.
+// double; the device does only FFTs (radix 4, Bluestein for other lengths) and products.
 //
 // A level along an axis of length n runs a group of threads per pair of lines: DFT_n, the two analysis
 // products folded to n/2 frequencies, two inverse DFT_{n/2} into [low | high].  The
@@ -33,7 +33,7 @@ namespace tomo {
 namespace {
 
 constexpr int kWavThreads = 256;
-constexpr int kWavTwN = 8192;      // twiddle table e^{-2 pi i k / 8192}, k < 4096
+constexpr int kWavTwN = 8192;      // twiddle table e^{-2 pi i k / 8192}, k < 6144
 constexpr int kWavMaxPow2 = 8192;  // longest power-of-two line
 constexpr int kWavMaxOther = 4096; // longest other line (Bluestein grid <= 8192)
 constexpr int kWavTailK = 256;
@@ -79,8 +79,11 @@ struct Grp {
     int t, nt;
 };
 
-// In-place radix-2 DFT of s[0, n) (natural order in and out), n = 2^logn >= 2, unnormalised;
-// inverse uses e^{+2 pi i kn/n}.  Ends with a barrier.
+// In-place DFT of s[0, n) (natural order in and out), n = 2^logn >= 2, unnormalised; inverse
+// uses e^{+2 pi i kn/n}.  Decimation in time after a bit-reversal permutation: one radix-2
+// stage when logn is odd, then radix-4 passes, each doing the radix-2 stages of spans h and
+// 2h at once: with w = e^{-2 pi i pos / 4h}, the inputs take w^2, w and w^3 and a 4-point
+// DFT whose only products are by -i (+i inverse).  Ends with a barrier.
 __device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict__ tw, bool inverse, Grp g) {
     for (int k = g.t; k < n; k += g.nt) {
         const int r = (int)(__brev((unsigned)k) >> (32 - logn));
@@ -91,26 +94,42 @@ __device__ void fft_pow2(double2* s, int n, int logn, const double2* __restrict_
         }
     }
     __syncthreads();
-    for (int lg = 1; lg <= logn; lg++) {
-        const int half = 1 << (lg - 1);
-        const int step = kWavTwN >> lg;
+    int lg = 1;
+    if (logn & 1) {
         for (int j = g.t; j < (n >> 1); j += g.nt) {
-            const int pos = j & (half - 1);
-            const int i0 = ((j >> (lg - 1)) << lg) + pos;
-            const double2 a = s[i0];
-            double2 b = s[i0 + half];
+            const double2 a = s[2 * j], b = s[2 * j + 1];
+            s[2 * j] = cadd(a, b);
+            s[2 * j + 1] = csub(a, b);
+        }
+        __syncthreads();
+        lg = 2;
+    }
+    for (; lg < logn; lg += 2) {
+        const int h = 1 << (lg - 1);
+        const int step = kWavTwN >> (lg + 1);  // e^{-2 pi i pos / 4h} = tw[pos * step]
+        for (int j = g.t; j < (n >> 2); j += g.nt) {
+            const int pos = j & (h - 1);
+            const int i0 = ((j >> (lg - 1)) << (lg + 1)) + pos;
+            const double2 a0 = s[i0];
+            double2 a1 = s[i0 + h], a2 = s[i0 + 2 * h], a3 = s[i0 + 3 * h];
             if (pos != 0) {
-                if (lg == 2) {
-                    // twiddle -i (forward) or +i (inverse): a swap and a sign
-                    b = inverse ? make_double2(-b.y, b.x) : make_double2(b.y, -b.x);
-                } else {
-                    double2 w = tw[pos * step];
-                    if (inverse) w.y = -w.y;
-                    b = cmul(b, w);
+                double2 w1 = tw[2 * pos * step], w2 = tw[pos * step], w3 = tw[3 * pos * step];
+                if (inverse) {
+                    w1.y = -w1.y;
+                    w2.y = -w2.y;
+                    w3.y = -w3.y;
                 }
+                a1 = cmul(a1, w1);
+                a2 = cmul(a2, w2);
+                a3 = cmul(a3, w3);
             }
-            s[i0] = cadd(a, b);
-            s[i0 + half] = csub(a, b);
+            const double2 b0 = cadd(a0, a1), b1 = csub(a0, a1), b2 = cadd(a2, a3), b3 = csub(a2, a3);
+            // -i b3 forward, +i b3 inverse
+            const double2 t = inverse ? make_double2(-b3.y, b3.x) : make_double2(b3.y, -b3.x);
+            s[i0] = cadd(b0, b2);
+            s[i0 + 2 * h] = csub(b0, b2);
+            s[i0 + h] = cadd(b1, t);
+            s[i0 + 3 * h] = csub(b1, t);
         }
         __syncthreads();
     }
@@ -458,8 +477,8 @@ WaveletPlan* wavelet_plan_create(int W, int H, int D, const int iters[3], int ty
     P->D = D;
     // (long)(percentageOfZeros * X * Y * Z), evaluated left to right
     P->nbpixels = (long long)(fraction_zeros * W * H * D);
-    P->tables.resize(kWavTwN / 2);
-    for (int k = 0; k < kWavTwN / 2; k++) {
+    P->tables.resize(3 * kWavTwN / 4);
+    for (int k = 0; k < 3 * kWavTwN / 4; k++) {
         const double ang = -2.0 * M_PI * k / kWavTwN;
         P->tables[k] = make_double2(std::cos(ang), std::sin(ang));
     }
@@ -479,9 +498,9 @@ WaveletPlan* wavelet_plan_create(int W, int H, int D, const int iters[3], int ty
         q.full = make_dft(*P, cache, q.n);
         q.half = make_dft(*P, cache, q.n / 2);
         make_filters(*P, q.n, type, alpha, tau, syn, q.lo, q.hi);
-        // enough line pairs per CTA that a butterfly stage has work for every thread
+        // enough line pairs per CTA that a radix-4 pass has work for every thread
         q.groups = 1;
-        while (q.groups < 32 && (long long)q.groups * q.n < 2 * kWavThreads) q.groups <<= 1;
+        while (q.groups < 32 && (long long)q.groups * q.n < 4 * kWavThreads) q.groups <<= 1;
         q.stride = q.n + (int)std::max(dft_scratch(q.full), dft_scratch(q.half));
         q.smem = sizeof(double2) * (size_t)q.groups * q.stride;
         P->smem_max = std::max(P->smem_max, q.smem);
