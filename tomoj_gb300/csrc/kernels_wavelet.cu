@@ -37,6 +37,7 @@ constexpr int kWavTwN = 8192;      // twiddle table e^{-2 pi i k / 8192}, k < 61
 constexpr int kWavMaxPow2 = 8192;  // longest power-of-two line
 constexpr int kWavMaxOther = 4096; // longest other line (Bluestein grid <= 8192)
 constexpr int kWavTailK = 256;
+constexpr int kWavSMs = 152;      // streaming multiprocessors of the part
 
 struct WavState {
     unsigned long long maxkey;  // max |v| as double bits (non-negative: ordered as integers)
@@ -350,7 +351,7 @@ struct WaveletPlan {
         long long es = 0, su = 0, sv = 0;
         Dft full, half;
         size_t lo = 0, hi = 0;
-        int groups = 1, stride = 0;
+        int groups = 1, nt = kWavThreads, stride = 0;
         size_t smem = 0;
     };
     int W = 0, H = 0, D = 0;
@@ -498,9 +499,15 @@ WaveletPlan* wavelet_plan_create(int W, int H, int D, const int iters[3], int ty
         q.full = make_dft(*P, cache, q.n);
         q.half = make_dft(*P, cache, q.n / 2);
         make_filters(*P, q.n, type, alpha, tau, syn, q.lo, q.hi);
-        // enough line pairs per CTA that a radix-4 pass has work for every thread
-        q.groups = 1;
-        while (q.groups < 32 && (long long)q.groups * q.n < 4 * kWavThreads) q.groups <<= 1;
+        // threads per line pair: one per radix-4 butterfly of the longest transform (4 to
+        // 256); line pairs per CTA: up to 256 threads, fewer when the pass would otherwise
+        // leave less than two CTAs per SM
+        const long long pairs = (long long)((q.nu + 1) / 2) * q.nv;
+        const int work = std::max(q.full.logn >= 0 ? q.n : q.full.M, q.half.logn >= 0 ? q.n / 2 : q.half.M) / 4;
+        q.nt = 4;
+        while (q.nt < kWavThreads && q.nt < work) q.nt <<= 1;
+        q.groups = kWavThreads / q.nt;
+        while (q.groups > 1 && pairs / q.groups < 2LL * kWavSMs) q.groups >>= 1;
         q.stride = q.n + (int)std::max(dft_scratch(q.full), dft_scratch(q.half));
         q.smem = sizeof(double2) * (size_t)q.groups * q.stride;
         P->smem_max = std::max(P->smem_max, q.smem);
@@ -589,10 +596,11 @@ cudaError_t launch_wavelet_filter(const WaveletPlan* P, float* vol, cudaStream_t
         L.tw = P->d_tables;
         const long long pairs = (long long)((q.nu + 1) / 2) * q.nv;
         const unsigned grid = (unsigned)((pairs + q.groups - 1) / q.groups);
+        const int block = q.groups * q.nt;
         if (q.syn)
-            wav_lines_kernel<true><<<grid, kWavThreads, q.smem, s>>>(L);
+            wav_lines_kernel<true><<<grid, block, q.smem, s>>>(L);
         else
-            wav_lines_kernel<false><<<grid, kWavThreads, q.smem, s>>>(L);
+            wav_lines_kernel<false><<<grid, block, q.smem, s>>>(L);
         count_launch();
     };
     for (size_t i = 0; i < nfwd; i++) run_pass(P->passes[i]);
