@@ -134,7 +134,10 @@ class ClockSampler:
 # ----------------------------------------------------------------------------- CPU arm
 def cpu_sample(wl, rows, threads, steps=1):
     """Time the C restatement of the reference's CPU path on `rows` volume rows of the
-    workload (same W, D, tilts, subsets): one WBP pass + one OS-SART iteration per step.
+    workload: the same W, D, tilts, phantom density, misalignment, noise, WBP filter and
+    subsets.  One step is what the reference does for one WBP pass and one OS-SART
+    iteration: align the projections (average fill for WBP, NaN fill for the iterative
+    pass), weight and backproject them, then the iteration.
     Returns (updates/s, seconds, updates)."""
     from oracle import oracle as O
     from tomoj_gb300 import phantom as P
@@ -143,20 +146,42 @@ def cpu_sample(wl, rows, threads, steps=1):
     W, D, n = wl["W"], wl["D"], wl["n"]
     H = rows
     g = O.Geom(W, H, D, W, H)
-    vol = P.ellipsoid_phantom(W, H, D, max(4, wl["ellipsoids"] // 4), wl["seed"])
+    vol = P.ellipsoid_phantom(W, H, D, wl["ellipsoids"], wl["seed"])
     angles = np.linspace(-wl["amax"], wl["amax"], n)
     eul = np.array([O.euler_tilt_y(a) for a in angles])
-    meas = np.nan_to_num(np.array([O.project(vol, g, e)[0] for e in eul], np.float32))
+    ideal = np.nan_to_num(np.array([O.project(vol, g, e)[0] for e in eul], np.float32))
+    if wl["shifts"] or wl["rot"]:
+        T = P.misalignment(n, wl["seed"] + 1, wl["shifts"], wl["rot"])
+        series = np.array([P.unalign(ideal[i], T[i]) for i in range(n)], np.float32)
+    else:
+        T = np.tile(np.array([1.0, 0, 0, 1, 0, 0]), (n, 1))
+        series = ideal
+    if wl["noise"]:
+        series = P.add_gaussian_noise(series, wl["noise"], wl["seed"] + 2)
+    stats = np.array([[series[i].mean(dtype=np.float64), series[i].std(dtype=np.float64)] for i in range(n)])
+    mask = O.ramp_mask(W, H, angles, hamming=(wl["wbp"] == "hamming_ramp"))
     order = O.order_shuffle(eul, 0)
     upd = wl["update"]
     ups = W * H * D * n * 2
     t0 = time.perf_counter()
     for _ in range(steps):
+        avg = np.array([O.align(series[i], T[i], False, stats[i, 0], stats[i, 1], O.FILL_AVG) for i in range(n)],
+                       np.float32)
+        meas = np.array([O.align(series[i], T[i], fill=O.FILL_NAN) for i in range(n)], np.float32)
         rec = np.zeros((D, H, W), np.float32)
-        O.wbp(rec, g, eul, meas, None)
+        O.wbp(rec, g, eul, avg, mask)
         O.ossart_iteration(rec, g, eul, meas, order, wl["relax"], upd)
     dt = time.perf_counter() - t0
     return ups * steps / dt, dt, ups * steps
+
+
+def config_of(args, wl, world):
+    """The `config` object both arms print for the workload."""
+    W, H, D, n = wl["W"], wl["H"], wl["D"], wl["n"]
+    return {"workload": args.workload, "W": W, "H": H, "D": D, "nproj": n, "proj": f"{W}x{H}", "wbp": wl["wbp"],
+            "shifts_px": wl["shifts"], "rot_deg": wl["rot"], "noise": wl["noise"], "ellipsoids": wl["ellipsoids"],
+            "n_iter": wl["n_iter"], "update": wl["update"], "updates_per_step": W * H * D * n * (1 + wl["n_iter"]),
+            "l2": f"inputs larger than L2 (volume {W * H * D * 4 // 10**6} MB)", "parallelism": f"replicas{world}"}
 
 
 def cpu_plan(wl, threads, target_s):
@@ -192,8 +217,7 @@ def run_reference(args, wl):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, **{k: wl[k] for k in ("W", "H", "D", "n", "n_iter", "update")},
-                   "l2": "inputs larger than L2"},
+        "config": config_of(args, wl, world),
         "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -444,6 +468,7 @@ def run_engine(args, wl):
                          f"{dt:.1f} s"}
 
     lib.tomo_destroy(h)
+    config1 = None if (args.no_extra or args.no_cpu or rank != 0 or world != 1) else run_config1_leg(lib, args)
     batched = None if args.no_extra else run_batched_leg(lib, args)
     serving = None if args.no_extra else run_serving_leg(args)
     precision = None if args.no_extra else run_precision_leg(lib, args)
@@ -452,14 +477,12 @@ def run_engine(args, wl):
             "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "W": W, "H": H, "D": D, "nproj": n, "proj": f"{W}x{H}",
-                       "wbp": wl["wbp"], "n_iter": wl["n_iter"], "update": wl["update"],
-                       "updates_per_step": updates_per_step, "l2": "inputs larger than L2 (volume 268 MB)",
-                       "parallelism": f"replicas{world}"},
+            "config": config_of(args, wl, world),
             "e2e": {"value": e2e_value, "unit": "voxel-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps, "phases_s": phase},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-            "row_streams": row_leg, "compressed_sensing": cs_leg, "batched": batched, "serving": serving, "precision": precision,
+            "row_streams": row_leg, "compressed_sensing": cs_leg, "config1_full": config1, "batched": batched,
+            "serving": serving, "precision": precision,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)
@@ -577,6 +600,73 @@ def run_serving_leg(args):
     s["wall_s"] = wall
     s["unit"] = "seconds (time to reconstruction)"
     return s
+
+
+def run_config1_leg(lib, args):
+    """The 256 x 64 x 256 workload (20 ellipsoids, 61 tilts of 256 x 64 at -60..60 deg made
+    by the oracle's projector, 1 % Gaussian noise; ramp-filtered WBP start, then 10 SIRT
+    iterations, relaxation 1), timed in full on both sides: the engine (CUDA events, device
+    resident) and the C restatement of the reference's CPU path on all host threads."""
+    import torch
+    from oracle import oracle as O
+    from tomoj_gb300 import phantom as P
+    wl = WORKLOADS["sirt256"]
+    W, H, D, n = wl["W"], wl["H"], wl["D"], wl["n"]
+    threads = os.cpu_count() or 1
+    O.build()
+    O.set_threads(threads)
+    g = O.Geom(W, H, D, W, H)
+    vol = P.ellipsoid_phantom(W, H, D, wl["ellipsoids"], wl["seed"])
+    angles = np.linspace(-wl["amax"], wl["amax"], n)
+    eul = np.array([O.euler_tilt_y(a) for a in angles])
+    series = np.nan_to_num(np.array([O.project(vol, g, e)[0] for e in eul], np.float32))
+    series = np.ascontiguousarray(P.add_gaussian_noise(series, wl["noise"], wl["seed"] + 2), np.float32)
+    ups = W * H * D * n * (1 + wl["n_iter"])
+    seed = 5
+    # engine
+    stream = torch.cuda.current_stream()
+    geo = _abi_mod().make_geom(W, H, D, W, H, n)
+    prm = _abi_mod().make_params(fill=_abi_mod().FILL_NAN)
+    h = C.c_void_p()
+    _abi_mod().check(lib.tomo_create(C.byref(geo), C.byref(prm), C.byref(h)))
+    e = np.ascontiguousarray(eul, np.float64)
+    try:
+        _abi_mod().check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        _abi_mod().check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi_mod().ptr(e, C.c_double), None, None))
+
+        def job():
+            _abi_mod().check(lib.tomo_fill_volume(h, 0.0))
+            _abi_mod().check(lib.tomo_set_weighting(h, _abi_mod().WEIGHT_RAMP, 0.0, None, None))
+            _abi_mod().check(lib.tomo_run_wbp(h, 0, H))
+            _abi_mod().check(lib.tomo_set_weighting(h, _abi_mod().WEIGHT_NONE, 0.0, None, None))
+            _abi_mod().check(lib.tomo_run_ossart(h, wl["n_iter"], wl["relax"], 0, seed, 0, H, 1, None))
+
+        for _ in range(3):
+            job()
+        reps = 10
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            job()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        gpu_s = ev0.elapsed_time(ev1) / 1000.0 / reps
+    finally:
+        lib.tomo_destroy(h)
+    # CPU: the whole job once
+    mask = O.ramp_mask(W, H, angles, hamming=False)
+    order = O.order_shuffle(eul, 0)
+    t0 = time.perf_counter()
+    rec = np.zeros((D, H, W), np.float32)
+    O.wbp(rec, g, eul, series, mask)
+    for _ in range(wl["n_iter"]):
+        O.ossart_iteration(rec, g, eul, series, order, wl["relax"], 0)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "sirt256: 256x64x256, 61 tilts of 256x64, ramp WBP + 10 SIRT iterations",
+            "updates": ups, "engine_s": gpu_s, "engine_voxel_updates_per_s": ups / gpu_s,
+            "cpu_s": cpu_s, "cpu_voxel_updates_per_s": ups / cpu_s, "cpu_cores": threads,
+            "cpu_kind": "port", "speedup": cpu_s / gpu_s}
 
 
 def phantom_on_device(W, H, D, n_ell, seed, device):

@@ -263,6 +263,14 @@ tomo_status tomo_set_profiling(tomo_projector* p, int32_t enabled);
 tomo_status tomo_profile_read(tomo_projector* p, double* out4);
 /* Tilts per forward-projection CTA (0 = automatic; tuning knob). */
 tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n);
+/* Failure-path test hook (no counterpart in the reference): while enabled, the
+ * forward projector of this handle does not issue the bulk copies of each CTA's
+ * first plane chunk, so that chunk's bounded mbarrier wait runs out, the CTA
+ * records the timeout in the device status word and returns with nothing in
+ * flight; the call reports TOMO_ERR_DEVICE and the handle stays usable.  Only
+ * volumes whose rows are staged with bulk copies (W * element size a multiple
+ * of 16 bytes) are affected. */
+tomo_status tomo_debug_hold_first_copy(tomo_projector* p, int32_t enabled);
 
 /* ---- projection + difference without allocation ----------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
@@ -275,7 +283,9 @@ tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n);
  *   err_out host double [T]               euler host double [nproj][9]
  * Its scratch lives in one static device array of about 5 MiB that every GPU
  * loading the library keeps until exit.  Limits: nproj <= 128, T <= 64,
- * w, h <= 2048, vertical tilt axis.  The first call on a device sets up the
+ * w, h <= 2048, W up to about 9500 (one plane row in the forward projector's
+ * shared memory), vertical tilt axis.  Long-object compensation is not applied
+ * (the plain projector's norms and differences).  The first call on a device sets up the
  * scratch address (make it before any stream capture).  Calls share the
  * scratch: calls that overlap on the GPU, or run concurrently, race.
  * Synchronous on `stream` (cudaStream_t as void*, NULL = default stream). */

@@ -6,10 +6,12 @@ norms FP64.  Tolerances:
 
 * FP16 storage: <= 1e-3 relative L2 against the FP64 oracle after 10 SIRT
   iterations (the format keeps 11 significant bits: rounding alone is ~1.4e-4).
-* BF16 storage: 8 significant bits, so rounding a volume once already costs
-  ~1.1e-3 to 1.6e-3 relative L2, and every iteration re-rounds it (measured on a
-  GB300: 4.0e-3 after 10 SIRT iterations).  BF16 therefore does not meet the
-  1e-3 target; its bound here is 6e-3 and FP16 is the storage that meets it.
+* BF16 storage is held to the same 1e-3 and fails it: with 8 significant bits,
+  rounding a volume once already costs ~1.1e-3 to 1.6e-3 relative L2, and every
+  iteration re-rounds it (measured on a GB300: 4.0e-3 after 10 SIRT iterations).
+  Its 1e-3 case is an expected failure (strict: it must keep failing, so a change
+  that made it pass would be noticed); a second test keeps it below the 6e-3 it
+  measures, so that it does not get worse.  FP16 is the storage that meets 1e-3.
 * A forward projection of a reduced volume is bit-identical to the FP32 forward
   projection of the same values (power-of-two scales commute with rounding).
 """
@@ -29,7 +31,8 @@ pytestmark = pytest.mark.gpu
 
 PRECS = {"bf16": _abi.PREC_BF16, "fp16": _abi.PREC_FP16}
 ULP_REL = {"bf16": 2.0 ** -8, "fp16": 2.0 ** -11}  # bound on |x - round(x)| / |x| (half an ulp, doubled)
-TOL_SIRT10 = {"bf16": 6e-3, "fp16": 1e-3}
+TOL_SIRT10 = 1e-3          # the reduced-precision target, for every storage type
+BF16_MEASURED_BOUND = 6e-3  # what BF16 storage does reach after 10 SIRT iterations
 
 
 class RHandle:
@@ -119,8 +122,9 @@ def test_reduced_forward_projection_is_bitwise_fp32_of_stored_values(engine, nam
         ref.close()
 
 
-@pytest.mark.parametrize("name", sorted(PRECS))
-def test_reduced_sirt_10_against_fp64_oracle(engine, name):
+def _sirt10_errors(engine, name):
+    """(rel-L2 vs the FP64 oracle, rel-L2 vs the FP32 engine, residual norms of both) after
+    10 SIRT iterations with `name` storage."""
     c = series_case(W=64, H=8, D=48, n=21, seed=21)
     n_iter, seed = 10, 99
     hd = RHandle(engine, c, PRECS[name])
@@ -141,12 +145,29 @@ def test_reduced_sirt_10_against_fp64_oracle(engine, name):
         e32 = rel_l2(got, got32)
         print(f"{name}: rel-L2 vs FP64 oracle {e64:.3e}, vs FP32 engine {e32:.3e}, "
               f"FP32 engine vs FP64 {rel_l2(got32, ref):.3e}")
-        assert e64 <= TOL_SIRT10[name], e64
-        # residual norms (FP64 reductions) follow the oracle's
-        assert np.allclose(err[:, 0], errs[:, 0], rtol=10 * TOL_SIRT10[name])
+        return e64, e32, err, errs
     finally:
         hd.close()
         f32.close()
+
+
+@pytest.mark.parametrize("name", [
+    "fp16",
+    pytest.param("bf16", marks=pytest.mark.xfail(
+        strict=True, reason="BF16 keeps 8 significant bits: one rounding of the volume costs ~1.1e-3 "
+                            "relative L2, so 10 SIRT iterations end near 4e-3; FP16 meets 1e-3")),
+])
+def test_reduced_sirt_10_against_fp64_oracle(engine, name):
+    e64, _, err, errs = _sirt10_errors(engine, name)
+    assert e64 <= TOL_SIRT10, e64
+    # residual norms (FP64 reductions) follow the oracle's
+    assert np.allclose(err[:, 0], errs[:, 0], rtol=10 * TOL_SIRT10)
+
+
+def test_bf16_sirt_10_stays_within_its_measured_bound(engine):
+    e64, _, err, errs = _sirt10_errors(engine, "bf16")
+    assert e64 <= BF16_MEASURED_BOUND, e64
+    assert np.allclose(err[:, 0], errs[:, 0], rtol=10 * BF16_MEASURED_BOUND)
 
 
 def test_fp16_overflow_of_a_slab_is_reported(engine):

@@ -328,7 +328,9 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 if (tid == 0) {
                     fence_proxy_async();
                     mbar_arrive_expect_tx(bar, (uint32_t)zn * rowb * (BLEND && blend ? 2u : 1u));
-                    for (int zz = 0; zz < zn; zz++) {
+                    // test hook: the first chunk's copies are held back (its wait runs out)
+                    const int issue = (a.hold_first_copy && c == c_begin) ? 0 : zn;
+                    for (int zz = 0; zz < issue; zz++) {
                         tma_load_1d(rawb + (size_t)zz * rowb, volb + ((size_t)(z0 + zz) * H + r) * rowb, rowb, bar);
                         if (BLEND && blend)
                             tma_load_1d(raw1 + (size_t)zz * W, volb + ((size_t)(z0 + zz) * H + r + 1) * rowb, rowb,
@@ -363,11 +365,12 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             const int zc = min(ZC, D - z0);
             const uint32_t parity = (uint32_t)((c - c_begin) & 1);
             if (use_tma) {
-                const bool ok = mbar_wait_bounded(bar, parity, kWaitTries);
+                const bool held = a.hold_first_copy && c == c_begin;  // nothing was issued for it
+                const bool ok = mbar_wait_bounded(bar, parity, held ? kHoldWaitTries : kWaitTries);
                 if (__syncthreads_or(!ok)) {
                     if (tid == 0) atomicOr(a.status, kStatusTimeout);
                     // let any copy still in flight land before the CTA's shared memory is released
-                    mbar_wait_bounded(bar, parity, kWaitTries);
+                    if (!held) mbar_wait_bounded(bar, parity, kWaitTries);
                     return;
                 }
             } else {

@@ -133,7 +133,7 @@ void build_generic_fp_tilt(const double* R, GenericFpTilt* o) {
 // oldx + (z+1) dirX + volcenterx; the ray counts a plane when
 // x + ACCURACY >= 0 && x < W, and one extra normIncrement when it leaves the
 // volume laterally.
-void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays) {
+void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays, float* normtab_scratch) {
     const double dirY = -(R[5] - R[3] * R[2] / R[0]) / (R[4] - R[3] * R[1] / R[0]);
     const double dirX = (R[1] * (-dirY) - R[2]) / R[0];
     const double ninc = std::sqrt(dirX * dirX + dirY * dirY + 1);
@@ -143,7 +143,13 @@ void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* ra
     tilt->ninc = ninc;
     const int D = g.D;
     // norm_sum is a float accumulating a double increment: norm(k) for k increments.
-    std::vector<float> normtab((size_t)D + 2, 0.0f);
+    std::vector<float> own;
+    float* normtab = normtab_scratch;
+    if (!normtab) {
+        own.assign((size_t)D + 2, 0.0f);
+        normtab = own.data();
+    }
+    normtab[0] = 0.0f;
     for (int k = 1; k < D + 2; k++) normtab[k] = (float)((double)normtab[k - 1] + ninc);
 
     for (int i = 0; i < g.w; i++) {
@@ -167,23 +173,22 @@ void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* ra
             const double zb = (bXmax - vcx - oldx0) / dirX - 1.0;
             find_interval(D, za, zb, in_fast, &lo, &cnt);
             if (near) {
-                // Replay the reference's accumulation exactly for rays that graze a border.
-                std::vector<char> flag((size_t)D, 0);
+                // Replay the reference's accumulation exactly for rays that graze a border:
+                // the first run of inside planes (the reference stops at the plane after it).
                 double oldx = oldx0;
+                int first = -1, run = 0;
                 for (int z = 0; z < D; z++) {
                     const double xc = oldx + dirX;
-                    flag[z] = in_exact(xc + vcx);
+                    if (in_exact(xc + vcx)) {
+                        if (first < 0) first = z;
+                        run++;
+                    } else if (first >= 0) {
+                        break;
+                    }
                     oldx = xc;
                 }
-                lo = 0;
-                cnt = 0;
-                int z = 0;
-                while (z < D && !flag[z]) z++;
-                if (z < D) {
-                    lo = z;
-                    while (z < D && flag[z]) z++;
-                    cnt = z - lo;
-                }
+                lo = first < 0 ? 0 : first;
+                cnt = run;
             }
         }
         int incr = cnt;

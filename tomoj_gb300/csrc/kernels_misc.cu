@@ -607,6 +607,24 @@ cudaError_t misc_init_attributes() {
     return cudaFuncSetAttribute(dft2_rows_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dft_smem);
 }
 
+int device_sms() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];  // 0: not queried yet
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return 1;
+    }
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        v = 1;
+    }
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s) {
     if (T <= 0) return cudaSuccess;
     dim3 grid((unsigned)std::min<size_t>((npix / 4 + 255) / 256 + 1, 64), T);
@@ -617,7 +635,7 @@ cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T,
 
 cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, device_sms() * 8);
     scan_nonfinite_kernel<<<blocks, 256, 0, s>>>(p, n, flags);
     count_launch();
     return cudaGetLastError();
@@ -716,7 +734,7 @@ cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* 
 
 cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, device_sms() * 16);
     fill_kernel<<<blocks, 256, 0, s>>>(p, n, v);
     count_launch();
     return cudaGetLastError();
@@ -724,7 +742,7 @@ cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s) {
 
 cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, device_sms() * 16);
     fista_kernel<<<blocks, 256, 0, s>>>(rec, prev, n, factor);
     count_launch();
     return cudaGetLastError();
@@ -739,7 +757,7 @@ cudaError_t launch_bayes_conv(const float* rec, float* dist, int W, int H, int D
 
 cudaError_t launch_bayes_apply(float* rec, float* dist, size_t n, double alpha, int positivity, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, device_sms() * 16);
     bayes_apply_kernel<<<blocks, 256, 0, s>>>(rec, dist, n, alpha, positivity);
     count_launch();
     return cudaGetLastError();
@@ -754,7 +772,7 @@ cudaError_t launch_bgart_collapse(float* vol, size_t n, double k, int dark_bg, d
     if ((e = cudaMemsetAsync(keys, 0xFF, 4, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(keys + 1, 0, 4, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(hist, 0, 256 * 8, s)) != cudaSuccess) return e;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, device_sms() * 8);
     bg_minmax_kernel<<<blocks, 256, 0, s>>>(vol, n, keys);
     bg_hist_kernel<<<blocks, 256, 0, s>>>(vol, n, keys, hist);
     bg_finalize_kernel<<<1, 1, 0, s>>>(keys, hist, k, bg_value, out);

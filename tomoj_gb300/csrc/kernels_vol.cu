@@ -130,7 +130,8 @@ __global__ void scan16_kernel(const uint16_t* __restrict__ vol, size_t n, int* f
 
 int grid_for(size_t n) {
     const size_t g = (n + kThreads - 1) / kThreads;
-    return (int)(g < 152 * 64 ? (g == 0 ? 1 : g) : 152 * 64);
+    const size_t cap = (size_t)device_sms() * 64;
+    return (int)(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
 }  // namespace

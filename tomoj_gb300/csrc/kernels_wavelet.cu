@@ -37,7 +37,6 @@ constexpr int kWavTwN = 8192;      // twiddle table e^{-2 pi i k / 8192}, k < 61
 constexpr int kWavMaxPow2 = 8192;  // longest power-of-two line
 constexpr int kWavMaxOther = 4096; // longest other line (Bluestein grid <= 8192)
 constexpr int kWavTailK = 256;
-constexpr int kWavSMs = 152;      // streaming multiprocessors of the part
 
 struct WavState {
     unsigned long long maxkey;  // max |v| as double bits (non-negative: ordered as integers)
@@ -507,7 +506,7 @@ WaveletPlan* wavelet_plan_create(int W, int H, int D, const int iters[3], int ty
         q.nt = 4;
         while (q.nt < kWavThreads && q.nt < work) q.nt <<= 1;
         q.groups = kWavThreads / q.nt;
-        while (q.groups > 1 && pairs / q.groups < 2LL * kWavSMs) q.groups >>= 1;
+        while (q.groups > 1 && pairs / q.groups < 2LL * device_sms()) q.groups >>= 1;
         q.stride = q.n + (int)std::max(dft_scratch(q.full), dft_scratch(q.half));
         q.smem = sizeof(double2) * (size_t)q.groups * q.stride;
         P->smem_max = std::max(P->smem_max, q.smem);
@@ -564,7 +563,7 @@ int wavelet_plan_passes(const WaveletPlan* P) { return (int)P->passes.size(); }
 cudaError_t launch_wavelet_filter(const WaveletPlan* P, float* vol, cudaStream_t s) {
     const size_t n = (size_t)P->W * P->H * P->D;
     if (n == 0) return cudaSuccess;
-    const int blocks = (int)std::min<size_t>((n + kWavThreads - 1) / kWavThreads, 152 * 8);
+    const int blocks = (int)std::min<size_t>((n + kWavThreads - 1) / kWavThreads, device_sms() * 8);
     auto dft_of = [&](const WaveletPlan::Dft& d) {
         WavDft r;
         r.n = d.n;

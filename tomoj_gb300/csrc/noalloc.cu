@@ -16,8 +16,11 @@
 // error message for tomo_last_error).
 //
 // Limits: nproj <= 128 tilts in the series, <= 64 tilts per call, w <= 2048,
-// h <= 2048, D <= 65535, vertical tilt axis (separable geometry); larger sizes
-// are rejected with TOMO_ERR_INVALID / TOMO_ERR_UNSUPPORTED.
+// h <= 2048, D <= 65535, W such that one plane row and its pairs fit the forward
+// projector's shared memory (W up to about 9500), vertical tilt axis (separable
+// geometry); larger sizes are rejected with TOMO_ERR_INVALID / TOMO_ERR_UNSUPPORTED.
+// Long-object compensation (setLongObjectCompensation) is not applied: the norms
+// and differences are those of the plain projector.
 //
 // The first call on each device does the set-up (cudaGetSymbolAddress of the
 // scratch array and the kernels' shared-memory attributes) with that device
@@ -60,8 +63,9 @@ constexpr size_t kNoAllocScratchBytes = kStatusOff + 256;                       
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Host-side scratch (file scope: the call does not touch the heap).
-static FpRay h_rays[kMaxW];
+// Host-side scratch (file scope: the call does not touch the heap).  Every tilt of a
+// call has its own ray-table slot, so all uploads are queued before one synchronisation.
+static FpRay h_rays[kMaxBatch][kMaxW];
 static FpTilt h_tilts[kMaxNproj];
 static float h_normtab[kMaxD + 2];
 static int h_batch[kMaxBatch];
@@ -73,50 +77,6 @@ static void* g_dev_scratch[kMaxDevices];
 tomo_status nerr(tomo_status code, const char* msg) {
     set_last_error(msg);
     return code;
-}
-
-// The forward-projection table builder of geometry.cpp without heap use: the
-// norm table lives in h_normtab and the border replay keeps no per-plane flags.
-void build_fp_tables_static(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays) {
-    constexpr double kAcc = (double)1e-10f;
-    const double dirY = -(R[5] - R[3] * R[2] / R[0]) / (R[4] - R[3] * R[1] / R[0]);
-    const double dirX = (R[1] * (-dirY) - R[2]) / R[0];
-    const double ninc = std::sqrt(dirX * dirX + dirY * dirY + 1);
-    const double vcx = g.vc[0], vcz = g.vc[2];
-    const double bXmax = (double)((float)g.W + 1e-10f);
-    tilt->step = (long long)std::llrint(dirX * kFix);
-    tilt->ninc = ninc;
-    const int D = g.D;
-    h_normtab[0] = 0.0f;
-    for (int k = 1; k < D + 2; k++) h_normtab[k] = (float)((double)h_normtab[k - 1] + ninc);
-    for (int i = 0; i < g.w; i++) {
-        const double icentered = (i - g.pc[0]) / g.scale;
-        double oldx0 = icentered - R[1] * 0.0 - R[2] * (-1 - vcz);
-        oldx0 /= R[0];
-        // the reference's own accumulation, stopped at the first plane after the run
-        int lo = -1, cnt = 0;
-        double oldx = oldx0;
-        for (int z = 0; z < D; z++) {
-            const double xc = oldx + dirX;
-            const double x = xc + vcx;
-            const bool in = x + kAcc >= 0 && x < bXmax;
-            if (in) {
-                if (lo < 0) lo = z;
-                cnt++;
-            } else if (lo >= 0) {
-                break;
-            }
-            oldx = xc;
-        }
-        if (lo < 0) lo = 0;
-        int incr = cnt;
-        if (cnt > 0 && lo + cnt - 1 < D - 1) incr++;
-        FpRay r;
-        r.zab = (int32_t)((uint32_t)lo | ((uint32_t)cnt << 16));
-        r.norm = cnt > 0 ? h_normtab[incr] : 0.0f;
-        r.X0 = (long long)std::llrint((oldx0 + dirX + vcx) * kFix);
-        rays[i] = r;
-    }
 }
 
 tomo_status device_scratch(unsigned char** out) {
@@ -161,6 +121,10 @@ extern "C" tomo_status tomo_project_and_difference_noalloc(const tomo_geom* geom
         return nerr(TOMO_ERR_INVALID, "projections larger than 2048 x 2048");
     if (geom->W <= 0 || geom->H <= 0 || geom->D <= 0 || geom->D > kMaxD)
         return nerr(TOMO_ERR_INVALID, "bad volume size");
+    // the forward projector stages at least one plane row of W voxels (and its pairs) in
+    // shared memory: wider volumes are refused before anything is uploaded
+    if (fp_qp(geom->w) == 0 || fp_smem_bytes(1, geom->W, fp_qp(geom->w), 1) > kFpSmemBudget)
+        return nerr(TOMO_ERR_INVALID, "volume width W too large for the forward projector's shared memory");
     Geometry g{};
     g.W = geom->W;
     g.H = geom->H;
@@ -188,14 +152,14 @@ extern "C" tomo_status tomo_project_and_difference_noalloc(const tomo_geom* geom
     double* d_err = reinterpret_cast<double*>(scr + kErrOff);
     int* d_batch = reinterpret_cast<int*>(scr + kBatchOff);
     int* d_status = reinterpret_cast<int*>(scr + kStatusOff);
-    // ray tables of the requested tilts, in their series slots
+    // ray tables of the requested tilts (the closed-form intervals of the handle path; only
+    // rays that graze a border replay the reference's accumulation), in their series slots
     for (int b = 0; b < T; b++) {
         const int t = tilts[b];
-        build_fp_tables_static(g, euler + 9 * (size_t)t, &h_tilts[t], h_rays);
-        if (cudaMemcpyAsync(d_rays + (size_t)t * g.w, h_rays, sizeof(FpRay) * g.w, cudaMemcpyHostToDevice, s) !=
+        build_fp_tables(g, euler + 9 * (size_t)t, &h_tilts[t], h_rays[b], h_normtab);
+        if (cudaMemcpyAsync(d_rays + (size_t)t * g.w, h_rays[b], sizeof(FpRay) * g.w, cudaMemcpyHostToDevice, s) !=
                 cudaSuccess ||
-            cudaMemcpyAsync(d_ft + t, &h_tilts[t], sizeof(FpTilt), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess) {  // the host tables are reused by the next tilt
+            cudaMemcpyAsync(d_ft + t, &h_tilts[t], sizeof(FpTilt), cudaMemcpyHostToDevice, s) != cudaSuccess) {
             cudaGetLastError();
             return nerr(TOMO_ERR_CUDA, "table upload failed");
         }

@@ -269,6 +269,7 @@ tomo_status run_fp(tomo_projector* p, const int* d_tilts, int T, int y0, bool wi
     a.h = g.h;
     a.row_off = g.fp_row_off;
     a.status = p->d_status;
+    a.hold_first_copy = p->hold_first_copy;
     CK(launch_fp_separable(a, p->stream));
     if (p->params.long_object) {
         CK(launch_long_object(norm, T, g.h, g.w, p->stream));
@@ -309,6 +310,7 @@ tomo_status run_fp_range(tomo_projector* p, const int* d_tilts, int T, int j0, i
     a.h = g.h;
     a.row_off = g.fp_row_off;
     a.status = p->d_status;
+    a.hold_first_copy = p->hold_first_copy;
     CK(launch_fp_separable(a, p->stream));
     return TOMO_OK;
 }
@@ -1390,6 +1392,12 @@ tomo_status tomo_profile_read(tomo_projector* p, double* out4) {
 tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n) {
     if (!p || n < 0) return fail(TOMO_ERR_INVALID, "bad argument");
     p->tilts_per_cta = n;
+    return TOMO_OK;
+}
+
+tomo_status tomo_debug_hold_first_copy(tomo_projector* p, int32_t enabled) {
+    if (!p) return fail(TOMO_ERR_INVALID, "null handle");
+    p->hold_first_copy = enabled != 0;
     return TOMO_OK;
 }
 

@@ -114,6 +114,7 @@ struct tomo_projector {
     void* bp_target() const { return bayes ? static_cast<void*>(d_dist) : vol(); }
     std::atomic<int> cancel{0};
     int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+    int hold_first_copy = 0;  // failure-path test hook of the forward projector (tomo_debug_hold_first_copy)
     // row streams: K row ranges of an OS-SART iteration run on K streams (rows are
     // independent), so that forward and backprojections of different rows overlap
     int row_streams = 1;

@@ -85,7 +85,9 @@ bool tilt_is_vertical(const double* R);
 // (-1 outside) and blend weight (ImageJ getInterpolatedValue's y weight).
 void build_fp_rowmap(const Geometry& g, int j0, int* row, float* yf);
 void build_bp_rowmap(const Geometry& g, int* row, float* yf);
-void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays /* w entries */);
+// normtab_scratch: D + 2 floats the builder may use (nullptr: it allocates its own).
+void build_fp_tables(const Geometry& g, const double* R, FpTilt* tilt, FpRay* rays /* w entries */,
+                     float* normtab_scratch = nullptr);
 void build_bp_tables(const Geometry& g, const double* R, BpTilt* tilt, int32_t* zint /* W entries */);
 void build_generic_fp_tilt(const double* R, GenericFpTilt* out);
 // M-point spectrum (M a power of two >= 2w - 1) of the real circular kernel
@@ -143,7 +145,12 @@ struct FpLaunch {
     const int* rowmap;
     const float* rowyf;
     int two_rows;           // shared memory holds both rows of every plane
+    // Failure-path test hook (tomo_debug_hold_first_copy): the first chunk's bulk copies
+    // are never issued, so its mbarrier wait runs out after kHoldWaitTries polls and the
+    // CTA reports kStatusTimeout and returns (nothing is in flight).  0 in normal use.
+    int hold_first_copy;
 };
+constexpr uint32_t kHoldWaitTries = 1u << 12;
 cudaError_t launch_fp_separable(const FpLaunch& a, cudaStream_t s);
 // Any geometry (kernels_generic.cu): one thread per ray / voxel in the reference's
 // double arithmetic.  proj/norm are [T][h][w] in batch order.
@@ -315,6 +322,10 @@ cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, const unsign
                                int* status, cudaStream_t s);
 cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, size_t nvox, int H, float value, cudaStream_t s);
 cudaError_t launch_scan_nonfinite_vol(const void* vol, int vtype, size_t n, int* flags, cudaStream_t s);
+
+// Streaming multiprocessors of the current device (queried once per device ordinal and
+// cached; 1 if the query fails).  Grid sizes of the grid-stride kernels scale with it.
+int device_sms();
 
 // Sets the calling thread's message for tomo_last_error.
 void set_last_error(const char* msg);
