@@ -173,6 +173,7 @@ def test_expired_wait_reports_device_error_and_handle_recovers(engine, oracle_li
         _abi.check(engine.tomo_debug_hold_first_copy(h, 0))
         # same handle, status cleared: a correct projection
         _abi.check(engine.tomo_set_volume(h, vol.ctypes.data, 0, 0, c["H"]))
+        _abi.check(engine.tomo_clear_projections(h))
         for i in range(c["n"]):
             _abi.check(engine.tomo_add_projection(h, i))
         _abi.check(engine.tomo_project(h, 0, c["H"]))

@@ -114,7 +114,7 @@ def test_normalized_alignment_matches_oracle(engine, oracle_lib, norm_case, fill
             ok = ~np.isnan(ref)
             assert np.abs(got[ok] - ref[ok]).max() <= 1e-6 * max(1.0, np.abs(ref[ok]).max()), i
             # the normalised image really is centred and scaled by the ROI statistics
-            raw = O.align(c["series"][i], c["T"][i], fill=ofill)
+            raw = O.align(c["series"][i], c["T"][i], False, mean, std, fill=ofill)  # average fill = the mean
             assert np.allclose(ref[ok], (raw[ok] - mean) / std, rtol=1e-5, atol=1e-5)
     finally:
         engine.tomo_destroy(h)

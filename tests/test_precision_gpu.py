@@ -12,8 +12,10 @@ norms FP64.  Tolerances:
   Its 1e-3 case is an expected failure (strict: it must keep failing, so a change
   that made it pass would be noticed); a second test keeps it below the 6e-3 it
   measures, so that it does not get worse.  FP16 is the storage that meets 1e-3.
-* A forward projection of a reduced volume is bit-identical to the FP32 forward
-  projection of the same values (power-of-two scales commute with rounding).
+* A forward projection of a reduced volume samples half2 pairs (v - d, d) built from
+  the stored values (one FP16 rounding per pair, in units of the row's slab scale):
+  it matches the FP32 forward projection of the same values to <= 1e-4 relative L2
+  per tilt, with the same NaN pattern and the same norms.
 """
 from __future__ import annotations
 
@@ -98,7 +100,7 @@ def test_reduced_volume_roundtrip_uses_slab_scales(engine, name):
 
 
 @pytest.mark.parametrize("name", sorted(PRECS))
-def test_reduced_forward_projection_is_bitwise_fp32_of_stored_values(engine, name):
+def test_reduced_forward_projection_matches_fp32_of_stored_values(engine, name):
     c = series_case(W=64, H=8, D=40, n=9, seed=5)
     red = RHandle(engine, c, PRECS[name])
     ref = RHandle(engine, c, _abi.PREC_FP32)
@@ -116,7 +118,13 @@ def test_reduced_forward_projection_is_bitwise_fp32_of_stored_values(engine, nam
             b = np.empty_like(a)
             _abi.check(engine.tomo_get_projection(red.h, i, _abi.ptr(a)))
             _abi.check(engine.tomo_get_projection(ref.h, i, _abi.ptr(b)))
-            assert np.array_equal(a, b, equal_nan=True)
+            assert np.array_equal(np.isnan(a), np.isnan(b))
+            assert rel_l2(a, b) <= 1e-4, (i, rel_l2(a, b))
+            na = np.empty_like(a)
+            nb = np.empty_like(a)
+            _abi.check(engine.tomo_get_norm(red.h, i, _abi.ptr(na)))
+            _abi.check(engine.tomo_get_norm(ref.h, i, _abi.ptr(nb)))
+            assert np.array_equal(na, nb)
     finally:
         red.close()
         ref.close()

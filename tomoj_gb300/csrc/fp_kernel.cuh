@@ -21,6 +21,9 @@
 // fp_kernel_q*.cu translation units.
 #pragma once
 #include <cmath>
+#include <type_traits>
+
+#include <cuda_fp16.h>
 
 #include "device_util.cuh"
 #include "tomo_internal.h"
@@ -39,15 +42,16 @@ struct Smem {
 };
 
 // Shared memory: mbarrier | raw chunk [rows][ZC][W] | pairs [ZC][W+4] | reduction scratch | steps.
-__host__ __device__ inline Smem layout(int ZC, int W, int tgmax, int rows = 1) {
+// PK (pair kind) 0: FP32 rows and float2 pairs; 1: 16-bit rows and half2 pairs.
+__host__ __device__ inline Smem layout(int ZC, int W, int tgmax, int rows = 1, int PK = 0) {
     Smem L;
     L.PW = W + 4;
     size_t o = 16;
     L.raw_off = o;
-    o += (size_t)rows * ZC * W * sizeof(float);
+    o += (size_t)rows * ZC * W * (PK ? sizeof(uint16_t) : sizeof(float));
     o = (o + 15) & ~(size_t)15;
     L.pair_off = o;
-    o += (size_t)ZC * L.PW * sizeof(float2);
+    o += (size_t)ZC * L.PW * (PK ? sizeof(uint32_t) : sizeof(float2));
     o = (o + 15) & ~(size_t)15;
     L.red_off = o;
     o += (kThreads / 32) * sizeof(double);
@@ -110,6 +114,39 @@ __device__ __forceinline__ void pair1_16(const uint16_t* __restrict__ src, float
     float d = (k + 1 < W) ? vol_load16<VT>(src[k + 1]) - v : 0.0f;
     if (flat) d = 0.0f;
     dst[k + 2] = make_float2(v - d, d);
+}
+
+// Half2 pairs of a 16-bit row (PK 1): the pair of slot k is (v_k - d_k, d_k) computed in
+// FP32 from the stored values and rounded once to FP16 (both in units of the row's slab
+// scale, whose maximum is in [16, 32), so the FP16 range is never left): a sample is one
+// 32-bit shared load, two conversions and one FMA, and the gathers move half the bytes.
+__device__ __forceinline__ uint32_t hpair(float v, float d) {
+    const __half2 h = __floats2half2_rn(v - d, d);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+template <int VT>
+__device__ __forceinline__ void hpairs4_16(const uint16_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int m,
+                                           bool flat) {
+    const uint2 u = *reinterpret_cast<const uint2*>(src + 4 * m);
+    const float vx = vol_load16<VT>((uint16_t)(u.x & 0xFFFFu)), vy = vol_load16<VT>((uint16_t)(u.x >> 16));
+    const float vz = vol_load16<VT>((uint16_t)(u.y & 0xFFFFu)), vw = vol_load16<VT>((uint16_t)(u.y >> 16));
+    const float nx = (4 * m + 4 < W) ? vol_load16<VT>(src[4 * m + 4]) : vw;
+    float d0 = vy - vx, d1 = vz - vy, d2 = vw - vz, d3 = nx - vw;
+    if (flat) d0 = d1 = d2 = d3 = 0.0f;
+    // slot 4m + 2 is 8-byte aligned (W + 4 words per row, rows start 16-byte aligned)
+    uint2* o = reinterpret_cast<uint2*>(dst + 4 * m + 2);
+    o[0] = make_uint2(hpair(vx, d0), hpair(vy, d1));
+    o[1] = make_uint2(hpair(vz, d2), hpair(vw, d3));
+}
+
+template <int VT>
+__device__ __forceinline__ void hpair1_16(const uint16_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int k,
+                                          bool flat) {
+    const float v = vol_load16<VT>(src[k]);
+    float d = (k + 1 < W) ? vol_load16<VT>(src[k + 1]) - v : 0.0f;
+    if (flat) d = 0.0f;
+    dst[k + 2] = hpair(v, d);
 }
 
 // Pair k of a row blended between volume rows r (src0) and r + 1 (src1) with weight
@@ -206,8 +243,45 @@ __device__ __forceinline__ void build_pairs_chunk(const void* raw, const float* 
     }
 }
 
+// All half2 pairs of a staged chunk of zc 16-bit plane rows (PK 1).
+__device__ __forceinline__ void build_hpairs_chunk(const uint16_t* r16, uint32_t* __restrict__ pairs, int W, int PW,
+                                                   int zc, int vt, bool last_row, int zflat) {
+    auto flat = [&](int zz) { return last_row || zz == zflat; };
+    if (vt == kVolBF16) {
+        if ((W & 3) == 0)
+            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+                hpairs4_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
+            });
+        else
+            for_chunk_groups(zc, W, [&](int zz, int k) {
+                hpair1_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
+            });
+    } else {
+        if ((W & 3) == 0)
+            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+                hpairs4_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
+            });
+        else
+            for_chunk_groups(zc, W, [&](int zz, int k) {
+                hpair1_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
+            });
+    }
+    for (int e = threadIdx.x; e < zc * 4; e += kThreads) {
+        const int zz = e >> 2, t = e & 3;
+        const int col = (t < 2) ? 0 : W - 1;
+        const float v = vol_load16_rt(vt, r16[(size_t)zz * W + col]);
+        const int k = (t < 2) ? t - 2 : W + t - 2;  // -2, -1, W, W+1
+        pairs[(size_t)zz * PW + k + 2] = hpair(v, 0.0f);
+    }
+}
+
 __device__ __forceinline__ float sample(const float2* __restrict__ P, long long x) {
     const float2 p = P[(int)(x >> 32)];
+    return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
+}
+
+__device__ __forceinline__ float sample(const __half2* __restrict__ P, long long x) {
+    const float2 p = __half22float2(P[(int)(x >> 32)]);
     return fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
 }
 
@@ -227,13 +301,19 @@ struct PartialOut {
     long long x;
     float s;
 };
-static __device__ __noinline__ PartialOut partial_chunk(const float2* __restrict__ P, long long x, long long step, int lo,
-                                                 int cnt, int zc) {
+__device__ __forceinline__ float2 pair_at(const float2* __restrict__ P, long long x) { return P[(int)(x >> 32)]; }
+__device__ __forceinline__ float2 pair_at(const __half2* __restrict__ P, long long x) {
+    return __half22float2(P[(int)(x >> 32)]);
+}
+
+template <class PT>
+static __device__ __noinline__ PartialOut partial_chunk(const PT* __restrict__ P, long long x, long long step, int lo,
+                                                        int cnt, int zc) {
     float s = 0.0f;
     for (int zz = 0; zz < zc; zz++) {
         const bool in = (unsigned)(zz - lo) < (unsigned)cnt;
         float2 p = make_float2(0.0f, 0.0f);
-        if (in) p = P[(int)(x >> 32)];
+        if (in) p = pair_at(P, x);
         s += fmaf(fix_one_plus_frac((uint32_t)x), p.y, p.x);
         x += step;
     }
@@ -242,8 +322,8 @@ static __device__ __noinline__ PartialOut partial_chunk(const float2* __restrict
 
 // Full chunk of one ray (all ZC planes inside): two interleaved sub-chains (even / odd
 // planes).  Returns the position after ZC steps and the chunk's sum.
-template <int ZC>
-__device__ __forceinline__ PartialOut full_chunk_inl(const float2* __restrict__ P, long long x, long long step) {
+template <int ZC, class PT>
+__device__ __forceinline__ PartialOut full_chunk_inl(const PT* __restrict__ P, long long x, long long step) {
     const long long s2 = 2 * step;
     long long x0 = x, x1 = x + step;
     float a0 = 0.0f, a1 = 0.0f;
@@ -261,16 +341,19 @@ __device__ __forceinline__ PartialOut full_chunk_inl(const float2* __restrict__ 
 // depth part zp of a.zparts.
 // BLEND: the fractional-row form (row maps, two staged rows per plane).  A separate
 // instantiation, so that the whole-row kernels compile without any of it.
-template <int QP, int ZC, bool BLEND>
+// PK: pair kind (0: FP32 volume, float2 pairs; 1: 16-bit volume, half2 pairs).
+template <int QP, int ZC, bool BLEND, int PK>
 __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma,
                                         const int zp) {
+    static_assert(!(BLEND && PK), "the fractional-row form is FP32 only");
+    using PairT = typename std::conditional<PK == 1, __half2, float2>::type;
     constexpr int TGMAX = kFpRays / QP > 0 ? kFpRays / QP : 1;
     constexpr int NR = TGMAX * QP;
     extern __shared__ __align__(16) unsigned char smem[];
-    const Smem L = layout(ZC, a.W, TGMAX, BLEND ? 2 : 1);
+    const Smem L = layout(ZC, a.W, TGMAX, BLEND ? 2 : 1, PK);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     float* raw = reinterpret_cast<float*>(smem + L.raw_off);
-    float2* pairs = reinterpret_cast<float2*>(smem + L.pair_off);
+    PairT* pairs = reinterpret_cast<PairT*>(smem + L.pair_off);
     double* red = reinterpret_cast<double*>(smem + L.red_off);
     long long* s_step = reinterpret_cast<long long*>(smem + L.step_off);
 
@@ -376,11 +459,15 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             } else {
                 __syncthreads();
             }
-            build_pairs_chunk(raw, raw1, pairs, W, PW, zc, vt, BLEND && blend, yf, last_row,
-                              D - 1 - z0 < zc ? D - 1 - z0 : -1);
+            if (PK == 1)
+                build_hpairs_chunk(reinterpret_cast<const uint16_t*>(raw), reinterpret_cast<uint32_t*>(pairs), W, PW,
+                                   zc, vt, last_row, D - 1 - z0 < zc ? D - 1 - z0 : -1);
+            else
+                build_pairs_chunk(raw, raw1, reinterpret_cast<float2*>(pairs), W, PW, zc, vt, BLEND && blend, yf,
+                                  last_row, D - 1 - z0 < zc ? D - 1 - z0 : -1);
             __syncthreads();
             if (c + 1 < c_end && use_tma) stage(c + 1);
-            const float2* P = pairs + 2;
+            const PairT* P = pairs + 2;
             // ray slot k over this chunk: full (unrolled chains), none (skip) or partial
             auto one = [&](int k) {
                 const long long st = s_step[k / QP];
@@ -500,28 +587,32 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     }
 }
 
-template <int QP, int ZC, bool BLEND>
+template <int QP, int ZC, bool BLEND, int PK>
 __global__ void __launch_bounds__(kThreads, kFpCtasPerSm) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
-    fp_body<QP, ZC, BLEND>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
+    fp_body<QP, ZC, BLEND, PK>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
 }
 
-// Batched form: CTA b works on item {problem, first tilt, row, use_tma} of many problems.
-template <int QP, int ZC>
+// Batched form: CTA b works on item {problem, first tilt, row, use_tma} of many problems
+// (all of pair kind PK: FP32 and 16-bit volumes go to separate launches).
+template <int QP, int ZC, int PK>
 __global__ void __launch_bounds__(kThreads, kFpCtasPerSm)
     fp_kernel_batch(const FpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
-    fp_body<QP, ZC, false>(descs[it.x], it.y, it.z, it.w, 0);
+    fp_body<QP, ZC, false, PK>(descs[it.x], it.y, it.z, it.w, 0);
 }
 
 template <int QP, int ZC>
 cudaError_t set_attr_one() {
-    cudaError_t e = cudaFuncSetAttribute(fp_kernel<QP, ZC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kMaxSmem);
+    const int m = (int)kMaxSmem;
+    cudaError_t e = cudaFuncSetAttribute(fp_kernel<QP, ZC, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(fp_kernel<QP, ZC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    e = cudaFuncSetAttribute(fp_kernel<QP, ZC, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(fp_kernel_batch<QP, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kMaxSmem);
+    e = cudaFuncSetAttribute(fp_kernel<QP, ZC, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(fp_kernel_batch<QP, ZC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fp_kernel_batch<QP, ZC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
 template <int QP>
@@ -536,15 +627,18 @@ cudaError_t set_attr_qp() {
 
 template <int QP, int ZC>
 void launch_zc(const FpLaunch& a, dim3 grid, size_t smem, int use_tma, cudaStream_t s) {
-    if (a.two_rows) fp_kernel<QP, ZC, true><<<grid, kThreads, smem, s>>>(a, use_tma);
-    else fp_kernel<QP, ZC, false><<<grid, kThreads, smem, s>>>(a, use_tma);
+    if (a.two_rows) fp_kernel<QP, ZC, true, 0><<<grid, kThreads, smem, s>>>(a, use_tma);
+    else if (a.vtype != kVolF32) fp_kernel<QP, ZC, false, 1><<<grid, kThreads, smem, s>>>(a, use_tma);
+    else fp_kernel<QP, ZC, false, 0><<<grid, kThreads, smem, s>>>(a, use_tma);
 }
 
 template <int QP>
 cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     const int rows = a.two_rows ? 2 : 1;
-    const int ZC = fp_choose_zc(a.W, rows);
-    const Smem L = layout(ZC, a.W, kFpRays / QP > 0 ? kFpRays / QP : 1, rows);
+    const int PK = a.vtype != kVolF32 ? 1 : 0;
+    if (PK && a.two_rows) return cudaErrorInvalidValue;
+    const int ZC = fp_choose_zc(a.W, rows, a.vtype);
+    const Smem L = layout(ZC, a.W, kFpRays / QP > 0 ? kFpRays / QP : 1, rows, PK);
     if (L.total > kMaxSmem) return cudaErrorInvalidValue;
     const int use_tma = fp_use_tma(a.W, a.vtype, a.vol);
     dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0, a.zparts > 1 ? a.zparts : 1);
@@ -559,18 +653,24 @@ cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int QP, int PK>
+void launch_batch_pk(const FpLaunch* descs, const int4* items, int n_items, int ZC, size_t smem, cudaStream_t s) {
+    switch (ZC) {
+        case 16: fp_kernel_batch<QP, 16, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 8: fp_kernel_batch<QP, 8, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 4: fp_kernel_batch<QP, 4, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 2: fp_kernel_batch<QP, 2, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        default: fp_kernel_batch<QP, 1, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
+    }
+}
+
 template <int QP>
-cudaError_t launch_batch_qp(const FpLaunch* descs, const int4* items, int n_items, int ZC, size_t smem,
+cudaError_t launch_batch_qp(const FpLaunch* descs, const int4* items, int n_items, int ZC, size_t smem, int pk,
                             cudaStream_t s) {
     if (n_items <= 0) return cudaSuccess;
     if (smem > kMaxSmem) return cudaErrorInvalidValue;
-    switch (ZC) {
-        case 16: fp_kernel_batch<QP, 16><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        case 8: fp_kernel_batch<QP, 8><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        case 4: fp_kernel_batch<QP, 4><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        case 2: fp_kernel_batch<QP, 2><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        default: fp_kernel_batch<QP, 1><<<n_items, kThreads, smem, s>>>(descs, items); break;
-    }
+    if (pk) launch_batch_pk<QP, 1>(descs, items, n_items, ZC, smem, s);
+    else launch_batch_pk<QP, 0>(descs, items, n_items, ZC, smem, s);
     count_launch();
     return cudaGetLastError();
 }
@@ -583,8 +683,8 @@ cudaError_t launch_batch_qp(const FpLaunch* descs, const int4* items, int n_item
     namespace tomo {                                                                                     \
     cudaError_t fp_launch_q##QP(const FpLaunch& a, cudaStream_t s) { return fpk::launch_qp<QP>(a, s); } \
     cudaError_t fp_attr_q##QP() { return fpk::set_attr_qp<QP>(); }                                     \
-    cudaError_t fp_batch_q##QP(const FpLaunch* d, const int4* it, int n, int zc, size_t smem,            \
+    cudaError_t fp_batch_q##QP(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk,    \
                                cudaStream_t s) {                                                         \
-        return fpk::launch_batch_qp<QP>(d, it, n, zc, smem, s);                                          \
+        return fpk::launch_batch_qp<QP>(d, it, n, zc, smem, pk, s);                                      \
     }                                                                                                    \
     }

@@ -127,7 +127,14 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
     // 16 * H * W below 2^32, so the offsets are 32-bit products of a uniform value
     const unsigned plane = (unsigned)H * (unsigned)W;
     const float vsc = (VT == kVolF32) ? 1.0f : a.vscale[r];
-    float vox[kNC][kKZ], comp[kNC][kKZ];
+    // Reduced storage without the per-add NaN/Inf/positivity rules: the tilts of a staged
+    // chunk are summed in `part` (plain FP32, at most 32 terms) and each chunk's sum is
+    // added to the voxel with Kahan compensation, the compensation terms parked in shared
+    // memory between chunks (read and written once per chunk).  With the per-add rules
+    // every add is compensated (bp_add_kahan).
+    constexpr bool CHUNK_KAHAN = (VT != kVolF32) && !SANITIZE && !POS;
+    __shared__ float comp_sh[CHUNK_KAHAN ? kNC * kKZ * kThr : 1];
+    float vox[kNC][kKZ], comp[kNC][kKZ], part[kNC][kKZ];
     int nk[kNC];
 #pragma unroll
     for (int c = 0; c < kNC; c++) {
@@ -144,7 +151,11 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
             for (int k = 0; k < kKZ; k++) vox[c][k] = (k < nk[c]) ? vol_load16<VT>(vb[k * plane]) * vsc : 0.0f;
         }
 #pragma unroll
-        for (int k = 0; k < kKZ; k++) comp[c][k] = 0.0f;
+        for (int k = 0; k < kKZ; k++) {
+            comp[c][k] = 0.0f;
+            part[c][k] = 0.0f;
+            if (CHUNK_KAHAN) comp_sh[(c * kKZ + k) * kThr + tid] = 0.0f;
+        }
     }
 
     const int xa = x0, xb = min(x0 + kTX - 1, W - 1);
@@ -255,10 +266,15 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
                     for (int k = 0; k < kKZ; k += 2) {
                         const float2 p0 = sh.seg[(int)(X >> 32)];
                         const float2 p1 = sh.seg[(int)(X1 >> 32)];
-                        bp_acc<SANITIZE, POS, VT>(vox[c][k], comp[c][k],
-                                                  fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x));
-                        bp_acc<SANITIZE, POS, VT>(vox[c][k + 1], comp[c][k + 1],
-                                                  fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x));
+                        const float s0 = fmaf(fix_one_plus_frac((uint32_t)X), p0.y, p0.x);
+                        const float s1 = fmaf(fix_one_plus_frac((uint32_t)X1), p1.y, p1.x);
+                        if (CHUNK_KAHAN) {
+                            part[c][k] += s0;
+                            part[c][k + 1] += s1;
+                        } else {
+                            bp_acc<SANITIZE, POS, VT>(vox[c][k], comp[c][k], s0);
+                            bp_acc<SANITIZE, POS, VT>(vox[c][k + 1], comp[c][k + 1], s1);
+                        }
                         X += S2;
                         X1 += S2;
                     }
@@ -267,13 +283,28 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
                     for (int k = 0; k < kKZ; k++) {
                         if ((unsigned)(k - kl) < (unsigned)cnt) {
                             const float2 p = sh.seg[(int)(X >> 32)];
-                            bp_acc<SANITIZE, POS, VT>(vox[c][k], comp[c][k],
-                                                      fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x));
+                            const float sv = fmaf(fix_one_plus_frac((uint32_t)X), p.y, p.x);
+                            if (CHUNK_KAHAN) part[c][k] += sv;
+                            else bp_acc<SANITIZE, POS, VT>(vox[c][k], comp[c][k], sv);
                         }
                         X += S;
                     }
                 }
             }
+        }
+        if (CHUNK_KAHAN) {
+#pragma unroll
+            for (int c = 0; c < kNC; c++)
+#pragma unroll
+                for (int k = 0; k < kKZ; k++) {
+                    float cp = comp_sh[(c * kKZ + k) * kThr + tid];
+                    const float y = part[c][k] - cp;
+                    const float t = vox[c][k] + y;
+                    cp = (t - vox[c][k]) - y;
+                    vox[c][k] = t;
+                    comp_sh[(c * kKZ + k) * kThr + tid] = cp;
+                    part[c][k] = 0.0f;
+                }
         }
         __syncthreads();
     }
@@ -295,7 +326,7 @@ __device__ __forceinline__ void bp_body(const BpLaunch& a, const int x0, const i
 #pragma unroll
             for (int k = 0; k < kKZ; k++) {
                 if (k < nk[c]) {
-                    const float v = vox[c][k] - comp[c][k];
+                    const float v = vox[c][k] - (CHUNK_KAHAN ? comp_sh[(c * kKZ + k) * kThr + tid] : comp[c][k]);
                     m = fmaxf(m, fabsf(v));
                     float q = v * inv;
                     if (VT == kVolF16 && fabsf(q) > kF16Max && isfinite(q)) {

@@ -15,11 +15,11 @@ cudaError_t fp_attr_q2();
 cudaError_t fp_attr_q4();
 cudaError_t fp_attr_q8();
 cudaError_t fp_attr_q16();
-cudaError_t fp_batch_q1(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
-cudaError_t fp_batch_q2(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
-cudaError_t fp_batch_q4(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
-cudaError_t fp_batch_q8(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
-cudaError_t fp_batch_q16(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, cudaStream_t s);
+cudaError_t fp_batch_q1(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
+cudaError_t fp_batch_q2(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
+cudaError_t fp_batch_q4(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
+cudaError_t fp_batch_q8(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
+cudaError_t fp_batch_q16(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
 
 namespace {
 constexpr int kFpThreads = 256;
@@ -51,19 +51,22 @@ int fp_qp(int w) {
     return qp <= 1 ? 1 : qp <= 2 ? 2 : qp <= 4 ? 4 : qp <= 8 ? 8 : qp <= 16 ? 16 : 0;
 }
 
-// Shared-memory bytes of a CTA for width W and planes per chunk ZC (matches fpk::layout).
-size_t fp_smem_bytes(int ZC, int W, int qp, int rows) {
-    size_t o = 16 + (size_t)rows * ZC * W * sizeof(float);
+// Shared-memory bytes of a CTA for width W and planes per chunk ZC (matches fpk::layout):
+// FP32 volumes stage 4-byte voxels and build 8-byte pairs, 16-bit volumes 2-byte voxels
+// and 4-byte pairs.
+size_t fp_smem_bytes(int ZC, int W, int qp, int rows, int vtype) {
+    const bool h = vtype != kVolF32;
+    size_t o = 16 + (size_t)rows * ZC * W * (h ? 2 : 4);
     o = (o + 15) & ~(size_t)15;
-    o += (size_t)ZC * (W + 4) * sizeof(float2);
+    o += (size_t)ZC * (W + 4) * (h ? 4 : 8);
     o = (o + 15) & ~(size_t)15;
     o += (kFpThreads / 32) * sizeof(double) + (size_t)(kFpRays / qp > 0 ? kFpRays / qp : 1) * sizeof(long long);
     return o;
 }
 
-int fp_choose_zc(int W, int rows) {
+int fp_choose_zc(int W, int rows, int vtype) {
     for (int zc = 16; zc > 1; zc >>= 1)
-        if (fp_smem_bytes(zc, W, 1, rows) <= kFpSmemBudget) return zc;
+        if (fp_smem_bytes(zc, W, 1, rows, vtype) <= kFpSmemBudget) return zc;
     return 1;
 }
 
@@ -93,13 +96,13 @@ int fp_zparts(int ctas, int D, int zc, int sms) {
 }
 
 cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,
-                            cudaStream_t s) {
+                            int pk, cudaStream_t s) {
     switch (qp) {
-        case 1: return fp_batch_q1(descs, items, n_items, zc, smem, s);
-        case 2: return fp_batch_q2(descs, items, n_items, zc, smem, s);
-        case 4: return fp_batch_q4(descs, items, n_items, zc, smem, s);
-        case 8: return fp_batch_q8(descs, items, n_items, zc, smem, s);
-        case 16: return fp_batch_q16(descs, items, n_items, zc, smem, s);
+        case 1: return fp_batch_q1(descs, items, n_items, zc, smem, pk, s);
+        case 2: return fp_batch_q2(descs, items, n_items, zc, smem, pk, s);
+        case 4: return fp_batch_q4(descs, items, n_items, zc, smem, pk, s);
+        case 8: return fp_batch_q8(descs, items, n_items, zc, smem, pk, s);
+        case 16: return fp_batch_q16(descs, items, n_items, zc, smem, pk, s);
     }
     return cudaErrorInvalidValue;
 }

@@ -142,7 +142,7 @@ int auto_tilts_per_cta(const tomo_projector* p, int T, int rows) {
 int fp_split(tomo_projector* p, int T, int rows, int tpc) {
     const Geometry& g = p->g;
     const int groups = (T + tpc - 1) / tpc;
-    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W, g.fractional ? 2 : 1), p->sms);
+    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W, g.fractional ? 2 : 1, p->vtype), p->sms);
     if (P <= 1) return 1;
     const size_t need_part = (size_t)P * T * p->npix;
     const size_t need_tk = (size_t)groups * g.h;

@@ -256,11 +256,12 @@ cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T,
 cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s);
 int fp_max_tilts_per_cta(int w);
 int fp_qp(int w);
-int fp_choose_zc(int W, int rows = 1);
-size_t fp_smem_bytes(int ZC, int W, int qp, int rows = 1);
-// Batched forward projection: CTA b runs items[b] = {descriptor, first tilt, row, use_tma}.
+int fp_choose_zc(int W, int rows = 1, int vtype = kVolF32);
+size_t fp_smem_bytes(int ZC, int W, int qp, int rows = 1, int vtype = kVolF32);
+// Batched forward projection: CTA b runs items[b] = {descriptor, first tilt, row, use_tma};
+// pk = 1 when every descriptor of the launch has a 16-bit volume, 0 when all are FP32.
 cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,
-                            cudaStream_t s);
+                            int pk, cudaStream_t s);
 cudaError_t fp_init_attributes();
 cudaError_t misc_init_attributes();
 cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s);
