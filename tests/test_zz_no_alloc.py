@@ -110,7 +110,7 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(engine):
                                                     _abi.ptr(err, C.c_double), None)
     assert rc == -1 and b"2048" in engine.tomo_last_error()
     # a volume row too wide for the forward projector's shared memory is refused up front
-    geom = _abi.make_geom(12000, 8, 32, 1024, 8, 3)
+    geom = _abi.make_geom(30000, 8, 32, 1024, 8, 3)
     rc = engine.tomo_project_and_difference_noalloc(C.byref(geom), _abi.ptr(eul, C.c_double), _abi.ptr(tl, C.c_int32),
                                                     1, 1.0, dummy, dummy, dummy, dummy, dummy,
                                                     _abi.ptr(err, C.c_double), None)

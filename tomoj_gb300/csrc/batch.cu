@@ -35,7 +35,7 @@ struct tomo_batch {
     int4* d_bp_items = nullptr;
     size_t cap_fp = 0, cap_bp = 0, cap_fpi = 0, cap_bpi = 0, cap_red = 0;
     struct FpSeg {
-        int s, qp, zc, pk;
+        int s, qp, nt, zc, pk;
         size_t smem;
         int off, n;
     };
@@ -105,8 +105,8 @@ tomo_status build_plan(tomo_batch* b) {
     std::vector<BpLaunch> bp;
     std::vector<ErrReduce> red;
     // work items grouped by (s, qp, zc, pair kind) for FP and (s, sanitize, pos, storage type) for BP
-    std::map<std::tuple<int, int, int, int>, std::vector<int4>> fpi;
-    std::map<std::tuple<int, int, int, int>, size_t> fpsmem;
+    std::map<std::tuple<int, int, int, int, int>, std::vector<int4>> fpi;
+    std::map<std::tuple<int, int, int, int, int>, size_t> fpsmem;
     std::map<std::tuple<int, int, int, int>, std::vector<int4>> bpi;
     std::map<int, std::vector<ErrReduce>> reds;
     b->max_nsub = 0;
@@ -126,8 +126,8 @@ tomo_status build_plan(tomo_batch* b) {
         b->has_fista = b->has_fista || p->fista;
         // rows the forward projector never writes must read as zero residual
         BCK(cudaMemsetAsync(p->d_errpart, 0, sizeof(double) * (size_t)N * g.h, b->stream));
-        const int qp = fp_qp(g.w);
-        const int zc = fp_choose_zc(g.W, 1, p->vtype);
+        const int qp = fp_qp(g.w), nt = fp_threads(g.w);
+        const int zc = fp_choose_zc(g.W, 1, p->vtype, nt);
         const int pk = p->vtype != kVolF32 ? 1 : 0;
         const int use_tma = fp_use_tma(g.W, p->vtype, p->vol());
         const int offset = (g.h > g.H && g.scale == 1) ? (g.h - g.H) / 2 : 0;
@@ -161,7 +161,7 @@ tomo_status build_plan(tomo_batch* b) {
             a.status = p->d_status;
             const int di = (int)fp.size();
             fp.push_back(a);
-            const auto key = std::make_tuple(s, qp, zc, pk);
+            const auto key = std::make_tuple(s, qp, nt, zc, pk);
             fpsmem[key] = std::max(fpsmem[key], fp_smem_bytes(zc, g.W, qp, 1, p->vtype));
             auto& items = fpi[key];
             for (int g0 = 0; g0 < T; g0 += a.tilts_per_cta)
@@ -191,10 +191,16 @@ tomo_status build_plan(tomo_batch* b) {
             const int bi = (int)bp.size();
             bp.push_back(c);
             auto& bitems = bpi[std::make_tuple(s, c.sanitize, c.positivity, c.vtype)];
-            for (int r = 0; r < g.H; r++) {
-                const int jp = r + g.bp_row_off;
-                if (jp < 0 || jp >= g.h) continue;
-                for (int zt = 0; zt < (g.D + tz - 1) / tz; zt++)
+            const bool pairs = bp_row_pairs(c.vtype, c.sanitize != 0, c.positivity != 0);
+            const int rstep = pairs ? 2 : 1, tzr = pairs ? bp_pair_tile_z(c.vtype) : tz;
+            for (int r = 0; r < g.H; r += rstep) {
+                bool reached = false;  // a row of the item sees a projection row
+                for (int q = 0; q < rstep && r + q < g.H; q++) {
+                    const int jp = r + q + g.bp_row_off;
+                    reached = reached || (jp >= 0 && jp < g.h);
+                }
+                if (!reached) continue;
+                for (int zt = 0; zt < (g.D + tzr - 1) / tzr; zt++)
                     for (int xt = 0; xt < (g.W + tx - 1) / tx; xt++) bitems.push_back(make_int4(bi, xt, zt, r));
             }
         }
@@ -206,7 +212,8 @@ tomo_status build_plan(tomo_batch* b) {
     b->red_segs.clear();
     for (auto& kv : fpi) {
         tomo_batch::FpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
-                             std::get<3>(kv.first), fpsmem[kv.first], (int)fp_all.size(), (int)kv.second.size()};
+                             std::get<3>(kv.first), std::get<4>(kv.first), fpsmem[kv.first], (int)fp_all.size(),
+                             (int)kv.second.size()};
         fp_all.insert(fp_all.end(), kv.second.begin(), kv.second.end());
         b->fp_segs.push_back(sg);
     }
@@ -247,7 +254,7 @@ tomo_status launch_step(tomo_batch* b) {
     for (int s = 0; s < b->max_nsub; s++) {
         for (auto& sg : b->fp_segs)
             if (sg.s == s)
-                BCK(launch_fp_batch(sg.qp, b->d_fp, b->d_fp_items + sg.off, sg.n, sg.zc, sg.smem, sg.pk, b->stream));
+                BCK(launch_fp_batch(sg.qp, sg.nt, b->d_fp, b->d_fp_items + sg.off, sg.n, sg.zc, sg.smem, sg.pk, b->stream));
         for (auto& sg : b->red_segs)
             if (sg.s == s) BCK(launch_reduce_err_batch(b->d_red + sg.off, sg.n, sg.maxT, b->stream));
         for (tomo_projector* p : b->members) BCKS(handle_bp_pre(p, b->stream));

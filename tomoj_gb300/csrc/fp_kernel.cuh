@@ -32,9 +32,7 @@
 namespace tomo {
 namespace fpk {
 
-constexpr int kThreads = 256;
 constexpr uint32_t kWaitTries = 1u << 24;
-constexpr size_t kMaxSmem = kFpSmemBudget;
 
 struct Smem {
     int PW;
@@ -54,7 +52,7 @@ __host__ __device__ inline Smem layout(int ZC, int W, int tgmax, int rows = 1, i
     o += (size_t)ZC * L.PW * (PK ? sizeof(uint32_t) : sizeof(float2));
     o = (o + 15) & ~(size_t)15;
     L.red_off = o;
-    o += (kThreads / 32) * sizeof(double);
+    o += (kFpMaxThreads / 32) * sizeof(double);
     L.step_off = o;
     o += (size_t)tgmax * sizeof(long long);
     L.total = o;
@@ -66,7 +64,7 @@ __host__ __device__ inline Smem layout(int ZC, int W, int tgmax, int rows = 1, i
 // fma(1 + f, d_k, v_k - d_k).  d = 0 where the reference returns the raw floor voxel
 // (last column, last row, last plane) and outside [0, W-1].
 //
-// A chunk's rows are converted together: the block is laid out as kThreads / q rows x
+// A chunk's rows are converted together: the block is laid out as NT / q rows x
 // q groups (q groups per row), so a 512-wide row of 128 float4 groups keeps all 256
 // threads busy instead of half of them.
 
@@ -168,23 +166,24 @@ __device__ __forceinline__ void pair1_blend(const float* __restrict__ src0, cons
 }
 
 // Calls fn(zz, m) for every row zz < zc and group m < q, spreading rows over the block.
-template <class Fn>
+template <int NT, class Fn>
 __device__ __forceinline__ void for_chunk_groups(int zc, int q, Fn fn) {
     const int tid = threadIdx.x;
-    if (q <= kThreads) {
-        const int R = kThreads / q;
+    if (q <= NT) {
+        const int R = NT / q;
         const int r0 = tid / q, m = tid - r0 * q;
         if (r0 < R)
             for (int zz = r0; zz < zc; zz += R) fn(zz, m);
     } else {
         for (int zz = 0; zz < zc; zz++)
-            for (int m = tid; m < q; m += kThreads) fn(zz, m);
+            for (int m = tid; m < q; m += NT) fn(zz, m);
     }
 }
 
 // All pairs of a staged chunk of zc plane rows.  raw: rows [zc][W] as stored (FP32 or
 // 16-bit), raw1: row r + 1 of every plane (blended form); zflat: the chunk row of the
 // volume's last plane, or -1.
+template <int NT>
 __device__ __forceinline__ void build_pairs_chunk(const void* raw, const float* raw1, float2* __restrict__ pairs, int W,
                                                   int PW, int zc, int vt, bool blend, float yf, bool last_row,
                                                   int zflat) {
@@ -192,41 +191,41 @@ __device__ __forceinline__ void build_pairs_chunk(const void* raw, const float* 
     const uint16_t* r16 = static_cast<const uint16_t*>(raw);
     auto flat = [&](int zz) { return last_row || zz == zflat; };
     if (blend) {
-        for_chunk_groups(zc, W, [&](int zz, int k) {
+        for_chunk_groups<NT>(zc, W, [&](int zz, int k) {
             pair1_blend(r32 + (size_t)zz * W, raw1 + (size_t)zz * W, yf, pairs + (size_t)zz * PW, W, k, flat(zz));
         });
     } else if (vt == kVolF32) {
         if ((W & 3) == 0)
-            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+            for_chunk_groups<NT>(zc, W >> 2, [&](int zz, int m) {
                 pairs4_f32(r32 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
             });
         else
-            for_chunk_groups(zc, W, [&](int zz, int k) {
+            for_chunk_groups<NT>(zc, W, [&](int zz, int k) {
                 pair1_f32(r32 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
             });
     } else if (vt == kVolBF16) {
         if ((W & 3) == 0)
-            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+            for_chunk_groups<NT>(zc, W >> 2, [&](int zz, int m) {
                 pairs4_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
             });
         else
-            for_chunk_groups(zc, W, [&](int zz, int k) {
+            for_chunk_groups<NT>(zc, W, [&](int zz, int k) {
                 pair1_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
             });
     } else {
         if ((W & 3) == 0)
-            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+            for_chunk_groups<NT>(zc, W >> 2, [&](int zz, int m) {
                 pairs4_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
             });
         else
-            for_chunk_groups(zc, W, [&](int zz, int k) {
+            for_chunk_groups<NT>(zc, W, [&](int zz, int k) {
                 pair1_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
             });
     }
     // slots -2, -1, W, W+1 of every row: the edge values with slope 0.  In the blended
     // form x in [-ACCURACY, 0) samples column 0 with weight 0 (the blended value) and
     // slots past the row are never sampled (x < W).
-    for (int e = threadIdx.x; e < zc * 4; e += kThreads) {
+    for (int e = threadIdx.x; e < zc * 4; e += NT) {
         const int zz = e >> 2, t = e & 3;
         const int col = (t < 2) ? 0 : W - 1;
         const size_t o = (size_t)zz * W + col;
@@ -244,29 +243,30 @@ __device__ __forceinline__ void build_pairs_chunk(const void* raw, const float* 
 }
 
 // All half2 pairs of a staged chunk of zc 16-bit plane rows (PK 1).
+template <int NT>
 __device__ __forceinline__ void build_hpairs_chunk(const uint16_t* r16, uint32_t* __restrict__ pairs, int W, int PW,
                                                    int zc, int vt, bool last_row, int zflat) {
     auto flat = [&](int zz) { return last_row || zz == zflat; };
     if (vt == kVolBF16) {
         if ((W & 3) == 0)
-            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+            for_chunk_groups<NT>(zc, W >> 2, [&](int zz, int m) {
                 hpairs4_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
             });
         else
-            for_chunk_groups(zc, W, [&](int zz, int k) {
+            for_chunk_groups<NT>(zc, W, [&](int zz, int k) {
                 hpair1_16<kVolBF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
             });
     } else {
         if ((W & 3) == 0)
-            for_chunk_groups(zc, W >> 2, [&](int zz, int m) {
+            for_chunk_groups<NT>(zc, W >> 2, [&](int zz, int m) {
                 hpairs4_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, m, flat(zz));
             });
         else
-            for_chunk_groups(zc, W, [&](int zz, int k) {
+            for_chunk_groups<NT>(zc, W, [&](int zz, int k) {
                 hpair1_16<kVolF16>(r16 + (size_t)zz * W, pairs + (size_t)zz * PW, W, k, flat(zz));
             });
     }
-    for (int e = threadIdx.x; e < zc * 4; e += kThreads) {
+    for (int e = threadIdx.x; e < zc * 4; e += NT) {
         const int zz = e >> 2, t = e & 3;
         const int col = (t < 2) ? 0 : W - 1;
         const float v = vol_load16_rt(vt, r16[(size_t)zz * W + col]);
@@ -287,10 +287,10 @@ __device__ __forceinline__ float sample(const __half2* __restrict__ P, long long
 
 // Detector column of ray slot (t, q) of thread tid: warps own blocks of 32 consecutive
 // columns (contiguous shared-memory reads).
-template <int QP>
+template <int NT, int QP>
 __device__ __forceinline__ int ray_column(int t, int q, int tid) {
     (void)t;
-    return tid + q * kThreads;
+    return tid + q * NT;
 }
 
 // Partial chunk of one ray (it enters or leaves the volume inside the chunk):
@@ -342,7 +342,7 @@ __device__ __forceinline__ PartialOut full_chunk_inl(const PT* __restrict__ P, l
 // BLEND: the fractional-row form (row maps, two staged rows per plane).  A separate
 // instantiation, so that the whole-row kernels compile without any of it.
 // PK: pair kind (0: FP32 volume, float2 pairs; 1: 16-bit volume, half2 pairs).
-template <int QP, int ZC, bool BLEND, int PK>
+template <int NT, int QP, int ZC, bool BLEND, int PK>
 __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma,
                                         const int zp) {
     static_assert(!(BLEND && PK), "the fractional-row form is FP32 only");
@@ -380,7 +380,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
 #pragma unroll
     for (int k = 0; k < NR; k++) {
         const int t = k / QP, q = k % QP;
-        const int i = ray_column<QP>(t, q, tid);
+        const int i = ray_column<NT, QP>(t, q, tid);
         acc[k] = 0.0f;
         X[k] = 0;
         zab[k] = 0;
@@ -423,17 +423,17 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             } else if (vt == kVolF32) {
                 for (int zz = 0; zz < zn; zz++) {
                     const float* src = reinterpret_cast<const float*>(volb + ((size_t)(z0 + zz) * H + r) * rowb);
-                    for (int k = tid; k < W; k += kThreads) raw[(size_t)zz * W + k] = src[k];
+                    for (int k = tid; k < W; k += NT) raw[(size_t)zz * W + k] = src[k];
                     if (BLEND && blend) {
                         const float* s1 = src + (size_t)W;
-                        for (int k = tid; k < W; k += kThreads) raw1[(size_t)zz * W + k] = s1[k];
+                        for (int k = tid; k < W; k += NT) raw1[(size_t)zz * W + k] = s1[k];
                     }
                 }
             } else {
                 uint16_t* raw16 = reinterpret_cast<uint16_t*>(raw);
                 for (int zz = 0; zz < zn; zz++) {
                     const uint16_t* src = reinterpret_cast<const uint16_t*>(volb + ((size_t)(z0 + zz) * H + r) * rowb);
-                    for (int k = tid; k < W; k += kThreads) raw16[(size_t)zz * W + k] = src[k];
+                    for (int k = tid; k < W; k += NT) raw16[(size_t)zz * W + k] = src[k];
                 }
             }
         };
@@ -460,10 +460,10 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                 __syncthreads();
             }
             if (PK == 1)
-                build_hpairs_chunk(reinterpret_cast<const uint16_t*>(raw), reinterpret_cast<uint32_t*>(pairs), W, PW,
+                build_hpairs_chunk<NT>(reinterpret_cast<const uint16_t*>(raw), reinterpret_cast<uint32_t*>(pairs), W, PW,
                                    zc, vt, last_row, D - 1 - z0 < zc ? D - 1 - z0 : -1);
             else
-                build_pairs_chunk(raw, raw1, reinterpret_cast<float2*>(pairs), W, PW, zc, vt, BLEND && blend, yf,
+                build_pairs_chunk<NT>(raw, raw1, reinterpret_cast<float2*>(pairs), W, PW, zc, vt, BLEND && blend, yf,
                                   last_row, D - 1 - z0 < zc ? D - 1 - z0 : -1);
             __syncthreads();
             if (c + 1 < c_end && use_tma) stage(c + 1);
@@ -509,7 +509,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
 #pragma unroll
         for (int k = 0; k < NR; k++) {
             const int t = k / QP, q = k % QP;
-            const int i = ray_column<QP>(t, q, tid);
+            const int i = ray_column<NT, QP>(t, q, tid);
             if (t < TG && i < w) a.part[(((size_t)zp * a.T + g0 + t) * h + j) * w + i] = acc[k];
         }
         __threadfence();
@@ -526,7 +526,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
 #pragma unroll
         for (int k = 0; k < NR; k++) {
             const int t = k / QP, q = k % QP;
-            const int i = ray_column<QP>(t, q, tid);
+            const int i = ray_column<NT, QP>(t, q, tid);
             float sum = 0.0f;
             if (t < TG && i < w)
                 for (int pp = 0; pp < P; pp++) sum += __ldcg(a.part + (((size_t)pp * a.T + g0 + t) * h + j) * w + i);
@@ -546,7 +546,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
         double e2 = 0.0;
 #pragma unroll
         for (int q = 0; q < QP; q++) {
-            const int i = ray_column<QP>(t, q, tid);
+            const int i = ray_column<NT, QP>(t, q, tid);
             if (i >= w) continue;
             const int cnt = (int)((uint32_t)zab[t * QP + q] >> 16);
             float th, nrm;
@@ -579,7 +579,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             __syncthreads();
             if (tid == 0) {
                 double sum = 0.0;
-                for (int k = 0; k < kThreads / 32; k++) sum += red[k];
+                for (int k = 0; k < NT / 32; k++) sum += red[k];
                 a.errpart[(size_t)(g0 + t) * h + j] = sum;
             }
             __syncthreads();
@@ -587,90 +587,90 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
     }
 }
 
-template <int QP, int ZC, bool BLEND, int PK>
-__global__ void __launch_bounds__(kThreads, kFpCtasPerSm) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
-    fp_body<QP, ZC, BLEND, PK>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
+template <int NT, int QP, int ZC, bool BLEND, int PK>
+__global__ void __launch_bounds__(NT, fp_ctas_per_sm(NT)) fp_kernel(const __grid_constant__ FpLaunch a, int use_tma) {
+    fp_body<NT, QP, ZC, BLEND, PK>(a, blockIdx.x * a.tilts_per_cta, a.j0 + blockIdx.y, use_tma, blockIdx.z);
 }
 
 // Batched form: CTA b works on item {problem, first tilt, row, use_tma} of many problems
 // (all of pair kind PK: FP32 and 16-bit volumes go to separate launches).
-template <int QP, int ZC, int PK>
-__global__ void __launch_bounds__(kThreads, kFpCtasPerSm)
+template <int NT, int QP, int ZC, int PK>
+__global__ void __launch_bounds__(NT, fp_ctas_per_sm(NT))
     fp_kernel_batch(const FpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
-    fp_body<QP, ZC, false, PK>(descs[it.x], it.y, it.z, it.w, 0);
+    fp_body<NT, QP, ZC, false, PK>(descs[it.x], it.y, it.z, it.w, 0);
 }
 
-template <int QP, int ZC>
+template <int NT, int QP, int ZC>
 cudaError_t set_attr_one() {
-    const int m = (int)kMaxSmem;
-    cudaError_t e = cudaFuncSetAttribute(fp_kernel<QP, ZC, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    const int m = (int)fp_smem_budget(NT);
+    cudaError_t e = cudaFuncSetAttribute(fp_kernel<NT, QP, ZC, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(fp_kernel<QP, ZC, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(fp_kernel<NT, QP, ZC, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(fp_kernel<QP, ZC, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(fp_kernel<NT, QP, ZC, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(fp_kernel_batch<QP, ZC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    e = cudaFuncSetAttribute(fp_kernel_batch<NT, QP, ZC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(fp_kernel_batch<QP, ZC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    return cudaFuncSetAttribute(fp_kernel_batch<NT, QP, ZC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
-template <int QP>
+template <int NT, int QP>
 cudaError_t set_attr_qp() {
     cudaError_t e;
-    if ((e = set_attr_one<QP, 16>()) != cudaSuccess) return e;
-    if ((e = set_attr_one<QP, 8>()) != cudaSuccess) return e;
-    if ((e = set_attr_one<QP, 4>()) != cudaSuccess) return e;
-    if ((e = set_attr_one<QP, 2>()) != cudaSuccess) return e;
-    return set_attr_one<QP, 1>();
+    if ((e = set_attr_one<NT, QP, 16>()) != cudaSuccess) return e;
+    if ((e = set_attr_one<NT, QP, 8>()) != cudaSuccess) return e;
+    if ((e = set_attr_one<NT, QP, 4>()) != cudaSuccess) return e;
+    if ((e = set_attr_one<NT, QP, 2>()) != cudaSuccess) return e;
+    return set_attr_one<NT, QP, 1>();
 }
 
-template <int QP, int ZC>
+template <int NT, int QP, int ZC>
 void launch_zc(const FpLaunch& a, dim3 grid, size_t smem, int use_tma, cudaStream_t s) {
-    if (a.two_rows) fp_kernel<QP, ZC, true, 0><<<grid, kThreads, smem, s>>>(a, use_tma);
-    else if (a.vtype != kVolF32) fp_kernel<QP, ZC, false, 1><<<grid, kThreads, smem, s>>>(a, use_tma);
-    else fp_kernel<QP, ZC, false, 0><<<grid, kThreads, smem, s>>>(a, use_tma);
+    if (a.two_rows) fp_kernel<NT, QP, ZC, true, 0><<<grid, NT, smem, s>>>(a, use_tma);
+    else if (a.vtype != kVolF32) fp_kernel<NT, QP, ZC, false, 1><<<grid, NT, smem, s>>>(a, use_tma);
+    else fp_kernel<NT, QP, ZC, false, 0><<<grid, NT, smem, s>>>(a, use_tma);
 }
 
-template <int QP>
+template <int NT, int QP>
 cudaError_t launch_qp(const FpLaunch& a, cudaStream_t s) {
     const int rows = a.two_rows ? 2 : 1;
     const int PK = a.vtype != kVolF32 ? 1 : 0;
     if (PK && a.two_rows) return cudaErrorInvalidValue;
-    const int ZC = fp_choose_zc(a.W, rows, a.vtype);
+    const int ZC = fp_choose_zc(a.W, rows, a.vtype, NT);
     const Smem L = layout(ZC, a.W, kFpRays / QP > 0 ? kFpRays / QP : 1, rows, PK);
-    if (L.total > kMaxSmem) return cudaErrorInvalidValue;
+    if (L.total > fp_smem_budget(NT)) return cudaErrorInvalidValue;
     const int use_tma = fp_use_tma(a.W, a.vtype, a.vol);
     dim3 grid((a.T + a.tilts_per_cta - 1) / a.tilts_per_cta, a.j1 - a.j0, a.zparts > 1 ? a.zparts : 1);
     switch (ZC) {
-        case 16: launch_zc<QP, 16>(a, grid, L.total, use_tma, s); break;
-        case 8: launch_zc<QP, 8>(a, grid, L.total, use_tma, s); break;
-        case 4: launch_zc<QP, 4>(a, grid, L.total, use_tma, s); break;
-        case 2: launch_zc<QP, 2>(a, grid, L.total, use_tma, s); break;
-        default: launch_zc<QP, 1>(a, grid, L.total, use_tma, s); break;
+        case 16: launch_zc<NT, QP, 16>(a, grid, L.total, use_tma, s); break;
+        case 8: launch_zc<NT, QP, 8>(a, grid, L.total, use_tma, s); break;
+        case 4: launch_zc<NT, QP, 4>(a, grid, L.total, use_tma, s); break;
+        case 2: launch_zc<NT, QP, 2>(a, grid, L.total, use_tma, s); break;
+        default: launch_zc<NT, QP, 1>(a, grid, L.total, use_tma, s); break;
     }
     count_launch();
     return cudaGetLastError();
 }
 
-template <int QP, int PK>
+template <int NT, int QP, int PK>
 void launch_batch_pk(const FpLaunch* descs, const int4* items, int n_items, int ZC, size_t smem, cudaStream_t s) {
     switch (ZC) {
-        case 16: fp_kernel_batch<QP, 16, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        case 8: fp_kernel_batch<QP, 8, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        case 4: fp_kernel_batch<QP, 4, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        case 2: fp_kernel_batch<QP, 2, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
-        default: fp_kernel_batch<QP, 1, PK><<<n_items, kThreads, smem, s>>>(descs, items); break;
+        case 16: fp_kernel_batch<NT, QP, 16, PK><<<n_items, NT, smem, s>>>(descs, items); break;
+        case 8: fp_kernel_batch<NT, QP, 8, PK><<<n_items, NT, smem, s>>>(descs, items); break;
+        case 4: fp_kernel_batch<NT, QP, 4, PK><<<n_items, NT, smem, s>>>(descs, items); break;
+        case 2: fp_kernel_batch<NT, QP, 2, PK><<<n_items, NT, smem, s>>>(descs, items); break;
+        default: fp_kernel_batch<NT, QP, 1, PK><<<n_items, NT, smem, s>>>(descs, items); break;
     }
 }
 
-template <int QP>
+template <int NT, int QP>
 cudaError_t launch_batch_qp(const FpLaunch* descs, const int4* items, int n_items, int ZC, size_t smem, int pk,
                             cudaStream_t s) {
     if (n_items <= 0) return cudaSuccess;
-    if (smem > kMaxSmem) return cudaErrorInvalidValue;
-    if (pk) launch_batch_pk<QP, 1>(descs, items, n_items, ZC, smem, s);
-    else launch_batch_pk<QP, 0>(descs, items, n_items, ZC, smem, s);
+    if (smem > fp_smem_budget(NT)) return cudaErrorInvalidValue;
+    if (pk) launch_batch_pk<NT, QP, 1>(descs, items, n_items, ZC, smem, s);
+    else launch_batch_pk<NT, QP, 0>(descs, items, n_items, ZC, smem, s);
     count_launch();
     return cudaGetLastError();
 }
@@ -678,13 +678,15 @@ cudaError_t launch_batch_qp(const FpLaunch* descs, const int4* items, int n_item
 }  // namespace fpk
 }  // namespace tomo
 
-// One translation unit per QP defines these entry points.
-#define TOMO_FP_INSTANTIATE(QP)                                                                          \
-    namespace tomo {                                                                                     \
-    cudaError_t fp_launch_q##QP(const FpLaunch& a, cudaStream_t s) { return fpk::launch_qp<QP>(a, s); } \
-    cudaError_t fp_attr_q##QP() { return fpk::set_attr_qp<QP>(); }                                     \
-    cudaError_t fp_batch_q##QP(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk,    \
-                               cudaStream_t s) {                                                         \
-        return fpk::launch_batch_qp<QP>(d, it, n, zc, smem, pk, s);                                      \
-    }                                                                                                    \
+// One translation unit per (threads, QP) pair defines these entry points.
+#define TOMO_FP_INSTANTIATE(NT, QP)                                                                        \
+    namespace tomo {                                                                                       \
+    cudaError_t fp_launch_t##NT##_q##QP(const FpLaunch& a, cudaStream_t s) {                               \
+        return fpk::launch_qp<NT, QP>(a, s);                                                               \
+    }                                                                                                      \
+    cudaError_t fp_attr_t##NT##_q##QP() { return fpk::set_attr_qp<NT, QP>(); }                            \
+    cudaError_t fp_batch_t##NT##_q##QP(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, \
+                                       cudaStream_t s) {                                                   \
+        return fpk::launch_batch_qp<NT, QP>(d, it, n, zc, smem, pk, s);                                    \
+    }                                                                                                      \
     }

@@ -1,4 +1,5 @@
 // Forward-projection kernels for QP = 2 detector columns per thread (see fp_kernel.cuh).
 #include "fp_kernel.cuh"
 
-TOMO_FP_INSTANTIATE(2)
+TOMO_FP_INSTANTIATE(256, 2)
+TOMO_FP_INSTANTIATE(512, 2)

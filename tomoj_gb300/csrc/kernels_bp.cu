@@ -367,6 +367,348 @@ __global__ void __launch_bounds__(kBpCtaThreads, BpOcc<VT>::value)
     bp_body<SANITIZE, POS, VT, 96>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
 }
 
+// ---------------------------------------------------------------------------------------
+// Two volume rows per thread.  With a vertical tilt axis and whole-row centre offsets the
+// rows r and r + 1 see the same image-column position at every (x, z) of a tilt, so the
+// position, interpolation weight and z-interval test of a (voxel column, tilt) serve both
+// rows.  The two rows' image segments are interleaved per pair slot as
+// (v0 - d0, v1 - d1, d0, d1): one 128-bit shared load feeds a packed FP32x2 FMA (the two
+// samples) and a packed add into the two voxels.  Each lane of the packed operations
+// rounds as the scalar fmaf / add of the one-row kernel, so the result is bitwise the same.
+//
+// Tile: 64 x-columns x 4*KZ z-planes x 2 rows; thread (tx, tzg) owns KZ voxels along z of
+// column x0 + tx in both rows.  16 tilts are staged per chunk.  16-bit volumes take the
+// per-chunk Kahan form only (no per-add NaN / positivity rules: those go to the one-row
+// kernel).
+template <int KZ>
+struct Bp2 {
+    static constexpr int kTC = 16;
+    static constexpr int kSeg = 96;
+    static constexpr int kRawSeg = kSeg + 8;
+    static constexpr int kTZ2 = 4 * KZ;
+    static constexpr size_t seg_off = 0;                                                 // float4 [kTC][kSeg]
+    static constexpr size_t raw_off = seg_off + sizeof(float4) * kTC * kSeg;            // float [kTC][2][kRawSeg]
+    static constexpr size_t zint_off = raw_off + sizeof(float) * kTC * 2 * kRawSeg;     // int [kTC][kTX]
+    static constexpr size_t az_off = zint_off + sizeof(int) * kTC * kTX;                 // long long [kTC][4]
+    static constexpr size_t cs_off = az_off + sizeof(long long) * kTC * 4;               // long long C[kTC], S[kTC]
+    static constexpr size_t st_off = cs_off + sizeof(long long) * 2 * kTC;               // int seg / raw start
+    static constexpr size_t comp_off = (st_off + sizeof(int) * 2 * kTC + 15) & ~(size_t)15;  // float [2][KZ][256]
+    static constexpr size_t bytes(bool kahan) {
+        return comp_off + (kahan ? sizeof(float) * 2 * KZ * kBpThreads : 0);
+    }
+};
+
+// Voxels per thread along z: 16 for FP32 volumes (80 registers, three CTAs per SM); 8 for
+// 16-bit volumes, whose per-chunk partial sums double the voxel registers.
+template <int VT>
+struct Bp2Occ {
+    static constexpr int value = 3;
+    static constexpr int kz = VT == kVolF32 ? 16 : 8;
+};
+
+template <bool SANITIZE, bool POS, int VT, int KZ>
+__device__ __forceinline__ void bp2_body(const BpLaunch& a, const int x0, const int z0, const int r0) {
+    using L = Bp2<KZ>;
+    constexpr int kTC = L::kTC, kSeg = L::kSeg, kRawSeg = L::kRawSeg;
+    constexpr bool CHUNK_KAHAN = VT != kVolF32;
+    static_assert(VT == kVolF32 || (!SANITIZE && !POS), "16-bit rows with per-add rules use the one-row kernel");
+    extern __shared__ __align__(16) unsigned char bsm[];
+    float4* seg = reinterpret_cast<float4*>(bsm + L::seg_off);
+    float(*raw)[2][kRawSeg] = reinterpret_cast<float(*)[2][kRawSeg]>(bsm + L::raw_off);
+    int(*zint)[kTX] = reinterpret_cast<int(*)[kTX]>(bsm + L::zint_off);
+    long long(*AZ)[4] = reinterpret_cast<long long(*)[4]>(bsm + L::az_off);
+    long long* sC = reinterpret_cast<long long*>(bsm + L::cs_off);
+    long long* sS = sC + kTC;
+    int* seg_start = reinterpret_cast<int*>(bsm + L::st_off);
+    int* raw_start = seg_start + kTC;
+    float* comp_sh = reinterpret_cast<float*>(bsm + L::comp_off);
+
+    const int tid = threadIdx.x;
+    const int tx = tid % kTX;
+    const int tzg = tid / kTX;
+    const int W = a.W, H = a.H, D = a.D, w = a.w, h = a.h;
+    // rows r0 and r0 + 1 of [y0, y1); a row whose projection row is outside [0, h) is left as it is
+    int jp[2];
+    bool rin[2];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int r = r0 + q;
+        jp[q] = r + a.row_off;
+        rin[q] = r < a.y1 && jp[q] >= 0 && jp[q] < h;
+    }
+    if (!rin[0] && !rin[1]) return;
+    const int zs = z0 + tzg * KZ;
+    const int x = x0 + tx;
+    const int nk = (x < W) ? min(KZ, D - zs) : 0;
+    const unsigned plane = (unsigned)H * (unsigned)W;
+    float vsc[2] = {1.0f, 1.0f};
+    if (VT != kVolF32) {
+        vsc[0] = rin[0] ? a.vscale[r0] : 1.0f;
+        vsc[1] = rin[1] ? a.vscale[r0 + 1] : 1.0f;
+    }
+    float2 vx[KZ], pt[KZ];
+    {
+        const size_t v0 = ((size_t)zs * H + r0) * W + x;  // voxel (x, r0, zs); row r0 + 1 is W further
+        if (VT == kVolF32) {
+            const float* vb = static_cast<const float*>(a.vol) + v0;
+#pragma unroll
+            for (int k = 0; k < KZ; k++) {
+                vx[k].x = (k < nk && rin[0]) ? vb[k * plane] : 0.0f;
+                vx[k].y = (k < nk && rin[1]) ? vb[k * plane + W] : 0.0f;
+            }
+        } else {
+            const uint16_t* vb = static_cast<const uint16_t*>(a.vol) + v0;
+#pragma unroll
+            for (int k = 0; k < KZ; k++) {
+                vx[k].x = (k < nk && rin[0]) ? vol_load16<VT>(vb[k * plane]) * vsc[0] : 0.0f;
+                vx[k].y = (k < nk && rin[1]) ? vol_load16<VT>(vb[k * plane + W]) * vsc[1] : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < KZ; k++) {
+            pt[k] = make_float2(0.0f, 0.0f);
+            if (CHUNK_KAHAN) {
+                comp_sh[(0 * KZ + k) * kBpThreads + tid] = 0.0f;
+                comp_sh[(1 * KZ + k) * kBpThreads + tid] = 0.0f;
+            }
+        }
+    }
+
+    const int xa = x0, xb = min(x0 + kTX - 1, W - 1);
+    const int za = z0, zb = min(z0 + L::kTZ2 - 1, D - 1);
+    const bool vec4 = ((w & 3) == 0) && ((reinterpret_cast<uintptr_t>(a.img) & 15) == 0);
+
+    for (int c0 = 0; c0 < a.T; c0 += kTC) {
+        const int tc = min(kTC, a.T - c0);
+        if (tid < tc) {
+            const int tilt = a.tilts[c0 + tid];
+            const BpTilt b = a.btilt[tilt];
+            sC[tid] = b.C;
+            sS[tid] = b.S;
+            const long long p00 = b.K + (long long)xa * b.C + (long long)za * b.S;
+            const long long p10 = b.K + (long long)xb * b.C + (long long)za * b.S;
+            const long long p01 = b.K + (long long)xa * b.C + (long long)zb * b.S;
+            const long long p11 = b.K + (long long)xb * b.C + (long long)zb * b.S;
+            const long long mn = min(min(p00, p10), min(p01, p11));
+            const int s = (int)(mn >> 32);
+            seg_start[tid] = s;
+            raw_start[tid] = s & ~3;
+            const long long base = (long long)(tid * kSeg - s) << 32;
+#pragma unroll
+            for (int g = 0; g < 4; g++) AZ[tid][g] = p00 + (long long)(g * KZ) * b.S + base;
+        }
+        for (int t = tzg; t < tc; t += kBpThreads / kTX)
+            zint[t][tx] = (x < W) ? a.zint[(size_t)a.tilts[c0 + t] * W + x] : 0;
+        __syncthreads();
+        // stage both rows' image segments: one warp per (tilt, row), 128-bit loads
+        for (int tq = tid >> 5; tq < 2 * tc; tq += kBpThreads / 32) {
+            const int t = tq >> 1, q = tq & 1;
+            if (!(q ? rin[1] : rin[0])) continue;
+            const float* row = a.img + ((size_t)(c0 + t) * h + (q ? jp[1] : jp[0])) * w;
+            for (int v = tid & 31; v < kRawSeg / 4; v += 32) {
+                const int k0 = raw_start[t] + 4 * v;
+                float4 f;
+                if (vec4 && k0 >= 0 && k0 + 3 < w) {
+                    f = *reinterpret_cast<const float4*>(row + k0);
+                } else {
+                    f.x = row[min(max(k0 + 0, 0), w - 1)];
+                    f.y = row[min(max(k0 + 1, 0), w - 1)];
+                    f.z = row[min(max(k0 + 2, 0), w - 1)];
+                    f.w = row[min(max(k0 + 3, 0), w - 1)];
+                }
+                *reinterpret_cast<float4*>(&raw[t][q][4 * v]) = f;
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < tc * kSeg; e += kBpThreads) {
+            const int t = e / kSeg, m = e - t * kSeg;
+            const int k = seg_start[t] + m;
+            const int o = k - raw_start[t];
+            float vd[2], dd[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                float v0 = 0.0f, d = 0.0f;
+                if (rin[q]) {
+                    const float* row = a.img + ((size_t)(c0 + t) * h + jp[q]) * w;
+                    int k0, k1;
+                    if (k >= 0 && k < w - 1) {
+                        v0 = raw[t][q][o];
+                        d = raw[t][q][o + 1] - v0;
+                        k0 = k;
+                        k1 = k + 1;
+                    } else {
+                        k0 = k1 = (k < 0) ? 0 : w - 1;
+                        v0 = row[k0];
+                    }
+                    if (SANITIZE) {
+                        const float* up = (jp[q] < h - 1) ? row + w : row;
+                        if (!isfinite(up[k0]) || !isfinite(up[k1])) v0 = __int_as_float(0x7fc00000);
+                    }
+                }
+                vd[q] = v0 - d;
+                dd[q] = d;
+            }
+            seg[t * kSeg + m] = make_float4(vd[0], vd[1], dd[0], dd[1]);
+        }
+        __syncthreads();
+        for (int t = 0; t < tc; t++) {
+            const long long S = sS[t];
+            long long X = AZ[t][tzg] + (long long)(unsigned)tx * sC[t];
+            const int zi = zint[t][tx];
+            const int kl = (zi & 0xFFFF) - zs;
+            const int cnt = (int)((uint32_t)zi >> 16);
+            const bool full = nk > 0 && kl <= 0 && kl + cnt >= KZ;
+            auto add = [&](int k, float2 sv) {
+                if (CHUNK_KAHAN) {
+                    pt[k] = __fadd2_rn(pt[k], sv);
+                } else if (!SANITIZE && !POS) {
+                    vx[k] = __fadd2_rn(vx[k], sv);
+                } else {
+                    float cdummy = 0.0f;
+                    bp_acc<SANITIZE, POS, kVolF32>(vx[k].x, cdummy, sv.x);
+                    bp_acc<SANITIZE, POS, kVolF32>(vx[k].y, cdummy, sv.y);
+                }
+            };
+            if (__all_sync(0xffffffffu, full)) {
+                long long X1 = X + S;
+                const long long S2 = 2 * S;
+#pragma unroll
+                for (int k = 0; k < KZ; k += 2) {
+                    const float4 p0 = seg[(int)(X >> 32)];
+                    const float4 p1 = seg[(int)(X1 >> 32)];
+                    const float f0 = fix_one_plus_frac((uint32_t)X), f1 = fix_one_plus_frac((uint32_t)X1);
+                    add(k, __ffma2_rn(make_float2(f0, f0), make_float2(p0.z, p0.w), make_float2(p0.x, p0.y)));
+                    add(k + 1, __ffma2_rn(make_float2(f1, f1), make_float2(p1.z, p1.w), make_float2(p1.x, p1.y)));
+                    X += S2;
+                    X1 += S2;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < KZ; k++) {
+                    if ((unsigned)(k - kl) < (unsigned)cnt) {
+                        const float4 p = seg[(int)(X >> 32)];
+                        const float f = fix_one_plus_frac((uint32_t)X);
+                        add(k, __ffma2_rn(make_float2(f, f), make_float2(p.z, p.w), make_float2(p.x, p.y)));
+                    }
+                    X += S;
+                }
+            }
+        }
+        if (CHUNK_KAHAN) {
+#pragma unroll
+            for (int k = 0; k < KZ; k++) {
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    float& vq = q ? vx[k].y : vx[k].x;
+                    const float part = q ? pt[k].y : pt[k].x;
+                    float cp = comp_sh[(q * KZ + k) * kBpThreads + tid];
+                    const float y = part - cp;
+                    const float tt = vq + y;
+                    cp = (tt - vq) - y;
+                    vq = tt;
+                    comp_sh[(q * KZ + k) * kBpThreads + tid] = cp;
+                }
+                pt[k] = make_float2(0.0f, 0.0f);
+            }
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        if (!rin[q]) continue;
+        const size_t v0 = ((size_t)zs * H + r0 + q) * W + x;
+        if (VT == kVolF32) {
+            float* vb = static_cast<float*>(a.vol) + v0;
+#pragma unroll
+            for (int k = 0; k < KZ; k++)
+                if (k < nk) vb[k * plane] = q ? vx[k].y : vx[k].x;
+        } else {
+            uint16_t* vb = static_cast<uint16_t*>(a.vol) + v0;
+            const float inv = 1.0f / vsc[q];
+            float m = 0.0f;
+            bool range = false;
+#pragma unroll
+            for (int k = 0; k < KZ; k++) {
+                if (k < nk) {
+                    const float v = (q ? vx[k].y : vx[k].x) - comp_sh[(q * KZ + k) * kBpThreads + tid];
+                    m = fmaxf(m, fabsf(v));
+                    float qv = v * inv;
+                    if (VT == kVolF16 && fabsf(qv) > kF16Max && isfinite(qv)) {
+                        range = true;
+                        qv = copysignf(kF16Max, qv);
+                    }
+                    vb[k * plane] = vol_store16<VT>(qv);
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((tid & 31) == 0 && m > 0.0f) atomicMax(a.vmax + r0 + q, __float_as_uint(m));
+            if (range) atomicOr(a.status, (int)kStatusRange);
+        }
+    }
+}
+
+template <bool SANITIZE, bool POS, int VT>
+__global__ void __launch_bounds__(kBpThreads, Bp2Occ<VT>::value) bp2_kernel(const __grid_constant__ BpLaunch a) {
+    constexpr int KZ = Bp2Occ<VT>::kz;
+    bp2_body<SANITIZE, POS, VT, KZ>(a, blockIdx.x * kTX, blockIdx.y * Bp2<KZ>::kTZ2, a.y0 + 2 * blockIdx.z);
+}
+
+// Batched form: CTA b works on item {problem, x tile, z tile, first row of the pair}.
+template <bool SANITIZE, bool POS, int VT>
+__global__ void __launch_bounds__(kBpThreads, Bp2Occ<VT>::value)
+    bp2_kernel_batch(const BpLaunch* __restrict__ descs, const int4* __restrict__ items) {
+    const int4 it = items[blockIdx.x];
+    constexpr int KZ = Bp2Occ<VT>::kz;
+    bp2_body<SANITIZE, POS, VT, KZ>(descs[it.x], it.y * kTX, it.z * Bp2<KZ>::kTZ2, it.w);
+}
+
+template <bool SANITIZE, bool POS, int VT>
+cudaError_t bp2_attr_one() {
+    const int m = (int)Bp2<Bp2Occ<VT>::kz>::bytes(VT != kVolF32);
+    cudaError_t e = cudaFuncSetAttribute(bp2_kernel<SANITIZE, POS, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(bp2_kernel_batch<SANITIZE, POS, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+}
+
+// FP32 volumes: every rule combination; 16-bit volumes: the plain form only.
+template <int VT>
+void bp2_vt(bool sanitize, bool positivity, const BpLaunch& a, dim3 grid, cudaStream_t s) {
+    const size_t sm = Bp2<Bp2Occ<VT>::kz>::bytes(VT != kVolF32);
+    if constexpr (VT == kVolF32) {
+        if (sanitize) {
+            if (positivity) bp2_kernel<true, true, VT><<<grid, kBpThreads, sm, s>>>(a);
+            else bp2_kernel<true, false, VT><<<grid, kBpThreads, sm, s>>>(a);
+        } else {
+            if (positivity) bp2_kernel<false, true, VT><<<grid, kBpThreads, sm, s>>>(a);
+            else bp2_kernel<false, false, VT><<<grid, kBpThreads, sm, s>>>(a);
+        }
+    } else {
+        (void)sanitize;
+        (void)positivity;
+        bp2_kernel<false, false, VT><<<grid, kBpThreads, sm, s>>>(a);
+    }
+}
+
+template <int VT>
+void bp2_batch_vt(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n, cudaStream_t s) {
+    const size_t sm = Bp2<Bp2Occ<VT>::kz>::bytes(VT != kVolF32);
+    if constexpr (VT == kVolF32) {
+        if (sanitize) {
+            if (positivity) bp2_kernel_batch<true, true, VT><<<n, kBpThreads, sm, s>>>(descs, items);
+            else bp2_kernel_batch<true, false, VT><<<n, kBpThreads, sm, s>>>(descs, items);
+        } else {
+            if (positivity) bp2_kernel_batch<false, true, VT><<<n, kBpThreads, sm, s>>>(descs, items);
+            else bp2_kernel_batch<false, false, VT><<<n, kBpThreads, sm, s>>>(descs, items);
+        }
+    } else {
+        (void)sanitize;
+        (void)positivity;
+        bp2_kernel_batch<false, false, VT><<<n, kBpThreads, sm, s>>>(descs, items);
+    }
+}
+
 template <int VT>
 void bp_batch_vt(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n, cudaStream_t s) {
     if (sanitize) {
@@ -395,9 +737,36 @@ int bp_tile_x() { return kTX; }
 int bp_tile_z() { return kTZ; }
 int bp_segment_pairs(bool wide) { return wide ? 192 : 96; }
 
+// FP32 volumes only: the 16-bit form's per-chunk partial sums cost more than the pairing
+// saves (measured: 89.9 against 85.7 ms per 2048 x 512 x 2048 x 121-tilt backprojection).
+bool bp_row_pairs(int vtype, bool sanitize, bool positivity) {
+    (void)sanitize;
+    (void)positivity;
+    return vtype == kVolF32;
+}
+int bp_pair_tile_z(int vtype) { return 4 * (vtype == kVolF32 ? Bp2Occ<kVolF32>::kz : Bp2Occ<kVolF16>::kz); }
+
+cudaError_t bp_init_attributes() {
+    cudaError_t e;
+    if ((e = bp2_attr_one<false, false, kVolF32>()) != cudaSuccess) return e;
+    if ((e = bp2_attr_one<false, true, kVolF32>()) != cudaSuccess) return e;
+    if ((e = bp2_attr_one<true, false, kVolF32>()) != cudaSuccess) return e;
+    if ((e = bp2_attr_one<true, true, kVolF32>()) != cudaSuccess) return e;
+    if ((e = bp2_attr_one<false, false, kVolBF16>()) != cudaSuccess) return e;
+    return bp2_attr_one<false, false, kVolF16>();
+}
+
 cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpLaunch* descs, const int4* items,
                             int n_items, cudaStream_t s) {
     if (n_items <= 0) return cudaSuccess;
+    if (bp_row_pairs(vtype, sanitize, positivity)) {
+        if (vtype == kVolF32) bp2_batch_vt<kVolF32>(sanitize, positivity, descs, items, n_items, s);
+        else if (vtype == kVolBF16) bp2_batch_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, s);
+        else if (vtype == kVolF16) bp2_batch_vt<kVolF16>(sanitize, positivity, descs, items, n_items, s);
+        else return cudaErrorInvalidValue;
+        count_launch();
+        return cudaGetLastError();
+    }
     if (vtype == kVolF32) bp_batch_vt<kVolF32>(sanitize, positivity, descs, items, n_items, s);
     else if (vtype == kVolBF16) bp_batch_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, s);
     else if (vtype == kVolF16) bp_batch_vt<kVolF16>(sanitize, positivity, descs, items, n_items, s);
@@ -408,6 +777,20 @@ cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpL
 
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s) {
     if (a.T <= 0 || a.y1 <= a.y0) return cudaSuccess;
+    const int tz2 = bp_pair_tile_z(a.vtype);
+    dim3 g2((a.W + kTX - 1) / kTX, (a.D + tz2 - 1) / tz2, (a.y1 - a.y0 + 1) / 2);
+    // row pairs halve the CTAs: below two waves of resident CTAs the one-row kernel's
+    // fuller grid is faster (256 x 64 x 256: 0.093 against 0.126 ms)
+    const long long ctas2 = (long long)g2.x * g2.y * g2.z;
+    if (!a.bprow && !a.wide_seg && bp_row_pairs(a.vtype, a.sanitize, a.positivity) &&
+        ctas2 >= 2LL * Bp2Occ<kVolF32>::value * (a.sms > 0 ? a.sms : 148)) {
+        if (a.vtype == kVolF32) bp2_vt<kVolF32>(a.sanitize, a.positivity, a, g2, s);
+        else if (a.vtype == kVolBF16) bp2_vt<kVolBF16>(false, false, a, g2, s);
+        else if (a.vtype == kVolF16) bp2_vt<kVolF16>(false, false, a, g2, s);
+        else return cudaErrorInvalidValue;
+        count_launch();
+        return cudaGetLastError();
+    }
     dim3 grid((a.W + kTX - 1) / kTX, (a.D + kTZ - 1) / kTZ, a.y1 - a.y0);
     if (a.wide_seg) {
         if (a.vtype != kVolF32) return cudaErrorInvalidValue;

@@ -123,7 +123,7 @@ extern "C" tomo_status tomo_project_and_difference_noalloc(const tomo_geom* geom
         return nerr(TOMO_ERR_INVALID, "bad volume size");
     // the forward projector stages at least one plane row of W voxels (and its pairs) in
     // shared memory: wider volumes are refused before anything is uploaded
-    if (fp_qp(geom->w) == 0 || fp_smem_bytes(1, geom->W, fp_qp(geom->w), 1) > kFpSmemBudget)
+    if (fp_qp(geom->w) == 0 || fp_smem_bytes(1, geom->W, fp_qp(geom->w), 1) > fp_smem_budget(fp_threads(geom->w)))
         return nerr(TOMO_ERR_INVALID, "volume width W too large for the forward projector's shared memory");
     Geometry g{};
     g.W = geom->W;

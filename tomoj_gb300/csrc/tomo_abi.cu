@@ -142,7 +142,9 @@ int auto_tilts_per_cta(const tomo_projector* p, int T, int rows) {
 int fp_split(tomo_projector* p, int T, int rows, int tpc) {
     const Geometry& g = p->g;
     const int groups = (T + tpc - 1) / tpc;
-    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W, g.fractional ? 2 : 1, p->vtype), p->sms);
+    const int nt = fp_threads(g.w);
+    const int P = fp_zparts(groups * rows, g.D, fp_choose_zc(g.W, g.fractional ? 2 : 1, p->vtype, nt), p->sms,
+                            fp_ctas_per_sm(nt));
     if (P <= 1) return 1;
     const size_t need_part = (size_t)P * T * p->npix;
     const size_t need_tk = (size_t)groups * g.h;
@@ -414,6 +416,7 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     a.positivity = p->params.positivity;
     a.sanitize = sanitize || p->vol_flag();
     a.status = p->d_status;
+    a.sms = p->sms;
     if (to_dist) {
         CK(launch_bp_separable(a, p->stream));
         return TOMO_OK;
@@ -600,7 +603,8 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
         return st;
     }
     p->stream = p->own_stream;
-    if (fp_init_attributes() != cudaSuccess || misc_init_attributes() != cudaSuccess) {
+    if (fp_init_attributes() != cudaSuccess || misc_init_attributes() != cudaSuccess ||
+        bp_init_attributes() != cudaSuccess) {
         tomo_destroy(p);
         return fail(TOMO_ERR_CUDA, "cannot configure kernel shared memory");
     }

@@ -27,12 +27,13 @@ constexpr double kFix = 4294967296.0;  // 2^32: fixed-point scale of positions
 #ifndef TOMO_FP_RAYS
 #define TOMO_FP_RAYS 16
 #endif
-#ifndef TOMO_FP_MIN_BLOCKS
-#define TOMO_FP_MIN_BLOCKS 2
-#endif
 constexpr int kFpRays = TOMO_FP_RAYS;
-constexpr int kFpCtasPerSm = TOMO_FP_MIN_BLOCKS;
-constexpr size_t kFpSmemBudget = (kFpCtasPerSm <= 2 ? 112 : 227 / kFpCtasPerSm - 1) * 1024;
+// CTA shape by detector width: 256 threads, two CTAs per SM, up to 512 columns; 512
+// threads, one CTA per SM, above (twice the rays per CTA, so a staged plane serves twice
+// the tilts: 1.4x faster at 2048 columns, slower at 512).
+constexpr int kFpMaxThreads = 512;
+constexpr int fp_ctas_per_sm(int nt) { return nt <= 256 ? 2 : 1; }
+constexpr size_t fp_smem_budget(int nt) { return (size_t)(nt <= 256 ? 112 : 226) * 1024; }
 
 // Device status word bits written by kernels (never trap: the host reads them).
 constexpr int kStatusTimeout = 1;       // an mbarrier wait exceeded its iteration budget
@@ -181,7 +182,7 @@ cudaError_t launch_bp_generic(const BpGenericLaunch& a, cudaStream_t s);
 
 // Depth parts for `ctas` (tilt group, row) CTAs: balances the grid over the resident
 // CTA slots of the device (1 = no split).
-int fp_zparts(int ctas, int D, int zc, int sms);
+int fp_zparts(int ctas, int D, int zc, int sms, int ctas_per_sm);
 // Plane rows are staged with bulk copies when every row starts on a 16-byte boundary.
 inline int fp_use_tma(int W, int vtype, const void* vol) {
     return ((W * vol_elem_bytes(vtype)) % 16 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
@@ -208,6 +209,7 @@ struct BpLaunch {
     int sanitize;           // apply NaN/Inf checks of the reference (images may be non-finite)
     int* status;
     int wide_seg;           // tile footprints up to 192 image columns (scale up to ~2.1)
+    int sms;                // multiprocessors of the device (grid-size choices; 0: unknown)
 };
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
 // Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row}.
@@ -215,6 +217,11 @@ cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpL
                             int n_items, cudaStream_t s);
 int bp_tile_x();
 int bp_tile_z();
+// Whole-row backprojections of this kind run two volume rows per CTA (batch items then
+// name the first row of each pair, every other row), with z tiles of bp_pair_tile_z().
+bool bp_row_pairs(int vtype, bool sanitize, bool positivity);
+int bp_pair_tile_z(int vtype);
+cudaError_t bp_init_attributes();
 // Image columns a BP tile may span for one tilt (segment pairs staged per tilt).
 int bp_segment_pairs(bool wide);
 
@@ -255,13 +262,14 @@ cudaError_t launch_diff(const float* meas, const int* tilts, const float* th, co
 cudaError_t launch_gather(float* dst, const float* src, const int* tilts, int T, size_t npix, cudaStream_t s);
 cudaError_t launch_scan_nonfinite(const float* p, size_t n, int* flags, cudaStream_t s);
 int fp_max_tilts_per_cta(int w);
-int fp_qp(int w);
-int fp_choose_zc(int W, int rows = 1, int vtype = kVolF32);
+int fp_threads(int w);  // threads per CTA for w detector columns
+int fp_qp(int w);       // detector columns per thread (0: w too wide)
+int fp_choose_zc(int W, int rows, int vtype, int nt);
 size_t fp_smem_bytes(int ZC, int W, int qp, int rows = 1, int vtype = kVolF32);
 // Batched forward projection: CTA b runs items[b] = {descriptor, first tilt, row, use_tma};
 // pk = 1 when every descriptor of the launch has a 16-bit volume, 0 when all are FP32.
-cudaError_t launch_fp_batch(int qp, const FpLaunch* descs, const int4* items, int n_items, int zc, size_t smem,
-                            int pk, cudaStream_t s);
+cudaError_t launch_fp_batch(int qp, int nt, const FpLaunch* descs, const int4* items, int n_items, int zc,
+                            size_t smem, int pk, cudaStream_t s);
 cudaError_t fp_init_attributes();
 cudaError_t misc_init_attributes();
 cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s);
