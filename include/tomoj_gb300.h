@@ -263,6 +263,11 @@ tomo_status tomo_set_profiling(tomo_projector* p, int32_t enabled);
 tomo_status tomo_profile_read(tomo_projector* p, double* out4);
 /* Tilts per forward-projection CTA (0 = automatic; tuning knob). */
 tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n);
+/* Volume rows per backprojection thread (tuning knob, no counterpart in the reference):
+ * 0 = by size and storage type, 1 = one row, 2 = two rows (FP32 volumes with a vertical
+ * tilt axis and whole-row centre offsets; otherwise one row).  Results are bitwise the
+ * same either way. */
+tomo_status tomo_set_bp_rows(tomo_projector* p, int32_t rows);
 /* Failure-path test hook (no counterpart in the reference): while enabled, the
  * forward projector of this handle does not issue the bulk copies of each CTA's
  * first plane chunk, so that chunk's bounded mbarrier wait runs out, the CTA

@@ -133,6 +133,41 @@ def test_backprojection_matches_oracle(engine, oracle_lib, case, kind):
         hd.close()
 
 
+@pytest.mark.parametrize("positivity", [False, True])
+@pytest.mark.parametrize("shape", [(64, 12, 48), (70, 7, 75)])
+def test_backprojection_row_pairs_match_one_row_and_oracle(engine, oracle_lib, shape, positivity):
+    """Two volume rows per backprojection thread (forced; the size rule would pick one row
+    for volumes this small): bitwise the one-row kernel, and the oracle to 1e-5.  An odd
+    row count leaves the last pair with one row; a sub-range of rows must leave the rows
+    outside it untouched."""
+    W, H, D = shape
+    c = series_case(W=W, H=H, D=D, n=9, seed=17, noise=0.0)
+    rng = np.random.default_rng(4)
+    imgs = rng.normal(0, 1, (c["n"], c["h"], c["w"])).astype(np.float32)
+    c2 = dict(c, series=imgs, T=np.tile([1.0, 0, 0, 1, 0, 0], (c["n"], 1)))
+    start = rng.standard_normal((D, H, W)).astype(np.float32)
+    order = [4, 0, 8, 2, 6, 1]
+    y0, y1 = 1, H
+    got = {}
+    for rows in (1, 2):
+        hd = Handle(engine, c2, positivity=positivity, vol=start)
+        try:
+            _abi.check(engine.tomo_set_bp_rows(hd.h, rows))
+            for i in order:
+                _abi.check(engine.tomo_add_projection(hd.h, i))
+            _abi.check(engine.tomo_backproject(hd.h, y0, y1))
+            got[rows] = hd.volume()
+        finally:
+            hd.close()
+    assert np.array_equal(got[1].view(np.uint32), got[2].view(np.uint32))
+    assert np.array_equal(got[2][:, :y0], start[:, :y0])
+    ref = start.copy()
+    g = O.Geom(W, H, D, W, H, positivity=positivity)
+    for i in order:
+        O.backproject(ref, g, c["eul"][i], imgs[i], y0, y1)
+    assert rel_l2(got[2] - start, ref - start) <= TOL_PASS, rel_l2(got[2] - start, ref - start)
+
+
 def test_alignment_matches_oracle(engine, oracle_lib, case):
     hd = Handle(engine, case)
     try:
@@ -248,6 +283,28 @@ def test_tvm_iteration_matches_oracle(engine, oracle_lib):
             O.ossart_iteration(ref, c["g"], c["eul"], meas, order, 1.0, 0)
             O.tv_denoise(ref, 25.0, 1.0, 0.01, 5)
         assert rel_l2(got, ref) <= 1e-5 * 10, rel_l2(got, ref)
+    finally:
+        hd.close()
+
+
+@pytest.mark.parametrize("shape", [(70, 19, 75), (33, 9, 33), (2, 3, 40)])
+def test_tv_denoise_matches_oracle_bitwise(engine, oracle_lib, shape):
+    """The fused TV step (one kernel per inner step, u rebuilt in shared memory) against
+    TotalVariationDenoising_3D's updateP / updateU sequence: identical float expressions
+    in the same order, so the denoised volume is the oracle's bit for bit.  The shapes
+    cover several x / y / z tiles of the kernel, ragged tile edges and a two-column volume."""
+    W, H, D = shape
+    c = series_case(W=W, H=H, D=D, n=3, seed=21)
+    rng = np.random.default_rng(5)
+    vol = (rng.standard_normal((D, H, W)) * 3.0).astype(np.float32)
+    hd = Handle(engine, c, vol=vol)
+    try:
+        _abi.check(engine.tomo_set_tvm(hd.h, 25.0, 1.0, 0.01, 5))
+        _abi.check(engine.tomo_end_iteration(hd.h))
+        got = hd.volume()
+        ref = vol.copy()
+        O.tv_denoise(ref, 25.0, 1.0, 0.01, 5)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), float(np.abs(got - ref).max())
     finally:
         hd.close()
 

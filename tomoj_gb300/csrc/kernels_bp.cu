@@ -782,8 +782,9 @@ cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s) {
     // row pairs halve the CTAs: below two waves of resident CTAs the one-row kernel's
     // fuller grid is faster (256 x 64 x 256: 0.093 against 0.126 ms)
     const long long ctas2 = (long long)g2.x * g2.y * g2.z;
+    const bool big = ctas2 >= 2LL * Bp2Occ<kVolF32>::value * (a.sms > 0 ? a.sms : 148);
     if (!a.bprow && !a.wide_seg && bp_row_pairs(a.vtype, a.sanitize, a.positivity) &&
-        ctas2 >= 2LL * Bp2Occ<kVolF32>::value * (a.sms > 0 ? a.sms : 148)) {
+        (a.rows_mode == 2 || (a.rows_mode == 0 && big))) {
         if (a.vtype == kVolF32) bp2_vt<kVolF32>(a.sanitize, a.positivity, a, g2, s);
         else if (a.vtype == kVolBF16) bp2_vt<kVolBF16>(false, false, a, g2, s);
         else if (a.vtype == kVolF16) bp2_vt<kVolF16>(false, false, a, g2, s);

@@ -285,33 +285,19 @@ __global__ void reduce_err_batch_kernel(const ErrReduce* __restrict__ jobs) {
     if ((threadIdx.x & 31) == 0) j.err[t] = s;
 }
 
-// TotalVariationDenoising_3D.updateP (Filters/.../TotalVariationDenoising_3D.java:115-156).
-__global__ void tv_p_kernel(const float* __restrict__ u, float* px, float* py, float* pz, int W, int H, int D,
-                            float theta, float g, float dt) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= W) return;
-    const size_t o = ((size_t)z * H + y) * W + x;
-    const float u0 = u[o];
-    const float duy = (y < H - 1) ? u[o + W] - u0 : 0.0f;
-    const float dux = (x < W - 1) ? u[o + 1] - u0 : 0.0f;
-    const float duz = (z < D - 1) ? u[o + (size_t)W * H] - u0 : 0.0f;
-    const float s = duy * duy + dux * dux + duz * duz;
-    const float dd1 = 1.0f + dt / theta / g * fabsf(__fsqrt_rn(s));
-    const float k = dt / theta;
-    px[o] = __fdiv_rn(px[o] - k * dux, dd1);
-    py[o] = __fdiv_rn(py[o] - k * duy, dd1);
-    pz[o] = __fdiv_rn(pz[o] - k * duz, dd1);
-}
+// TotalVariationDenoising_3D (Filters/.../TotalVariationDenoising_3D.java:84-202): inner
+// steps of updateP (:115-156) then updateU (:158-202), fused.  The step k -> k + 1 needs
+// u_k = f - theta * div p_k only where updateP reads it (the voxel and its +x, +y, +z
+// neighbours), so one kernel rebuilds u_k plane by plane in shared memory from p_k and f
+// and writes p_{k+1}; u itself is never stored between steps.  p is double-buffered
+// (a CTA reads p_k of its -x / -y / -z neighbours while others write p_{k+1}).  Every
+// value is computed with updateU's and updateP's float expressions in their order, so
+// the result is the unfused sequence's bit for bit.
 
-// TotalVariationDenoising_3D.updateU (TotalVariationDenoising_3D.java:158-202).
-__global__ void tv_u_kernel(const float* __restrict__ f, float* __restrict__ u, const float* __restrict__ px,
-                            const float* __restrict__ py, const float* __restrict__ pz, int W, int H, int D,
-                            float theta) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= W) return;
-    const size_t o = ((size_t)z * H + y) * W + x;
+// u = f - theta * div p at flat index o = (z, y, x), with updateU's boundary rules.
+__device__ __forceinline__ float tv_u_point(const float* f, const float* __restrict__ px, const float* __restrict__ py,
+                                            const float* __restrict__ pz, size_t o, int x, int y, int z, int W, int H,
+                                            int D, float theta) {
     float div;
     if (x == 0) div = px[o];
     else if (x == W - 1) div = -px[o];
@@ -322,7 +308,68 @@ __global__ void tv_u_kernel(const float* __restrict__ f, float* __restrict__ u, 
     if (z == 0) div += pz[o];
     else if (z == D - 1) div += -pz[o];
     else div += pz[o] - pz[o - (size_t)W * H];
-    u[o] = f[o] - theta * div;
+    return f[o] - theta * div;
+}
+
+constexpr int kTvX = 32, kTvY = 8, kTvZ = 32;  // CTA: 32 x 8 columns, marching 32 planes
+
+// One inner step: p_b = updateP(u_a, p_a) with u_a = updateU(f, p_a); FIRST: p_a = 0, u_a = f.
+template <bool FIRST>
+__global__ void __launch_bounds__(kTvX * kTvY) tv_step_kernel(const float* __restrict__ f, const float* __restrict__ pxa,
+                                                           const float* __restrict__ pya, const float* __restrict__ pza,
+                                                           float* __restrict__ pxb, float* __restrict__ pyb,
+                                                           float* __restrict__ pzb, int W, int H, int D, float theta,
+                                                           float g, float dt) {
+    __shared__ float us[2][kTvY + 1][kTvX + 1];  // u of planes z and z + 1 over the tile and its +x / +y halo
+    const int tx = threadIdx.x % kTvX, ty = threadIdx.x / kTvX;
+    const int x0 = blockIdx.x * kTvX, y0 = blockIdx.y * kTvY, z0 = blockIdx.z * kTvZ;
+    const int z1 = min(z0 + kTvZ, D);
+    const size_t WH = (size_t)W * H;
+    auto fill = [&](int b, int z) {
+        for (int e = threadIdx.x; e < (kTvY + 1) * (kTvX + 1); e += kTvX * kTvY) {
+            const int ly = e / (kTvX + 1), lx = e - ly * (kTvX + 1);
+            const int x = x0 + lx, y = y0 + ly;
+            float v = 0.0f;
+            if (x < W && y < H) {
+                const size_t o = (size_t)z * WH + (size_t)y * W + x;
+                v = FIRST ? f[o] : tv_u_point(f, pxa, pya, pza, o, x, y, z, W, H, D, theta);
+            }
+            us[b][ly][lx] = v;
+        }
+    };
+    fill(0, z0);
+    const int x = x0 + tx, y = y0 + ty;
+    const float k = dt / theta;
+    int cur = 0;
+    for (int z = z0; z < z1; z++) {
+        if (z + 1 < D) fill(cur ^ 1, z + 1);
+        __syncthreads();
+        if (x < W && y < H) {
+            const size_t o = (size_t)z * WH + (size_t)y * W + x;
+            const float u0 = us[cur][ty][tx];
+            const float duy = (y < H - 1) ? us[cur][ty + 1][tx] - u0 : 0.0f;
+            const float dux = (x < W - 1) ? us[cur][ty][tx + 1] - u0 : 0.0f;
+            const float duz = (z < D - 1) ? us[cur ^ 1][ty][tx] - u0 : 0.0f;
+            const float s = duy * duy + dux * dux + duz * duz;
+            const float dd1 = 1.0f + dt / theta / g * fabsf(__fsqrt_rn(s));
+            const float ox = FIRST ? 0.0f : pxa[o], oy = FIRST ? 0.0f : pya[o], oz = FIRST ? 0.0f : pza[o];
+            pxb[o] = __fdiv_rn(ox - k * dux, dd1);
+            pyb[o] = __fdiv_rn(oy - k * duy, dd1);
+            pzb[o] = __fdiv_rn(oz - k * duz, dd1);
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+}
+
+// The closing updateU, in place: fu holds f and receives u (each voxel reads only its own f).
+__global__ void tv_final_kernel(float* fu, const float* __restrict__ px, const float* __restrict__ py,
+                                const float* __restrict__ pz, int W, int H, int D, float theta) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= W) return;
+    const size_t o = ((size_t)z * H + y) * W + x;
+    fu[o] = tv_u_point(fu, px, py, pz, o, x, y, z, W, H, D, theta);
 }
 
 __global__ void fill_kernel(float* p, size_t n, float v) {
@@ -716,18 +763,22 @@ cudaError_t launch_reduce_err_batch(const ErrReduce* jobs, int n_jobs, int max_T
     return cudaGetLastError();
 }
 
-cudaError_t launch_tv_p(const float* u, float* px, float* py, float* pz, int W, int H, int D, float theta, float g,
-                        float dt, cudaStream_t s) {
-    dim3 grid((W + 127) / 128, H, D);
-    tv_p_kernel<<<grid, 128, 0, s>>>(u, px, py, pz, W, H, D, theta, g, dt);
+cudaError_t launch_tv_step(const float* f, const float* const pa[3], float* const pb[3], bool first, int W, int H,
+                           int D, float theta, float g, float dt, cudaStream_t s) {
+    dim3 grid((W + kTvX - 1) / kTvX, (H + kTvY - 1) / kTvY, (D + kTvZ - 1) / kTvZ);
+    if (first)
+        tv_step_kernel<true><<<grid, kTvX * kTvY, 0, s>>>(f, pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], W, H, D, theta,
+                                                          g, dt);
+    else
+        tv_step_kernel<false><<<grid, kTvX * kTvY, 0, s>>>(f, pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], W, H, D, theta,
+                                                           g, dt);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* py, const float* pz, int W, int H,
-                        int D, float theta, cudaStream_t s) {
+cudaError_t launch_tv_final(float* fu, const float* const p[3], int W, int H, int D, float theta, cudaStream_t s) {
     dim3 grid((W + 127) / 128, H, D);
-    tv_u_kernel<<<grid, 128, 0, s>>>(f, u, px, py, pz, W, H, D, theta);
+    tv_final_kernel<<<grid, 128, 0, s>>>(fu, p[0], p[1], p[2], W, H, D, theta);
     count_launch();
     return cudaGetLastError();
 }

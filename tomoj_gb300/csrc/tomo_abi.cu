@@ -417,6 +417,7 @@ tomo_status run_bp(tomo_projector* p, const float* imgs, const int* d_tilts, int
     a.sanitize = sanitize || p->vol_flag();
     a.status = p->d_status;
     a.sms = p->sms;
+    a.rows_mode = p->bp_rows;
     if (to_dist) {
         CK(launch_bp_separable(a, p->stream));
         return TOMO_OK;
@@ -435,27 +436,22 @@ tomo_status need_series(tomo_projector* p) {
 tomo_status tv_denoise(tomo_projector* p) {
     const Geometry& g = p->g;
     if (p->tv_iters <= 0) return TOMO_OK;
-    const size_t bytes = sizeof(float) * p->nvox;
     // reduced storage: the step runs on an FP32 copy f and packs u back with fresh slab scales
     const bool red = p->vtype != kVolF32;
-    const float* f = red ? p->d_tv_f : p->d_vol;
+    float* f = red ? p->d_tv_f : p->d_vol;
     if (red) CK(launch_vol_unpack(p->vol(), p->vtype, p->d_vscale, g.H, 0, g.W, g.H, g.D, p->d_tv_f, p->stream));
-    CK(cudaMemcpyAsync(p->d_tv_u, f, bytes, cudaMemcpyDeviceToDevice, p->stream));
-    CK(cudaMemsetAsync(p->d_px, 0, bytes, p->stream));
-    CK(cudaMemsetAsync(p->d_py, 0, bytes, p->stream));
-    CK(cudaMemsetAsync(p->d_pz, 0, bytes, p->stream));
+    float* a[3] = {p->d_px, p->d_py, p->d_pz};
+    float* b[3] = {p->d_qx, p->d_qy, p->d_qz};
     for (int it = 0; it < p->tv_iters; it++) {
-        CK(launch_tv_p(p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->tv_g, p->tv_dt,
-                       p->stream));
-        CK(launch_tv_u(f, p->d_tv_u, p->d_px, p->d_py, p->d_pz, g.W, g.H, g.D, p->tv_theta, p->stream));
+        CK(launch_tv_step(f, a, b, it == 0, g.W, g.H, g.D, p->tv_theta, p->tv_g, p->tv_dt, p->stream));
+        std::swap(a, b);
     }
+    CK(launch_tv_final(f, a, g.W, g.H, g.D, p->tv_theta, p->stream));
     if (red) {
         CK(cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * g.H, p->stream));
-        CK(launch_vol_rowmax(p->d_tv_u, g.H, 0, g.W, g.H, g.D, p->d_vmax, p->stream));
-        CK(launch_vol_pack(p->d_tv_u, g.H, 0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax, p->d_status,
+        CK(launch_vol_rowmax(p->d_tv_f, g.H, 0, g.W, g.H, g.D, p->d_vmax, p->stream));
+        CK(launch_vol_pack(p->d_tv_f, g.H, 0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax, p->d_status,
                            p->stream));
-    } else {
-        CK(cudaMemcpyAsync(p->d_vol, p->d_tv_u, bytes, cudaMemcpyDeviceToDevice, p->stream));
     }
     return TOMO_OK;
 }
@@ -1263,11 +1259,13 @@ tomo_status tomo_set_weighting(tomo_projector* p, int32_t kind, double radius, c
 tomo_status tomo_set_tvm(tomo_projector* p, float theta, float g, float dt, int32_t iterations) {
     if (!p) return fail(TOMO_ERR_INVALID, "null handle");
     if (iterations < 0) return fail(TOMO_ERR_INVALID, "negative iteration count");
-    if (iterations > 0 && !p->d_tv_u) {
-        CKS(alloc_n(p, &p->d_tv_u, p->nvox));
+    if (iterations > 0 && !p->d_px) {
         CKS(alloc_n(p, &p->d_px, p->nvox));
         CKS(alloc_n(p, &p->d_py, p->nvox));
         CKS(alloc_n(p, &p->d_pz, p->nvox));
+        CKS(alloc_n(p, &p->d_qx, p->nvox));
+        CKS(alloc_n(p, &p->d_qy, p->nvox));
+        CKS(alloc_n(p, &p->d_qz, p->nvox));
     }
     if (iterations > 0 && p->vtype != kVolF32 && !p->d_tv_f) CKS(alloc_n(p, &p->d_tv_f, p->nvox));
     p->tv_theta = theta;
@@ -1390,6 +1388,12 @@ tomo_status tomo_profile_read(tomo_projector* p, double* out4) {
     out4[1] = (double)p->prof_n[0];
     out4[2] = p->prof_ms[1];
     out4[3] = (double)p->prof_n[1];
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_bp_rows(tomo_projector* p, int32_t rows) {
+    if (!p || rows < 0 || rows > 2) return fail(TOMO_ERR_INVALID, "rows per backprojection thread: 0, 1 or 2");
+    p->bp_rows = rows;
     return TOMO_OK;
 }
 

@@ -74,7 +74,8 @@ struct tomo_projector {
     float2 *d_w2a = nullptr, *d_w2b = nullptr;
     int w2chunk = 0;
     tomo::DftRowPlan w2pw{}, w2ph{};
-    float *d_tv_u = nullptr, *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;
+    float *d_px = nullptr, *d_py = nullptr, *d_pz = nullptr;  // TV dual field, two buffers (lazy)
+    float *d_qx = nullptr, *d_qy = nullptr, *d_qz = nullptr;
     float* d_prev = nullptr;
 
     std::vector<double> euler;
@@ -114,6 +115,7 @@ struct tomo_projector {
     void* bp_target() const { return bayes ? static_cast<void*>(d_dist) : vol(); }
     std::atomic<int> cancel{0};
     int tilts_per_cta = 0;  // forward projector tilt grouping (0 = automatic)
+    int bp_rows = 0;        // backprojection rows per thread (0 = automatic, 1, 2)
     int hold_first_copy = 0;  // failure-path test hook of the forward projector (tomo_debug_hold_first_copy)
     // row streams: K row ranges of an OS-SART iteration run on K streams (rows are
     // independent), so that forward and backprojections of different rows overlap

@@ -210,6 +210,7 @@ struct BpLaunch {
     int* status;
     int wide_seg;           // tile footprints up to 192 image columns (scale up to ~2.1)
     int sms;                // multiprocessors of the device (grid-size choices; 0: unknown)
+    int rows_mode;          // volume rows per thread: 0 by size and type, 1 one, 2 two (where allowed)
 };
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
 // Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row}.
@@ -280,10 +281,11 @@ struct ErrReduce {
     int T, h;
 };
 cudaError_t launch_reduce_err_batch(const ErrReduce* jobs, int n_jobs, int max_T, cudaStream_t s);
-cudaError_t launch_tv_p(const float* u, float* px, float* py, float* pz, int W, int H, int D, float theta, float g,
-                        float dt, cudaStream_t s);
-cudaError_t launch_tv_u(const float* f, float* u, const float* px, const float* py, const float* pz, int W, int H,
-                        int D, float theta, cudaStream_t s);
+// One fused TV inner step p_b = updateP(updateU(f, p_a), p_a) (first: p_a = 0), and the
+// closing updateU written in place over f.
+cudaError_t launch_tv_step(const float* f, const float* const pa[3], float* const pb[3], bool first, int W, int H,
+                           int D, float theta, float g, float dt, cudaStream_t s);
+cudaError_t launch_tv_final(float* fu, const float* const p[3], int W, int H, int D, float theta, cudaStream_t s);
 cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t s);
 cudaError_t launch_fista(float* rec, const float* prev, size_t n, double factor, cudaStream_t s);
 cudaError_t launch_long_object(float* norm, int T, int h, int w, cudaStream_t s);
