@@ -404,12 +404,21 @@ def run_engine(args, wl):
                   "vs_one_plain_iteration": cms / (ms / args.steps / (1 + wl["n_iter"]))}
 
     # ---- roofline of the dominant kernel ----
+    # Both kernels keep the tilts of a launch on chip (a staged plane serves every tilt; a
+    # voxel is loaded once for all tilts), so DRAM carries about one volume read (+ write)
+    # per launch and the ceiling that binds is the shared-memory data path: one 128-byte
+    # wavefront per SM clock.  Wavefront and DRAM byte counts per launch come from the ncu
+    # capture summarised in profiles/kernels_ossart512.json (same workload, same launches);
+    # launch durations are this run's CUDA events.
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
-        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        hbm_peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
     else:
-        peak, peak_src = FALLBACK_HBM_GBS, "fallback"
+        hbm_peak, peak_src = FALLBACK_HBM_GBS, "fallback"
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    smem_peak = 128.0 * sms * sm_mhz * 1e6 / 1e9  # GB/s
     fp_ms, fp_n, bp_ms, bp_n = prof
     upd = n if wl["update"] == 0 else wl["update"]
     nsub = (n + upd - 1) // upd
@@ -417,45 +426,48 @@ def run_engine(args, wl):
     npix = W * H
     updates_per_launch = nvox * tilts_per_launch
     rays = tilts_per_launch * npix
-    # Algorithmic bytes per launch (per-unit accounting of an unfused projector that
-    # streams the volume once per tilt): FP 4 B per voxel-update (volume read) + 16 B per
-    # ray (measurement read, projection / norm / difference writes); BP 8 B per
-    # voxel-update (volume read + write) + 4 B per ray (difference read).
-    fp_alg = 4.0 * updates_per_launch + 16.0 * rays
-    bp_alg = 8.0 * updates_per_launch + 4.0 * rays
-    # Compulsory bytes of the fused kernels: the volume once per launch.
-    fp_comp = 4.0 * nvox + 16.0 * rays
-    bp_comp = 8.0 * nvox + 4.0 * rays
-    kernels = {
-        "fp_separable": {"avg_ms": fp_ms / max(fp_n, 1), "alg": fp_alg, "comp": fp_comp, "launches": int(fp_n)},
-        "bp_separable": {"avg_ms": bp_ms / max(bp_n, 1), "alg": bp_alg, "comp": bp_comp, "launches": int(bp_n)},
-    }
+    ncu = {}
+    kpath = os.path.join(ROOT, "profiles", "kernels_ossart512.json")
+    if os.path.exists(kpath) and args.workload == "ossart512":
+        ncu = json.load(open(kpath))["kernels"]
+    # unfused-equivalent bytes (a projector streaming the volume once per tilt, FP32): FP 4 B
+    # per voxel-update + 16 B per ray; BP 8 B per voxel-update + 4 B per ray
+    unfused = {"fp_separable": 4.0 * updates_per_launch + 16.0 * rays,
+               "bp_separable": 8.0 * updates_per_launch + 4.0 * rays}
+    compulsory = {"fp_separable": 4.0 * nvox + 16.0 * rays, "bp_separable": 8.0 * nvox + 4.0 * rays}
+    kernels = {}
+    for k, ms_tot, cnt in (("fp_separable", fp_ms, fp_n), ("bp_separable", bp_ms, bp_n)):
+        avg_s = ms_tot / max(cnt, 1) / 1000.0
+        nk = ncu.get(k, {})
+        dram = nk.get("dram_bytes_per_launch", compulsory[k])
+        kv = {"avg_ms": avg_s * 1000.0, "launches": int(cnt),
+              "hbm_GBs": dram / avg_s / 1e9, "hbm_frac": dram / avg_s / 1e9 / hbm_peak,
+              "dram_bytes_per_launch": dram, "dram_bytes_source": "ncu" if "dram_bytes_per_launch" in nk else "compulsory",
+              "unfused_equivalent_GBs": unfused[k] / avg_s / 1e9}
+        if "smem_wavefronts_per_launch" in nk:
+            sb = 128.0 * nk["smem_wavefronts_per_launch"]
+            kv.update({"smem_GBs": sb / avg_s / 1e9, "smem_frac": sb / avg_s / 1e9 / smem_peak})
+        kernels[k] = kv
     dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
     kd = kernels[dom]
-    sec = kd["avg_ms"] / 1000.0
-    achieved = kd["alg"] / sec / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_ossart512.json")
-    if os.path.exists(tpath) and args.workload == "ossart512":
-        traffic = json.load(open(tpath)).get(dom)
-    roofline = {
-        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-        "bytes_per_unit": ("FP: 4 B per voxel-update + 16 B per ray; BP: 8 B per voxel-update + 4 B per ray "
-                           "(FP32, unfused-projector accounting)"),
-        "algorithmic_bytes_per_launch": kd["alg"], "avg_launch_ms": kd["avg_ms"],
+    if "smem_frac" in kd:
+        roofline = {"bound": "smem", "kernel": dom, "achieved": kd["smem_GBs"], "peak": smem_peak, "unit": "GB/s",
+                    "frac": kd["smem_frac"], "peak_source": f"128 B per SM clock x {sms} SMs x {sm_mhz:.0f} MHz"}
+    else:
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": kd["hbm_GBs"], "peak": hbm_peak, "unit": "GB/s",
+                    "frac": kd["hbm_frac"], "peak_source": peak_src}
+    roofline.update({
+        "traffic": kd["dram_bytes_per_launch"], "avg_launch_ms": kd["avg_ms"],
         "updates_per_launch": updates_per_launch,
-        "compulsory_bytes_per_launch": kd["comp"],
-        "compulsory_GBs": kd["comp"] / sec / 1e9, "compulsory_frac": kd["comp"] / sec / 1e9 / peak,
-        "kernels": {k: {"avg_ms": v["avg_ms"], "launches": v["launches"],
-                        "GBs": v["alg"] / (v["avg_ms"] / 1000.0) / 1e9,
-                        "compulsory_GBs": v["comp"] / (v["avg_ms"] / 1000.0) / 1e9} for k, v in kernels.items()},
-        # the whole job under the plain-form accounting of a projector that streams the
-        # volume once per tilt: 12 B per voxel-update (4 B FP read + 8 B BP read-write);
-        # above 1 means the fused kernels move less than that per update
-        "job": {"bytes_per_update": 12, "achieved_GBs": value * 12.0 / 1e9 / world,
-                "frac_per_gpu": value * 12.0 / 1e9 / world / peak},
-    }
+        "hbm": {"achieved": kd["hbm_GBs"], "peak": hbm_peak, "unit": "GB/s", "frac": kd["hbm_frac"],
+                "peak_source": peak_src, "bytes": kd["dram_bytes_source"]},
+        "counts_source": "profiles/kernels_ossart512.json" if ncu else None,
+        "kernels": kernels,
+        # the plain-form accounting of a projector streaming the volume once per tilt: 12 B per
+        # voxel-update; above 1 only because the fused kernels never move those bytes
+        "unfused_equivalent": {"bytes_per_update": 12, "achieved_GBs": value * 12.0 / 1e9 / world,
+                               "frac_of_hbm": value * 12.0 / 1e9 / world / hbm_peak},
+    })
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu = None
@@ -703,36 +715,22 @@ def phantom_on_device(W, H, D, n_ell, seed, device):
     return vol
 
 
-def run_precision_leg(lib, args):
-    """BASELINE config 4, bounded: a 2048 x 512 x 2048 (W x H x D) phantom, 121 projections
-    of 2048 x 512 at -60..+60 deg in 1 deg steps with Poisson noise at 50 e-/px; SIRT
-    iterations with the volume stored in FP32, BF16 and FP16 (per-row slab scales,
-    Kahan-compensated FP32 backprojection sums, FP64 residual norms).  Reports each
-    form's voxel-updates/s and the reduced forms' relative L2 against the FP32 form
-    after the same iterations (against the FP64 oracle: tests/test_precision_gpu.py)."""
+def _config4_series(lib, W, H, D, n, seed, stream):
+    """The tilt-series of the reduced-precision workload: the seeded ellipsoid phantom
+    (evaluated on the GPU), its FP32 forward projection by the engine at -60..+60 deg in
+    equal steps, then Poisson noise at 50 e-/px.  Returns (series float32 (n, H, W), eulers)."""
     import torch
     from tomoj_gb300 import _abi
     from tomoj_gb300 import phantom as P
-    W, H, D = args.prec_size
-    n = 121
-    angles = np.linspace(-60.0, 60.0, n)
-    eul = euler_y(angles)
-    stream = torch.cuda.current_stream()
-    t0 = time.time()
-    vol = phantom_on_device(W, H, D, P.n_ellipsoids_for(W, H, D), 1238, "cuda")
-
-    def create(prec):
-        g = _abi.make_geom(W, H, D, W, H, n)
-        p = _abi.make_params(fill=_abi.FILL_NAN, precision=prec)
-        h = C.c_void_p()
-        _abi.check(lib.tomo_create(C.byref(g), C.byref(p), C.byref(h)))
-        _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
-        return h
-
-    # tilt-series: the engine's FP32 forward projection of the phantom, then Poisson noise
-    h = create(_abi.PREC_FP32)
+    eul = euler_y(np.linspace(-60.0, 60.0, n))
+    vol = phantom_on_device(W, H, D, P.n_ellipsoids_for(W, H, D), seed, "cuda")
+    g = _abi.make_geom(W, H, D, W, H, n)
+    prm = _abi.make_params(fill=_abi.FILL_NAN)
+    h = C.c_void_p()
+    _abi.check(lib.tomo_create(C.byref(g), C.byref(prm), C.byref(h)))
     series = np.empty((n, H, W), np.float32)
     try:
+        _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
         _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
         torch.cuda.synchronize()
         _abi.check(lib.tomo_set_volume(h, C.c_void_p(vol.data_ptr()), 1, 0, H))
@@ -745,38 +743,154 @@ def run_precision_leg(lib, args):
         lib.tomo_destroy(h)
     del vol
     torch.cuda.empty_cache()
-    series = P.add_poisson_noise(np.nan_to_num(series), 50.0, 1239)
+    return P.add_poisson_noise(np.nan_to_num(series), 50.0, seed + 1), eul
+
+
+def _device_rel_l2(a, b, chunk=64):
+    """||a - b|| / ||b|| of two (D, H, W) float32 device tensors, accumulated in FP64 by plane chunks."""
+    num = den = 0.0
+    for z in range(0, a.shape[0], chunk):
+        x, y = a[z:z + chunk].double(), b[z:z + chunk].double()
+        num += float(((x - y) ** 2).sum())
+        den += float((y ** 2).sum())
+    return (num / max(den, 1e-300)) ** 0.5
+
+
+def _schedule(lib, W, H, D, series, eul, prec, n_sirt, n_tvm, seed, stream):
+    """n_sirt SIRT iterations then n_tvm TVM iterations (SIRT + TV denoise: theta 25, g 1,
+    dt = lambda = 0.01, 5 inner steps) on one handle; both parts timed with CUDA events on the
+    handle's stream.  Returns (figures, volume after SIRT, final volume) with the volumes as
+    FP32 device tensors."""
+    import torch
+    from tomoj_gb300 import _abi
+    n = series.shape[0]
+    g = _abi.make_geom(W, H, D, W, H, n)
+    prm = _abi.make_params(fill=_abi.FILL_NAN, precision=prec)
+    h = C.c_void_p()
+    _abi.check(lib.tomo_create(C.byref(g), C.byref(prm), C.byref(h)))
+    try:
+        _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+        _abi.check(lib.tomo_run_ossart(h, 1, 1.0, 0, seed, 0, H, 1, None))  # warm-up: tables, graph
+        _abi.check(lib.tomo_fill_volume(h, 0.0))
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        _abi.check(lib.tomo_run_ossart(h, n_sirt, 1.0, 0, seed, 0, H, 1, None))
+        ev[1].record(stream)
+        after_sirt = torch.empty((D, H, W), dtype=torch.float32, device="cuda")
+        _abi.check(lib.tomo_get_volume(h, C.c_void_p(after_sirt.data_ptr()), 1, 0, H))
+        _abi.check(lib.tomo_set_tvm(h, 25.0, 1.0, 0.01, 5))
+        ev[1].synchronize()
+        ev[2].record(stream)
+        _abi.check(lib.tomo_run_ossart(h, n_tvm, 1.0, 0, seed, 0, H, 1, None))
+        ev3 = torch.cuda.Event(enable_timing=True)
+        ev3.record(stream)
+        torch.cuda.synchronize()
+        final = torch.empty((D, H, W), dtype=torch.float32, device="cuda")
+        _abi.check(lib.tomo_get_volume(h, C.c_void_p(final.data_ptr()), 1, 0, H))
+        torch.cuda.synchronize()
+    finally:
+        lib.tomo_destroy(h)
+    sirt_ms = ev[0].elapsed_time(ev[1])
+    tvm_ms = ev[2].elapsed_time(ev3)
+    ups = W * H * D * n
+    fig = {"sirt_voxel_updates_per_s": ups * n_sirt / (sirt_ms / 1000.0), "sirt_ms_per_iteration": sirt_ms / n_sirt,
+           "tvm_ms_per_iteration": tvm_ms / max(n_tvm, 1),
+           "schedule_voxel_updates_per_s": ups * (n_sirt + n_tvm) / ((sirt_ms + tvm_ms) / 1000.0),
+           "volume_bytes": W * H * D * (4 if prec == _abi.PREC_FP32 else 2)}
+    return fig, after_sirt, final
+
+
+def _fp64_reference(series, eul, W, H, D, n_sirt, n_tvm, seed, threads):
+    """The FP64 oracle (oracle/oracle64.py) on the same schedule, whole volume."""
+    from oracle import oracle as O
+    from oracle import oracle64 as O64
+    lib = _abi_mod().load()
+    n = series.shape[0]
+    O64.set_threads(threads)
+    g = O.Geom(W, H, D, W, H)
+    meas = np.ascontiguousarray(series, np.float64)
+    vol = np.zeros((D, H, W), np.float64)
+    for it in range(n_sirt):
+        O64.ossart_iteration(vol, g, eul, meas, O.order_shuffle(eul, int(lib.tomo_first_index(seed, it, n))), 1.0, 0)
+    after_sirt = vol.copy()
+    for it in range(n_tvm):
+        O64.ossart_iteration(vol, g, eul, meas, O.order_shuffle(eul, int(lib.tomo_first_index(seed, it, n))), 1.0, 0)
+        O64.tv_denoise(vol, 25.0, 1.0, 0.01, 5)
+    return after_sirt, vol
+
+
+def run_precision_leg(lib, args):
+    """BASELINE config 4 at its schedule: a W x H x D = 2048 x 512 x 2048 phantom, 121
+    projections of 2048 x 512 at -60..+60 deg in 1 deg steps with Poisson noise at 50 e-/px;
+    50 SIRT iterations, then 20 TVM iterations (SIRT + TV denoise, lambda = dt = 0.01), with
+    the volume stored in FP32, BF16 and FP16 (per-row slab scales, Kahan-compensated FP32
+    backprojection sums, FP64 residual norms).  Reports per storage its voxel-updates/s and
+    its relative L2 against the FP32 form (whole volume, after the SIRT part and at the end).
+
+    The FP64 oracle costs ~20 ns per voxel-update per core (about 18 min per volume row of
+    this size for the 50 SIRT iterations), so the relative L2 against FP64 is measured on the
+    same schedule, tilts, noise and phantom generator at args.prec_check (384 x 32 x 384 by
+    default), whole volume, with the oracle running on all host cores beside the GPU work."""
+    import threading
+    import torch
+    from tomoj_gb300 import _abi
+    stream = torch.cuda.current_stream()
+    n, seed = 121, 5
+    n_sirt, n_tvm = args.prec_sirt, args.prec_tvm
+    forms = (("fp32", _abi.PREC_FP32), ("bf16", _abi.PREC_BF16), ("fp16", _abi.PREC_FP16))
+    out = {"schedule": f"{n_sirt} SIRT + {n_tvm} TVM iterations (TV: theta 25, g 1, dt 0.01, 5 inner steps)"}
+    # --- FP64 check on the scaled volume: inputs, then the oracle on a host thread ---
+    cW, cH, cD = args.prec_check
+    t0 = time.time()
+    cser, ceul = _config4_series(lib, cW, cH, cD, n, 4321, stream)
+    ref64 = {}
+    threads = os.cpu_count() or 1
+
+    def oracle_job():
+        t = time.time()
+        ref64["sirt"], ref64["final"] = _fp64_reference(cser, ceul, cW, cH, cD, n_sirt, n_tvm, seed, threads)
+        ref64["seconds"] = time.time() - t
+
+    th = threading.Thread(target=oracle_job, daemon=True)
+    th.start()
+    check = {}
+    for name, prec in forms:
+        fig, a, f = _schedule(lib, cW, cH, cD, cser, ceul, prec, n_sirt, n_tvm, seed, stream)
+        check[name] = (a.cpu().numpy().astype(np.float64), f.cpu().numpy().astype(np.float64))
+        del a, f
+    # --- full size ---
+    W, H, D = args.prec_size
+    series, eul = _config4_series(lib, W, H, D, n, 1238, stream)
     log(f"[bench] precision inputs ready in {time.time() - t0:.1f}s")
-    nvox = W * H * D
-    iters = args.prec_iters
-    out, vols = {}, {}
-    for name, prec in (("fp32", _abi.PREC_FP32), ("bf16", _abi.PREC_BF16), ("fp16", _abi.PREC_FP16)):
-        h = create(prec)
-        try:
-            _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
-            _abi.check(lib.tomo_run_ossart(h, 1, 1.0, 0, 5, 0, H, 1, None))  # warm-up (graph, tables)
-            _abi.check(lib.tomo_fill_volume(h, 0.0))
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            _abi.check(lib.tomo_run_ossart(h, iters, 1.0, 0, 5, 0, H, 1, None))
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            ms = ev0.elapsed_time(ev1)
-            v = np.empty((D, H, W), np.float32)
-            _abi.check(lib.tomo_get_volume(h, v.ctypes.data, 0, 0, H))
-            vols[name] = v
-            out[name] = {"voxel_updates_per_s": nvox * n * iters / (ms / 1000.0), "ms_per_iteration": ms / iters,
-                         "volume_bytes": nvox * (4 if prec == _abi.PREC_FP32 else 2)}
-        finally:
-            lib.tomo_destroy(h)
-    ref = vols["fp32"].astype(np.float64)
-    den = float(np.linalg.norm(ref))
-    for name in ("bf16", "fp16"):
-        out[name]["rel_l2_vs_fp32"] = float(np.linalg.norm(vols[name] - ref) / den)
-        out[name]["speedup_vs_fp32"] = out[name]["voxel_updates_per_s"] / out["fp32"]["voxel_updates_per_s"]
-    out["workload"] = f"{W}x{H}x{D} phantom, {n} tilts of {W}x{H}, Poisson 50 e-/px, SIRT"
-    out["iterations"] = iters
+    ref_sirt = ref_final = None
+    for name, prec in forms:
+        fig, a, f = _schedule(lib, W, H, D, series, eul, prec, n_sirt, n_tvm, seed, stream)
+        if name == "fp32":
+            ref_sirt, ref_final = a, f
+        else:
+            fig["rel_l2_vs_fp32_after_sirt"] = _device_rel_l2(a, ref_sirt)
+            fig["rel_l2_vs_fp32"] = _device_rel_l2(f, ref_final)
+            fig["speedup_vs_fp32"] = fig["sirt_voxel_updates_per_s"] / out["fp32"]["sirt_voxel_updates_per_s"]
+            del a, f
+        out[name] = fig
+        torch.cuda.empty_cache()
+    del ref_sirt, ref_final
+    torch.cuda.empty_cache()
+    th.join()
+
+    def rel(x, y):
+        return float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+
+    for name, _ in forms:
+        a, f = check[name]
+        out[name]["rel_l2_vs_fp64_after_sirt"] = rel(a, ref64["sirt"])
+        out[name]["rel_l2_vs_fp64"] = rel(f, ref64["final"])
+        out[name]["meets_1e-3_vs_fp64"] = out[name]["rel_l2_vs_fp64"] <= 1e-3
+    out["workload"] = f"{W}x{H}x{D} phantom, {n} tilts of {W}x{H} at -60..60 deg (1 deg), Poisson 50 e-/px"
+    out["fp64_check"] = {"volume": f"{cW}x{cH}x{cD}", "tilts": n, "oracle": "oracle/oracle64 (FP64), whole volume",
+                         "cpu_threads": threads, "oracle_seconds": ref64.get("seconds")}
     return out
 
 
@@ -798,7 +912,10 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--prec-size", type=int, nargs=3, default=[2048, 512, 2048], metavar=("W", "H", "D"),
                     help="volume of the reduced-precision leg")
-    ap.add_argument("--prec-iters", type=int, default=3)
+    ap.add_argument("--prec-check", type=int, nargs=3, default=[384, 32, 384], metavar=("W", "H", "D"),
+                    help="volume on which the reduced-precision schedule is checked against the FP64 oracle")
+    ap.add_argument("--prec-sirt", type=int, default=50)
+    ap.add_argument("--prec-tvm", type=int, default=20)
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -93,7 +93,10 @@ const char* tomo_last_error(void);
 tomo_status tomo_set_memory_limit(uint64_t bytes);
 uint64_t tomo_memory_in_use(void);
 /* Free and total bytes of the current device (ProjectorGPU.computeMaximumSizeForVolume
- * sizes a volume from them, ProjectorGPU.java:162-166). */
+ * sizes a volume from them, ProjectorGPU.java:162-166).  Free counts the idle blocks of
+ * the engine's device memory pool: handle buffers are carved from one stream-ordered pool
+ * per device that keeps what destroyed handles return, so that retiring a handle does not
+ * wait for the whole device. */
 tomo_status tomo_device_memory(uint64_t* free_bytes, uint64_t* total_bytes);
 /* Number of kernels this library launched since load (all handles). */
 uint64_t tomo_kernel_launches(void);
@@ -268,6 +271,17 @@ tomo_status tomo_set_tilts_per_cta(tomo_projector* p, int32_t n);
  * tilt axis and whole-row centre offsets; otherwise one row).  Results are bitwise the
  * same either way. */
 tomo_status tomo_set_bp_rows(tomo_projector* p, int32_t rows);
+/* Autotuner (no counterpart in the reference): times the forward projection with
+ * difference and the backprojection of one update of `update` tilts (0: all) of the
+ * loaded series under each candidate kernel shape -- forward-projection tilts per CTA
+ * (automatic grouping, the register maximum and 3/4, 1/2, 1/4 of it) and backprojection
+ * rows per thread (1, 2) -- with CUDA events over `reps` launches each (0: 3), and keeps
+ * the fastest on the handle (tomo_set_tilts_per_cta / tomo_set_bp_rows; batches use each
+ * member's choice).  The added projections are cleared; the volume is saved and put back.
+ * Every candidate computes the same values, up to the FP32 summation order where a tilt
+ * grouping changes the depth split of a small grid.  out4 (may be NULL): {tilts per CTA
+ * (0 = automatic), rows per thread, forward ms, backprojection ms} of the choice. */
+tomo_status tomo_autotune(tomo_projector* p, int32_t update, int32_t reps, double* out4);
 /* Failure-path test hook (no counterpart in the reference): while enabled, the
  * forward projector of this handle does not issue the bulk copies of each CTA's
  * first plane chunk, so that chunk's bounded mbarrier wait runs out, the CTA

@@ -115,6 +115,7 @@ SIGNATURES = {
     "tomo_profile_read": (C.c_int32, [_P, _f64p]),
     "tomo_set_tilts_per_cta": (C.c_int32, [_P, C.c_int32]),
     "tomo_set_bp_rows": (C.c_int32, [_P, C.c_int32]),
+    "tomo_autotune": (C.c_int32, [_P, C.c_int32, C.c_int32, _f64p]),
     "tomo_debug_hold_first_copy": (C.c_int32, [_P, C.c_int32]),
     "tomo_batch_create": (C.c_int32, [C.POINTER(C.c_void_p)]),
     "tomo_batch_destroy": (C.c_int32, [C.c_void_p]),

@@ -43,6 +43,7 @@ struct tomo_batch {
         int s;
         bool sanitize, pos;
         int vt;
+        bool pairs;
         int off, n;
     };
     struct RedSeg {
@@ -107,7 +108,7 @@ tomo_status build_plan(tomo_batch* b) {
     // work items grouped by (s, qp, zc, pair kind) for FP and (s, sanitize, pos, storage type) for BP
     std::map<std::tuple<int, int, int, int, int>, std::vector<int4>> fpi;
     std::map<std::tuple<int, int, int, int, int>, size_t> fpsmem;
-    std::map<std::tuple<int, int, int, int>, std::vector<int4>> bpi;
+    std::map<std::tuple<int, int, int, int, int>, std::vector<int4>> bpi;
     std::map<int, std::vector<ErrReduce>> reds;
     b->max_nsub = 0;
     b->has_fista = false;
@@ -190,8 +191,9 @@ tomo_status build_plan(tomo_batch* b) {
             c.status = p->d_status;
             const int bi = (int)bp.size();
             bp.push_back(c);
-            auto& bitems = bpi[std::make_tuple(s, c.sanitize, c.positivity, c.vtype)];
-            const bool pairs = bp_row_pairs(c.vtype, c.sanitize != 0, c.positivity != 0);
+            // row pairs unless the member's tuning asks for one row per thread
+            const bool pairs = bp_row_pairs(c.vtype, c.sanitize != 0, c.positivity != 0) && p->bp_rows != 1;
+            auto& bitems = bpi[std::make_tuple(s, c.sanitize, c.positivity, c.vtype, pairs ? 1 : 0)];
             const int rstep = pairs ? 2 : 1, tzr = pairs ? bp_pair_tile_z(c.vtype) : tz;
             for (int r = 0; r < g.H; r += rstep) {
                 bool reached = false;  // a row of the item sees a projection row
@@ -219,7 +221,8 @@ tomo_status build_plan(tomo_batch* b) {
     }
     for (auto& kv : bpi) {
         tomo_batch::BpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first) != 0, std::get<2>(kv.first) != 0,
-                             std::get<3>(kv.first), (int)bp_all.size(), (int)kv.second.size()};
+                             std::get<3>(kv.first), std::get<4>(kv.first) != 0, (int)bp_all.size(),
+                             (int)kv.second.size()};
         bp_all.insert(bp_all.end(), kv.second.begin(), kv.second.end());
         b->bp_segs.push_back(sg);
     }
@@ -260,7 +263,8 @@ tomo_status launch_step(tomo_batch* b) {
         for (tomo_projector* p : b->members) BCKS(handle_bp_pre(p, b->stream));
         for (auto& sg : b->bp_segs)
             if (sg.s == s)
-                BCK(launch_bp_batch(sg.sanitize, sg.pos, sg.vt, b->d_bp, b->d_bp_items + sg.off, sg.n, b->stream));
+                BCK(launch_bp_batch(sg.sanitize, sg.pos, sg.vt, sg.pairs, b->d_bp, b->d_bp_items + sg.off, sg.n,
+                                    b->stream));
         for (tomo_projector* p : b->members) BCKS(handle_bp_post(p, b->stream));
     }
     for (tomo_projector* p : b->members) BCKS(handle_end_iteration(p));

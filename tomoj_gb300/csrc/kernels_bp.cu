@@ -756,10 +756,11 @@ cudaError_t bp_init_attributes() {
     return bp2_attr_one<false, false, kVolF16>();
 }
 
-cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpLaunch* descs, const int4* items,
-                            int n_items, cudaStream_t s) {
+cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, bool pairs, const BpLaunch* descs,
+                            const int4* items, int n_items, cudaStream_t s) {
     if (n_items <= 0) return cudaSuccess;
-    if (bp_row_pairs(vtype, sanitize, positivity)) {
+    if (pairs) {
+        if (!bp_row_pairs(vtype, sanitize, positivity)) return cudaErrorInvalidValue;
         if (vtype == kVolF32) bp2_batch_vt<kVolF32>(sanitize, positivity, descs, items, n_items, s);
         else if (vtype == kVolBF16) bp2_batch_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, s);
         else if (vtype == kVolF16) bp2_batch_vt<kVolF16>(sanitize, positivity, descs, items, n_items, s);

@@ -51,18 +51,85 @@ void tomo::set_last_error(const char* msg) { g_err = msg; }
 
 namespace {
 
+// Handle buffers come from one stream-ordered memory pool per device that keeps the blocks
+// it gets back (release threshold unlimited).  Destroying a handle returns its buffers with
+// cudaFreeAsync, which does not wait for the whole device as cudaFree does (a server that
+// retires a request would otherwise stall every other request's kernels), and the next
+// handle's buffers are carved from those blocks.  Admission counts the pool's idle blocks
+// as free HBM.  Allocations are made on a private stream and completed before use.
+struct DevicePool {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t stream = nullptr;
+    bool tried = false;
+};
+std::mutex g_pool_mu;
+DevicePool g_pools[64];
+
+DevicePool* device_pool() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    DevicePool& d = g_pools[dev];
+    if (!d.tried) {
+        d.tried = true;
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        if (cudaMemPoolCreate(&d.pool, &props) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            if (d.pool) cudaMemPoolDestroy(d.pool);
+            d.pool = nullptr;
+        } else {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(d.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
+    return d.pool ? &d : nullptr;
+}
+
+size_t pool_idle_bytes(const DevicePool* d) {
+    if (!d) return 0;
+    uint64_t reserved = 0, used = 0;
+    cudaMemPoolGetAttribute(d->pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+    cudaMemPoolGetAttribute(d->pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    return reserved > used ? (size_t)(reserved - used) : 0;
+}
+
+// Returns a buffer; `stream` orders the release after the work queued there.
+void dfree(void* ptr, cudaStream_t stream) {
+    if (!ptr) return;
+    DevicePool* d = device_pool();
+    if (d) {
+        if (cudaFreeAsync(ptr, stream) != cudaSuccess) cudaGetLastError();
+    } else {
+        cudaFree(ptr);
+    }
+}
+
 tomo_status dalloc(tomo_projector* p, void** ptr, size_t bytes) {
     if (bytes == 0) bytes = 16;
     const uint64_t lim = g_limit.load();
     if (lim != 0 && g_in_use.load() + bytes > lim)
         return fail(TOMO_ERR_NOMEM, "admission: " + std::to_string(bytes) + " bytes exceed the memory limit");
+    DevicePool* d = device_pool();
     size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes > free_b)
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes > free_b + pool_idle_bytes(d))
         return fail(TOMO_ERR_NOMEM, "admission: " + std::to_string(bytes) + " bytes exceed free HBM");
-    cudaError_t e = cudaMalloc(ptr, bytes);
+    cudaError_t e;
+    if (d) {
+        e = cudaMallocFromPoolAsync(ptr, bytes, d->pool, d->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+    } else {
+        e = cudaMalloc(ptr, bytes);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return fail(TOMO_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return fail(TOMO_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
     }
     p->allocs.push_back(*ptr);
     p->bytes += bytes;
@@ -79,7 +146,7 @@ tomo_status alloc_n(tomo_projector* p, T** ptr, size_t n) {
 template <class T>
 void free_n(tomo_projector* p, T** ptr, size_t n) {
     if (!*ptr) return;
-    cudaFree(*ptr);
+    dfree(*ptr, p->stream);  // after the handle's queued work that may still read it
     for (auto& a : p->allocs)
         if (a == (void*)*ptr) a = nullptr;
     g_in_use -= n * sizeof(T);
@@ -507,7 +574,7 @@ tomo_status tomo_device_memory(uint64_t* free_bytes, uint64_t* total_bytes) {
     if (!free_bytes || !total_bytes) return fail(TOMO_ERR_INVALID, "null argument");
     size_t f = 0, t = 0;
     CK(cudaMemGetInfo(&f, &t));
-    *free_bytes = f;
+    *free_bytes = f + pool_idle_bytes(device_pool());  // idle blocks of the handles' pool are free to handles
     *total_bytes = t;
     return TOMO_OK;
 }
@@ -649,7 +716,11 @@ tomo_status tomo_destroy(tomo_projector* p) {
         v.erase(std::remove(v.begin(), v.end(), p), v.end());
     }
     for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
-    for (void* a : p->allocs) cudaFree(a);
+    {
+        // the handle's stream is drained above; its row-stream work joins that stream
+        DevicePool* d = device_pool();
+        for (void* a : p->allocs) dfree(a, d ? d->stream : nullptr);
+    }
     g_in_use -= p->bytes;
     for (cudaEvent_t e : p->rs_ev) cudaEventDestroy(e);
     for (cudaStream_t q : p->rs)
@@ -1394,6 +1465,101 @@ tomo_status tomo_profile_read(tomo_projector* p, double* out4) {
 tomo_status tomo_set_bp_rows(tomo_projector* p, int32_t rows) {
     if (!p || rows < 0 || rows > 2) return fail(TOMO_ERR_INVALID, "rows per backprojection thread: 0, 1 or 2");
     p->bp_rows = rows;
+    return TOMO_OK;
+}
+
+// Autotuner: candidate kernel shapes timed on one update of this handle's series.
+tomo_status tomo_autotune(tomo_projector* p, int32_t update, int32_t reps, double* out4) {
+    if (!p || reps < 0) return fail(TOMO_ERR_INVALID, "bad argument");
+    CKS(need_series(p));
+    const Geometry& g = p->g;
+    const bool tunable = g.separable && !p->bp_generic;
+    const int T = (update <= 0 || update > g.N) ? g.N : update;
+    if (reps == 0) reps = 3;
+    double best_fp = 0, best_bp = 0;
+    if (tunable) {
+        // the trials use the projection slots and overwrite the volume: clear the added
+        // projections, keep a copy of the volume (and slab scales) and put it back afterwards
+        CKS(tomo_clear_projections(p));
+        const size_t vbytes = p->nvox * (p->vtype == kVolF32 ? sizeof(float) : sizeof(uint16_t));
+        unsigned char* save = nullptr;
+        float* save_sc = nullptr;
+        CKS(alloc_n(p, &save, vbytes));
+        if (p->vtype != kVolF32 && alloc_n(p, &save_sc, (size_t)g.H) != TOMO_OK) {
+            free_n(p, &save, vbytes);
+            return TOMO_ERR_NOMEM;
+        }
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        tomo_status st = TOMO_OK;
+        auto ck = [&](cudaError_t e) {
+            if (e != cudaSuccess && st == TOMO_OK) st = fail(TOMO_ERR_CUDA, cudaGetErrorString(e));
+        };
+        ck(cudaMemcpyAsync(save, p->vol(), vbytes, cudaMemcpyDeviceToDevice, p->stream));
+        if (save_sc) ck(cudaMemcpyAsync(save_sc, p->d_vscale, sizeof(float) * g.H, cudaMemcpyDeviceToDevice, p->stream));
+        ck(cudaEventCreate(&e0));
+        ck(cudaEventCreate(&e1));
+        for (int i = 0; i < T; i++) p->batch.push_back(i);
+        if (st == TOMO_OK) st = upload_batch(p);
+        const double factor = 1.0 / T;
+        // time `reps` launches of fn after one untimed one
+        auto timed = [&](const std::function<tomo_status()>& fn) -> double {
+            if (st != TOMO_OK) return 0;
+            if ((st = fn()) != TOMO_OK) return 0;
+            ck(cudaEventRecord(e0, p->stream));
+            for (int r = 0; r < reps && st == TOMO_OK; r++) st = fn();
+            ck(cudaEventRecord(e1, p->stream));
+            ck(cudaEventSynchronize(e1));
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, e0, e1));
+            return st == TOMO_OK ? ms / reps : 0;
+        };
+        // forward projection: tilts per CTA (0 = the balanced automatic grouping)
+        const int tgmax = fp_max_tilts_per_cta(g.w);
+        std::vector<int> cands = {0, tgmax, (3 * tgmax + 3) / 4, (tgmax + 1) / 2, (tgmax + 3) / 4};
+        std::sort(cands.begin() + 1, cands.end());
+        cands.erase(std::unique(cands.begin() + 1, cands.end()), cands.end());
+        int best_c = 0;
+        best_fp = 1e30;
+        for (int c : cands) {
+            if (c > T) continue;
+            p->tilts_per_cta = c;
+            const double ms = timed([&] { return run_fp(p, p->d_batch, T, 0, true, factor, 0); });
+            if (st == TOMO_OK && ms < best_fp) {
+                best_fp = ms;
+                best_c = c;
+            }
+        }
+        p->tilts_per_cta = best_c;
+        // backprojection of the differences: volume rows per thread
+        std::vector<int> rows = {0};
+        if (p->vtype == kVolF32 && !g.fractional && !p->bp_wide) rows = {1, 2};
+        int best_r = 0;
+        best_bp = 1e30;
+        for (int r : rows) {
+            p->bp_rows = r;
+            const double ms = timed([&] { return run_bp(p, p->d_diff, p->d_batch, T, 0, g.H, false, false); });
+            if (st == TOMO_OK && ms < best_bp) {
+                best_bp = ms;
+                best_r = r;
+            }
+        }
+        p->bp_rows = best_r;
+        ck(cudaMemcpyAsync(p->vol(), save, vbytes, cudaMemcpyDeviceToDevice, p->stream));
+        if (save_sc) ck(cudaMemcpyAsync(p->d_vscale, save_sc, sizeof(float) * g.H, cudaMemcpyDeviceToDevice, p->stream));
+        ck(cudaStreamSynchronize(p->stream));
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        free_n(p, &save, vbytes);
+        free_n(p, &save_sc, (size_t)g.H);
+        tomo_clear_projections(p);
+        if (st != TOMO_OK) return st;
+    }
+    if (out4) {
+        out4[0] = p->tilts_per_cta;
+        out4[1] = p->bp_rows;
+        out4[2] = best_fp;
+        out4[3] = best_bp;
+    }
     return TOMO_OK;
 }
 

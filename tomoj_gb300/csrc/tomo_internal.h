@@ -213,9 +213,10 @@ struct BpLaunch {
     int rows_mode;          // volume rows per thread: 0 by size and type, 1 one, 2 two (where allowed)
 };
 cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
-// Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row}.
-cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, const BpLaunch* descs, const int4* items,
-                            int n_items, cudaStream_t s);
+// Batched backprojection: CTA b runs items[b] = {descriptor, x tile, z tile, row} (with `pairs`, the
+// first row of a pair of rows; z tiles of bp_pair_tile_z()).
+cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, bool pairs, const BpLaunch* descs,
+                            const int4* items, int n_items, cudaStream_t s);
 int bp_tile_x();
 int bp_tile_z();
 // Whole-row backprojections of this kind run two volume rows per CTA (batch items then
