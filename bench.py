@@ -48,6 +48,13 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def want(args, leg):
+    """Whether the extra leg `leg` runs (not --no-extra, and named by --legs or --legs all)."""
+    if args.no_extra:
+        return False
+    return args.legs == "all" or leg in args.legs.split(",")
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -364,7 +371,7 @@ def run_engine(args, wl):
     # option: the forward projection of one row range overlaps the backprojection of
     # the other; bitwise the same volume) ----
     row_leg = None
-    if not args.no_extra:
+    if want(args, "row_streams"):
         _abi.check(lib.tomo_set_row_streams(h, 2))
         for _ in range(2):
             step()
@@ -384,7 +391,7 @@ def run_engine(args, wl):
     # ---- the compressed-sensing end-of-iteration filter on the same volume (FP64 wavelet
     # transform, threshold search, soft threshold, inverse; default levels from the width) ----
     cs_leg = None
-    if not args.no_extra:
+    if want(args, "compressed_sensing"):
         _abi.check(lib.tomo_set_compressed_sensing(h, 3, 3.0, 0.0, 0.95, None, 1))
         _abi.check(lib.tomo_end_iteration(h))
         ca, cb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -480,10 +487,10 @@ def run_engine(args, wl):
                          f"{dt:.1f} s"}
 
     lib.tomo_destroy(h)
-    config1 = None if (args.no_extra or args.no_cpu or rank != 0 or world != 1) else run_config1_leg(lib, args)
-    batched = None if args.no_extra else run_batched_leg(lib, args)
-    serving = None if args.no_extra else run_serving_leg(args)
-    precision = None if args.no_extra else run_precision_leg(lib, args)
+    config1 = None if (not want(args, "config1") or args.no_cpu or rank != 0 or world != 1) else run_config1_leg(lib, args)
+    batched = run_batched_leg(lib, args) if want(args, "batched") else None
+    serving = run_serving_leg(args) if want(args, "serving") else None
+    precision = run_precision_leg(lib, args) if want(args, "precision") else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
@@ -502,14 +509,46 @@ def run_engine(args, wl):
         torch.distributed.destroy_process_group()
 
 
+def _project_series(lib, vol, W, H, D, eul, stream):
+    """FP32 forward projection by the engine of a (D, H, W) device phantom at the given
+    Euler matrices: the ideal tilt-series (n, H, W) float32 on the host."""
+    from tomoj_gb300 import _abi
+    n = eul.shape[0]
+    g = _abi.make_geom(W, H, D, W, H, n)
+    prm = _abi.make_params(fill=_abi.FILL_NAN)
+    h = C.c_void_p()
+    _abi.check(lib.tomo_create(C.byref(g), C.byref(prm), C.byref(h)))
+    series = np.zeros((n, H, W), np.float32)
+    try:
+        _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+        stream.synchronize()
+        _abi.check(lib.tomo_set_volume(h, C.c_void_p(vol.data_ptr()), 1, 0, H))
+        for i in range(n):
+            _abi.check(lib.tomo_add_projection(h, i))
+        _abi.check(lib.tomo_project(h, 0, H))
+        for i in range(n):
+            _abi.check(lib.tomo_get_projection(h, i, _abi.ptr(series[i])))
+    finally:
+        lib.tomo_destroy(h)
+    return np.nan_to_num(series)
+
+
 def run_batched_leg(lib, args):
-    """BASELINE config 3, bounded: 64 independent series (W in {256,384,512,768,1024}, H 64,
-    D in [64,256], 41/61/81/121 tilts over +/-50..70 deg in uniform, Saxton or dose-symmetric
-    order), SIRT iterations in one batched launch sequence per iteration (graph), against the
-    same handles run one by one."""
+    """BASELINE config 3: 64 independent series (W in {256,384,512,768,1024}, H 64, D in
+    [64,256], 41/61/81/121 tilts over +/-50..70 deg in uniform, Saxton or dose-symmetric
+    order), each the engine's projection of its own seeded ellipsoid phantom; 30 SIRT
+    iterations.  Every member's kernel shapes come from the autotuner (tomo_autotune).
+    Timed with CUDA events on one stream: the 64 handles one by one, the batch (one launch
+    per kernel variant, the iteration a CUDA graph), the same batch in persistent form (one
+    forward launch per CTA size and one backprojection launch per iteration), and the batch
+    with FP16 volume storage."""
+    import torch
+    from tomoj_gb300 import _abi
     from tomoj_gb300 import phantom as P
+    stream = torch.cuda.current_stream()
     g = np.random.Generator(np.random.PCG64(3))
-    handles, Ns, ups = [], [], 0
+    specs = []
     for m in range(64):
         W = int(g.choice([256, 384, 512, 768, 1024]))
         H, D, n = 64, int(g.integers(64, 257)), int(g.choice([41, 61, 81, 121]))
@@ -517,101 +556,208 @@ def run_batched_leg(lib, args):
         scheme = int(g.integers(0, 3))
         angles = (np.linspace(-amax, amax, n) if scheme == 0 else
                   P.saxton_tilts(amax, n) if scheme == 1 else P.dose_symmetric_tilts(amax, n))
-        eul = euler_y(angles)
-        geo = _abi_mod().make_geom(W, H, D, W, H, n)
-        prm = _abi_mod().make_params()
-        h = C.c_void_p()
-        _abi_mod().check(lib.tomo_create(C.byref(geo), C.byref(prm), C.byref(h)))
-        yy, xx = np.mgrid[0:H, 0:W].astype(np.float32)
-        base = np.exp(-((xx - W / 2) ** 2) / (2 * (0.2 * W) ** 2)).astype(np.float32) * np.float32(0.3 * D)
-        ser = np.ascontiguousarray(np.broadcast_to(base, (n, H, W)), np.float32)
-        _abi_mod().check(lib.tomo_load_series(h, ser.ctypes.data, 0, _abi_mod().ptr(eul, C.c_double), None, None))
-        handles.append(h)
-        Ns.append(n)
-        ups += W * H * D * n
+        specs.append((W, H, D, n, euler_y(angles), 1000 + m))
+    t_in = time.time()
+    series = []
+    for W, H, D, n, eul, seed in specs:
+        vol = phantom_on_device(W, H, D, P.n_ellipsoids_for(W, H, D), seed, "cuda")
+        series.append(_project_series(lib, vol, W, H, D, eul, stream))
+        del vol
+    torch.cuda.empty_cache()
+    ups = sum(W * H * D * n for W, H, D, n, _, _ in specs)
     n_iter = 30
-    import torch
-    torch.cuda.synchronize()
-    for h in handles[:2]:
-        _abi_mod().check(lib.tomo_run_ossart(h, 1, 1.0, 0, 1, 0, 64, 1, None))
-    t0 = time.perf_counter()
-    for h in handles:
-        _abi_mod().check(lib.tomo_run_ossart(h, n_iter, 1.0, 0, 1, 0, 64, 1, None))
-    one = ups * n_iter / (time.perf_counter() - t0)
-    b = C.c_void_p()
-    _abi_mod().check(lib.tomo_batch_create(C.byref(b)))
-    arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
-    _abi_mod().check(lib.tomo_batch_set(b, arr, len(handles)))
-    rel = np.ones(len(handles))
-    upd = np.zeros(len(handles), np.int32)
+    sp = C.c_void_p(stream.cuda_stream)
 
-    def it(k):
-        first = np.array([lib.tomo_first_index(1, k, n) for n in Ns], np.int32)
-        _abi_mod().check(lib.tomo_batch_iteration(b, _abi_mod().ptr(rel, C.c_double), _abi_mod().ptr(upd, C.c_int32),
-                                                  _abi_mod().ptr(first, C.c_int32), 1, None))
-    it(0)
-    t0 = time.perf_counter()
-    for k in range(n_iter):
-        it(k)
-    bat = ups * n_iter / (time.perf_counter() - t0)
-    lib.tomo_batch_destroy(b)
-    # the same series as two batches (alternate members) iterated from two host threads:
-    # each batch has its own stream, so one batch's forward projections can run beside
-    # the other's backprojections
-    from concurrent.futures import ThreadPoolExecutor
-    halves = []
-    for part in (0, 1):
-        hb = C.c_void_p()
-        _abi_mod().check(lib.tomo_batch_create(C.byref(hb)))
-        mem = handles[part::2]
-        arr2 = (C.c_void_p * len(mem))(*[h.value for h in mem])
-        _abi_mod().check(lib.tomo_batch_set(hb, arr2, len(mem)))
-        halves.append((hb, Ns[part::2], len(mem)))
+    def make(prec):
+        hs = []
+        for (W, H, D, n, eul, _), ser in zip(specs, series):
+            geo = _abi.make_geom(W, H, D, W, H, n)
+            prm = _abi.make_params(precision=prec)
+            h = C.c_void_p()
+            _abi.check(lib.tomo_create(C.byref(geo), C.byref(prm), C.byref(h)))
+            _abi.check(lib.tomo_load_series(h, ser.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+            hs.append(h)
+        return hs
 
-    def run_half(hv, iters):
-        hb, ns, m = hv
-        r = np.ones(m)
-        u = np.zeros(m, np.int32)
-        for k in iters:
-            first = np.array([lib.tomo_first_index(1, k, n) for n in ns], np.int32)
-            _abi_mod().check(lib.tomo_batch_iteration(hb, _abi_mod().ptr(r, C.c_double), _abi_mod().ptr(u, C.c_int32),
-                                                      _abi_mod().ptr(first, C.c_int32), 1, None))
+    def tune(hs):
+        shapes = {}
+        t0 = time.time()
+        for h in hs:
+            out = np.zeros(4)
+            _abi.check(lib.tomo_autotune(h, 0, 2, _abi.ptr(out, C.c_double)))
+            key = f"tilts_per_cta={int(out[0]) or 'auto'},bp_rows={int(out[1]) or 'auto'}"
+            shapes[key] = shapes.get(key, 0) + 1
+        return shapes, time.time() - t0
 
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        list(ex.map(lambda hv: run_half(hv, [0]), halves))
-        t0 = time.perf_counter()
-        list(ex.map(lambda hv: run_half(hv, range(n_iter)), halves))
-        two = ups * n_iter / (time.perf_counter() - t0)
-    for hb, _, _ in halves:
-        lib.tomo_batch_destroy(hb)
-    for h in handles:
-        lib.tomo_destroy(h)
-    return {"workload": "64 heterogeneous series, SIRT, FP32", "iterations": n_iter,
-            "updates_per_iteration": ups, "voxel_updates_per_s": bat, "one_by_one_voxel_updates_per_s": one,
-            "speedup_vs_one_by_one": bat / one, "two_batches_voxel_updates_per_s": two,
-            "two_batches_speedup_vs_one_by_one": two / one}
+    def timed(fn):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        ev0.record(stream)
+        k0 = lib.tomo_kernel_launches()
+        fn()
+        ev1.record(stream)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / 1000.0, lib.tomo_kernel_launches() - k0
+
+    def batch_of(hs, persistent):
+        b = C.c_void_p()
+        _abi.check(lib.tomo_batch_create(C.byref(b)))
+        _abi.check(lib.tomo_batch_set_stream(b, sp))
+        _abi.check(lib.tomo_batch_set_persistent(b, persistent))
+        arr = (C.c_void_p * len(hs))(*[h.value for h in hs])
+        _abi.check(lib.tomo_batch_set(b, arr, len(hs)))
+        return b
+
+    rel = np.ones(64)
+    upd = np.zeros(64, np.int32)
+
+    def iterate(b, ks):
+        for k in ks:
+            first = np.array([lib.tomo_first_index(1, k, sp_[3]) for sp_ in specs], np.int32)
+            _abi.check(lib.tomo_batch_iteration(b, _abi.ptr(rel, C.c_double), _abi.ptr(upd, C.c_int32),
+                                                _abi.ptr(first, C.c_int32), 1, None))
+
+    out = {"workload": "64 heterogeneous series (seeded ellipsoid phantoms), SIRT, 30 iterations",
+           "iterations": n_iter, "updates_per_iteration": ups}
+    hs = make(_abi.PREC_FP32)
+    try:
+        shapes, tune_s = tune(hs)
+        out["autotuned_shapes"] = shapes
+        out["autotune_s"] = tune_s
+        for h in hs:
+            _abi.check(lib.tomo_set_stream(h, sp))
+        for h in hs[:2]:
+            _abi.check(lib.tomo_run_ossart(h, 1, 1.0, 0, 1, 0, 64, 1, None))
+        for h in hs:
+            _abi.check(lib.tomo_fill_volume(h, 0.0))
+        sec, _ = timed(lambda: [_abi.check(lib.tomo_run_ossart(h, n_iter, 1.0, 0, 1, 0, 64, 1, None)) for h in hs])
+        out["one_by_one_voxel_updates_per_s"] = ups * n_iter / sec
+        for h in hs:
+            _abi.check(lib.tomo_set_stream(h, None))
+        for persistent, key in ((0, "per_variant"), (1, "persistent")):
+            for h in hs:
+                _abi.check(lib.tomo_fill_volume(h, 0.0))
+            b = batch_of(hs, persistent)
+            try:
+                iterate(b, [0])  # plan, graph
+                sec, launches = timed(lambda: iterate(b, range(n_iter)))
+            finally:
+                lib.tomo_batch_destroy(b)
+            out[key] = {"voxel_updates_per_s": ups * n_iter / sec, "launches_per_iteration": launches / n_iter}
+    finally:
+        for h in hs:
+            lib.tomo_destroy(h)
+    hs = make(_abi.PREC_FP16)
+    try:
+        tune(hs)
+        b = batch_of(hs, 0)
+        try:
+            iterate(b, [0])
+            for h in hs:
+                _abi.check(lib.tomo_fill_volume(h, 0.0))
+            sec, launches = timed(lambda: iterate(b, range(n_iter)))
+        finally:
+            lib.tomo_batch_destroy(b)
+        out["fp16"] = {"voxel_updates_per_s": ups * n_iter / sec, "launches_per_iteration": launches / n_iter}
+    finally:
+        for h in hs:
+            lib.tomo_destroy(h)
+    one = out["one_by_one_voxel_updates_per_s"]
+    out["voxel_updates_per_s"] = out["per_variant"]["voxel_updates_per_s"]
+    out["speedup_vs_one_by_one"] = out["per_variant"]["voxel_updates_per_s"] / one
+    out["persistent_speedup_vs_one_by_one"] = out["persistent"]["voxel_updates_per_s"] / one
+    out["fp16_speedup_vs_one_by_one"] = out["fp16"]["voxel_updates_per_s"] / one
+    out["inputs_s"] = time.time() - t_in
+    return out
+
+
+def _serving_costs(lib, precision):
+    """Per-unit GPU costs of each request kind for the serving replay, measured on one
+    1024 x 1024 x 256 request with 61 tilts in the leg's storage precision: seconds per
+    voxel-update of a SIRT, OS-SART (update ceil(61/10)) and WBP pass, and seconds per voxel
+    of a TV-denoise step (TVM iteration minus SIRT iteration)."""
+    from tomoj_gb300.serving import OSSART, SIRT, TVM, WBP, CostModel, EngineAdapter, synthetic_requests
+    eng = EngineAdapter(lanes=1)
+    base = synthetic_requests(1, seed=7, sizes=(1024,), thick=(256,), tilts=(61,), precision=precision)[0]
+    ups = base.updates_per_iteration()
+    out = {}
+    try:
+        for kind, n_it in ((WBP, 1), (SIRT, 4), (OSSART, 4), (TVM, 4)):
+            base.kind = kind
+            hd = eng.create(base)
+            try:
+                upd = 7 if kind == OSSART else 0
+                run = (lambda k: eng.run_wbp(hd, base)) if kind == WBP else \
+                    (lambda k: _abi_mod().check(lib.tomo_run_ossart(hd, k, 1.0, upd, 3, 0, base.H, 1, None)))
+                run(1)  # warm-up (tables, graph)
+                t0 = time.perf_counter()
+                run(n_it)
+                out[kind] = (time.perf_counter() - t0) / n_it
+            finally:
+                eng.destroy(hd)
+    finally:
+        eng.close()
+    nvox = base.W * base.H * base.D
+    return CostModel({SIRT: out[SIRT] / ups, OSSART: out[OSSART] / ups, WBP: out[WBP] / ups},
+                     tv_s_per_voxel=max(out[TVM] - out[SIRT], 0.0) / nvox)
 
 
 def run_serving_leg(args):
-    """BASELINE config 5, bounded to args.serve_requests requests: Poisson arrivals (4/s) of
-    series of {512,1024,2048}^2 x {128,256,512} with {41,61,121} tilts, WBP 30 % / SIRT 40 % /
-    OS-SART 20 % / TVM 10 %, 5-50 iterations; continuous batching with HBM admission."""
+    """BASELINE config 5: Poisson arrivals (4/s) of series of {512,1024,2048}^2 x {128,256,512}
+    with {41,61,121} tilts, WBP 30 % / SIRT 40 % / OS-SART 20 % / TVM 10 %, 5-50 iterations,
+    volumes stored in FP16; continuous batching in three lanes with HBM admission.  Served:
+    the first args.serve_requests requests of the seeded schedule (p50/p99 overall, per method
+    and per size, offered load).  Replayed in virtual time with per-unit costs measured here:
+    the same requests (against the served figures) and the whole 1000-request schedule.  The
+    p50 drift check serves one short schedule at the start and again at the end."""
     import torch
-    from tomoj_gb300.serving import EngineAdapter, Server, summarize, synthetic_requests
+    from tomoj_gb300 import _abi
+    from tomoj_gb300.serving import EngineAdapter, Server, simulate, summarize, synthetic_requests
+    prec = _abi.PREC_FP16
     # admission is by free HBM: hand back what earlier legs left in torch's allocator cache
     torch.cuda.empty_cache()
-    reqs = synthetic_requests(args.serve_requests, seed=42)
-    eng = EngineAdapter()
-    try:
-        t0 = time.perf_counter()
-        res = Server(eng, max_active=64).run(reqs)
-        wall = time.perf_counter() - t0
-    finally:
-        eng.close()
-    s = summarize(res)
-    s["wall_s"] = wall
-    s["unit"] = "seconds (time to reconstruction)"
-    return s
+    lib = _abi_mod().load()
+    cost = _serving_costs(lib, prec)
+
+    def serve(reqs):
+        eng = EngineAdapter(lanes=3)
+        try:
+            t0 = time.perf_counter()
+            res = Server(eng, max_active=64).run(reqs)
+            wall = time.perf_counter() - t0
+        finally:
+            eng.close()
+        s = summarize(res, requests=reqs)
+        s["wall_s"] = wall
+        return s
+
+    def short(s):
+        return {k: s[k] for k in ("requests", "p50_s", "p99_s", "mean_s", "voxel_updates_per_s")}
+
+    drift_reqs = synthetic_requests(24, seed=9, sizes=(512, 1024), precision=prec)
+    drift0 = serve(drift_reqs)
+    reqs = synthetic_requests(args.serve_requests, seed=42, precision=prec)
+    out = serve(reqs)
+    drift1 = serve(drift_reqs)
+    del reqs
+    sim_same = summarize(simulate(synthetic_requests(args.serve_requests, seed=42, precision=prec, with_series=False),
+                                  cost), requests=None)
+    full = synthetic_requests(1000, seed=42, precision=prec, with_series=False)
+    sim_full = summarize(simulate(full, cost), requests=full)
+    out["unit"] = "seconds (time to reconstruction)"
+    out["precision"] = "fp16"
+    out["lanes"] = "3 (iteration < 8e9, < 6e10, larger voxel-updates); WBP on a worker at top priority"
+    out["replay"] = {
+        "cost_model": {"s_per_update": cost.s_per_update, "tv_s_per_voxel": cost.tv_s_per_voxel,
+                       "measured_on": "1024x1024x256, 61 tilts, fp16"},
+        "same_requests": short(sim_same),
+        "schedule_1000": {k: sim_full[k] for k in ("requests", "p50_s", "p99_s", "mean_s", "makespan_s",
+                                                   "voxel_updates_per_s", "offered_load", "per_kind", "per_size")},
+    }
+    out["p50_drift_check"] = {"schedule": "24 requests of 512^2 / 1024^2 (seed 9), served before and after the "
+                                          "main leg in the same process",
+                              "before": short(drift0), "after": short(drift1)}
+    return out
 
 
 def run_config1_leg(lib, args):
@@ -909,7 +1055,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched, serving and precision legs")
-    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--legs", default="all",
+                    help="comma list of extra legs to run: row_streams, compressed_sensing, config1, batched, "
+                         "serving, precision (default all)")
+    ap.add_argument("--serve-requests", type=int, default=128)
     ap.add_argument("--prec-size", type=int, nargs=3, default=[2048, 512, 2048], metavar=("W", "H", "D"),
                     help="volume of the reduced-precision leg")
     ap.add_argument("--prec-check", type=int, nargs=3, default=[384, 32, 384], metavar=("W", "H", "D"),

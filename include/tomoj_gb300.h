@@ -108,6 +108,9 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
 tomo_status tomo_destroy(tomo_projector* p);
 /* cudaStream_t passed as void*; NULL returns to the handle's own stream. */
 tomo_status tomo_set_stream(tomo_projector* p, void* stream);
+/* Recreates the handle's own stream at a scheduling priority (no counterpart in the
+ * reference; same scale as tomo_batch_set_priority: 0 default, larger more urgent). */
+tomo_status tomo_set_priority(tomo_projector* p, int32_t priority);
 
 /* ---- data ---------------------------------------------------------------
  * Uploads the unaligned tilt-series and per-tilt geometry and builds the
@@ -249,6 +252,25 @@ tomo_status tomo_cancel(tomo_projector* p);
 typedef struct tomo_batch tomo_batch;
 tomo_status tomo_batch_create(tomo_batch** out);
 tomo_status tomo_batch_destroy(tomo_batch* b);
+/* Scheduling priority of the batch's stream (no counterpart in the reference): 0 is the
+ * device default, each step above asks for the next more urgent stream priority, clamped
+ * to the device's range.  As SMs free up, CTAs of a more urgent stream are dispatched
+ * first, so a batch of small series is not held behind the long launches of a batch of
+ * large ones. */
+tomo_status tomo_batch_set_priority(tomo_batch* b, int32_t priority);
+/* cudaStream_t passed as void* for the batch's work (NULL: the batch's own stream).
+ * Members' own streams must be idle at each iteration, as with the batch's own stream. */
+tomo_status tomo_batch_set_stream(tomo_batch* b, void* stream);
+/* Persistent launches (no counterpart in the reference; default off): each forward phase
+ * is one launch per CTA size (256 threads up to 512 detector columns, 512 above) and each
+ * backprojection phase one launch per storage type and rule set, of resident CTAs that
+ * take work items from a device list, longest first, through an atomic cursor.  Off: one
+ * launch per kernel variant with a CTA per item, which measured faster on GB300 (64
+ * heterogeneous series: 0.97 against 0.85-0.88 T voxel-updates/s).  Results are bitwise
+ * the same.  on: 0 off, 1 on; for tuning, a sum of 2 (forward phase persistent), 4
+ * (backprojection persistent), 8 (lists in plan order instead of longest first) and 16
+ * (launches of a phase one after another instead of side by side). */
+tomo_status tomo_batch_set_persistent(tomo_batch* b, int32_t on);
 /* Replaces the membership (n handles). */
 tomo_status tomo_batch_set(tomo_batch* b, tomo_projector* const* members, int32_t n);
 /* One OS-SART iteration of every member (osartIteration, TomoReconstruction2.java:636-733):

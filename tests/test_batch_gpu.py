@@ -67,3 +67,62 @@ def test_batch_iterations_equal_individual_runs(engine, use_graph):
         engine.tomo_batch_destroy(b)
         for hd in hds:
             hd.close()
+
+
+PERSIST_SPECS = [  # widths on both CTA sizes (256 threads: QP 1, 2; 512 threads: QP 2, 4), FP32 and FP16
+    (dict(W=200, H=5, D=24, n=11, seed=21), _abi.PREC_FP16, 4),
+    (dict(W=300, H=4, D=20, n=9, seed=22), _abi.PREC_FP32, 0),
+    (dict(W=700, H=4, D=16, n=7, seed=23), _abi.PREC_FP16, 3),
+    (dict(W=1100, H=3, D=12, n=5, seed=24), _abi.PREC_FP32, 0),
+]
+
+
+def _prec_handle(lib, c, prec):
+    g = _abi.make_geom(c["W"], c["H"], c["D"], c["w"], c["h"], c["n"])
+    p = _abi.make_params(precision=prec)
+    h = C.c_void_p()
+    _abi.check(lib.tomo_create(C.byref(g), C.byref(p), C.byref(h)))
+    eul = np.ascontiguousarray(c["eul"], np.float64)
+    series = np.ascontiguousarray(c["series"], np.float32)
+    _abi.check(lib.tomo_load_series(h, series.ctypes.data, 0, _abi.ptr(eul, C.c_double), None, None))
+    return h
+
+
+@pytest.mark.parametrize("use_graph", [0, 1])
+def test_persistent_launches_equal_per_variant_launches(engine, use_graph):
+    """The persistent form (one forward launch per CTA size, one backprojection launch per
+    storage type, items pulled from a list) computes bitwise what one launch per kernel
+    variant with a CTA per item computes, with fewer launches per iteration."""
+    cases = [(series_case(**s), prec, u) for s, prec, u in PERSIST_SPECS]
+    n_iter, seeds = 2, [5, 6, 7, 8]
+    vols, launches = {}, {}
+    for persistent in (0, 1):
+        hs = [_prec_handle(engine, c, prec) for c, prec, _ in cases]
+        b = C.c_void_p()
+        _abi.check(engine.tomo_batch_create(C.byref(b)))
+        try:
+            _abi.check(engine.tomo_batch_set_persistent(b, persistent))
+            arr = (C.c_void_p * len(hs))(*[h.value for h in hs])
+            _abi.check(engine.tomo_batch_set(b, arr, len(hs)))
+            rel = np.ones(len(hs))
+            upd = np.array([u for _, _, u in cases], np.int32)
+            for it in range(n_iter):
+                first = np.array([engine.tomo_first_index(sd, it, c["n"]) for sd, (c, _, _) in zip(seeds, cases)],
+                                 np.int32)
+                k0 = engine.tomo_kernel_launches()
+                _abi.check(engine.tomo_batch_iteration(b, _abi.ptr(rel, C.c_double), _abi.ptr(upd, C.c_int32),
+                                                       _abi.ptr(first, C.c_int32), use_graph, None))
+                launches[persistent] = engine.tomo_kernel_launches() - k0
+            vols[persistent] = []
+            for h, (c, _, _) in zip(hs, cases):
+                out = np.empty((c["D"], c["H"], c["W"]), np.float32)
+                _abi.check(engine.tomo_get_volume(h, out.ctypes.data, 0, 0, c["H"]))
+                vols[persistent].append(out)
+        finally:
+            engine.tomo_batch_destroy(b)
+            for h in hs:
+                engine.tomo_destroy(h)
+    for m in range(len(cases)):
+        assert np.array_equal(vols[0][m], vols[1][m]), m
+        assert np.isfinite(vols[1][m]).all() and np.abs(vols[1][m]).max() > 0, m
+    assert launches[1] < launches[0], launches

@@ -133,7 +133,7 @@ def test_serving_defers_a_request_until_memory_frees(engine, case):
     angles = case["angles"]
     reqs = [Request(k, 0.0, SIRT, np.ascontiguousarray(case["series"], np.float32), angles, case["W"], case["H"],
                     case["D"], n_iter, 0, 1.0, 17 + k, keep_volume=True) for k in range(2)]
-    eng = EngineAdapter(split=1)
+    eng = EngineAdapter(lanes=1)
     base = engine.tomo_memory_in_use()
     try:
         _abi.check(engine.tomo_set_memory_limit(base + need + need // 2))

@@ -72,6 +72,7 @@ SIGNATURES = {
     "tomo_create": (C.c_int32, [C.POINTER(Geom), C.POINTER(Params), C.POINTER(_P)]),
     "tomo_destroy": (C.c_int32, [_P]),
     "tomo_set_stream": (C.c_int32, [_P, C.c_void_p]),
+    "tomo_set_priority": (C.c_int32, [_P, C.c_int32]),
     "tomo_load_series": (C.c_int32, [_P, C.c_void_p, C.c_int32, _f64p, _f64p, _f64p]),
     "tomo_get_aligned": (C.c_int32, [_P, C.c_int32, _f32p]),
     "tomo_set_fill": (C.c_int32, [_P, C.c_int32]),
@@ -120,6 +121,9 @@ SIGNATURES = {
     "tomo_batch_create": (C.c_int32, [C.POINTER(C.c_void_p)]),
     "tomo_batch_destroy": (C.c_int32, [C.c_void_p]),
     "tomo_batch_set": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32]),
+    "tomo_batch_set_priority": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tomo_batch_set_persistent": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tomo_batch_set_stream": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "tomo_batch_iteration": (C.c_int32, [C.c_void_p, _f64p, _i32p, _i32p, C.c_int32, _f64p]),
     "tomo_project_and_difference_noalloc": (C.c_int32, [C.POINTER(Geom), _f64p, _i32p, C.c_int32, C.c_double,
                                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -5,7 +5,10 @@
 // for every update index s, one forward-projection launch per kernel variant
 // covers update s of every member that has one (each CTA reads its
 // {descriptor, tilt group, row} work item), one batched residual reduction
-// follows, and one backprojection launch covers all members' tiles.  The
+// follows, and one backprojection launch covers all members' tiles.  Optionally
+// (tomo_batch_set_persistent) each phase is one persistent launch per CTA size
+// instead: resident CTAs take items from a list, longest first, through an
+// atomic cursor, and the launches of a phase run side by side.  The
 // per-member descriptors and work lists are rebuilt only when the membership
 // or the update sizes change, and the step's launches are captured once as a
 // CUDA graph and replayed while they stay valid; every iteration only uploads
@@ -13,6 +16,7 @@
 // reads their residuals back.
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -26,7 +30,8 @@ struct tomo_batch {
     std::vector<int> upd;        // update size of each member in the cached plan
     std::vector<double> factor;  // relaxation factor of each member in the cached plan
     bool plan_valid = false;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // where the batch's work runs
+    cudaStream_t own_stream = nullptr;  // the stream the batch created
     // device plan
     FpLaunch* d_fp = nullptr;
     BpLaunch* d_bp = nullptr;
@@ -49,9 +54,35 @@ struct tomo_batch {
     struct RedSeg {
         int s, off, n, maxT;
     };
+    // persistent launches: one per (s, block size, chunk depth) for the forward phase and
+    // per (s, flags, storage type, row pairs) for the backprojection; cursor: its slot of
+    // d_cursor, zeroed at the start of every iteration
+    struct FpPSeg {
+        int s, nt, zc;
+        size_t smem;
+        int off, n, cursor, grid;
+    };
+    struct BpPSeg {
+        int s;
+        bool sanitize, pos;
+        int vt;
+        bool pairs;
+        int off, n, cursor, grid;
+    };
     std::vector<FpSeg> fp_segs;
     std::vector<BpSeg> bp_segs;
     std::vector<RedSeg> red_segs;
+    std::vector<FpPSeg> fp_psegs;
+    std::vector<BpPSeg> bp_psegs;
+    int persistent = 0;  // tomo_batch_set_persistent mode (default: a launch per kernel variant)
+    int* d_cursor = nullptr;
+    size_t cap_cursor = 0;
+    int n_cursor = 0;
+    int priority = 0;
+    // side streams and events for launches of one phase that run side by side
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> ev_join;
+    cudaEvent_t ev_fork = nullptr;
     int max_nsub = 0;
     bool has_fista = false;
     cudaGraphExec_t exec = nullptr;
@@ -62,6 +93,9 @@ struct tomo_batch {
 };
 
 namespace {
+
+// tomo_batch_set_persistent modes (1 = forward and backprojection persistent, longest first)
+constexpr int kPersistFp = 2, kPersistBp = 4, kPersistListOrder = 8, kPersistSerial = 16, kPersistFullGrid = 32;
 
 #define BCK(expr)                                                                              \
     do {                                                                                       \
@@ -109,6 +143,8 @@ tomo_status build_plan(tomo_batch* b) {
     std::map<std::tuple<int, int, int, int, int>, std::vector<int4>> fpi;
     std::map<std::tuple<int, int, int, int, int>, size_t> fpsmem;
     std::map<std::tuple<int, int, int, int, int>, std::vector<int4>> bpi;
+    std::map<std::tuple<int, int, int, int, int>, std::vector<double>> fpcost, bpcost;  // per item, persistent
+    std::map<std::tuple<int, int, int, int, int>, std::vector<int>> fpclass;  // kernel body of a persistent item
     std::map<int, std::vector<ErrReduce>> reds;
     b->max_nsub = 0;
     b->has_fista = false;
@@ -131,6 +167,9 @@ tomo_status build_plan(tomo_batch* b) {
         const int zc = fp_choose_zc(g.W, 1, p->vtype, nt);
         const int pk = p->vtype != kVolF32 ? 1 : 0;
         const int use_tma = fp_use_tma(g.W, p->vtype, p->vol());
+        int lq = 0;
+        while ((1 << lq) < qp) lq++;
+        const bool fp_persist = (b->persistent & kPersistFp) && fp_persist_supported(nt, zc);
         const int offset = (g.h > g.H && g.scale == 1) ? (g.h - g.H) / 2 : 0;
         const int j0 = std::max(0, (int)std::floor(offset * g.scale + 0.5));
         for (int s = 0; s < nsub; s++) {
@@ -162,11 +201,21 @@ tomo_status build_plan(tomo_batch* b) {
             a.status = p->d_status;
             const int di = (int)fp.size();
             fp.push_back(a);
-            const auto key = std::make_tuple(s, qp, nt, zc, pk);
+            // persistent launches group by block size and chunk depth only (qp = pk = -1)
+            const auto key = fp_persist ? std::make_tuple(s, -1, nt, zc, -1) : std::make_tuple(s, qp, nt, zc, pk);
             fpsmem[key] = std::max(fpsmem[key], fp_smem_bytes(zc, g.W, qp, 1, p->vtype));
             auto& items = fpi[key];
-            for (int g0 = 0; g0 < T; g0 += a.tilts_per_cta)
-                for (int j = j0; j < g.h; j++) items.push_back(make_int4(di, g0, j, use_tma));
+            // a row's tilt groups one after another: the staged planes are read again from L2
+            const int flags = use_tma | (fp_persist ? (lq << 1) | (pk << 4) : 0);
+            const double cost = (double)g.D * g.w * a.tilts_per_cta;  // ray-steps of a full item
+            for (int j = j0; j < g.h; j++)
+                for (int g0 = 0; g0 < T; g0 += a.tilts_per_cta) {
+                    items.push_back(make_int4(di, g0, j, flags));
+                    if (fp_persist) {
+                        fpcost[key].push_back(cost);
+                        fpclass[key].push_back(lq * 2 + pk);
+                    }
+                }
             reds[s].push_back(ErrReduce{a.errpart, p->d_err + slot, T, g.h});
             BpLaunch c{};
             c.vol = p->bp_target();
@@ -203,29 +252,66 @@ tomo_status build_plan(tomo_batch* b) {
                 }
                 if (!reached) continue;
                 for (int zt = 0; zt < (g.D + tzr - 1) / tzr; zt++)
-                    for (int xt = 0; xt < (g.W + tx - 1) / tx; xt++) bitems.push_back(make_int4(bi, xt, zt, r));
+                    for (int xt = 0; xt < (g.W + tx - 1) / tx; xt++) {
+                        bitems.push_back(make_int4(bi, xt, zt, r));
+                        bpcost[std::make_tuple(s, c.sanitize, c.positivity, c.vtype, pairs ? 1 : 0)].push_back(
+                            (double)T * std::min(tzr, g.D - zt * tzr));
+                    }
             }
         }
     }
-    // flatten
+    // flatten; the lists of persistent launches go longest item first (stable, so a row's
+    // tilt groups stay together)
+    // by kernel body first (CTAs that run the same body side by side share the instruction
+    // cache), then longest first
+    auto by_cost = [](std::vector<int4>& items, const std::vector<double>& cost, const std::vector<int>* cls) {
+        std::vector<size_t> idx(items.size());
+        for (size_t i = 0; i < idx.size(); i++) idx[i] = i;
+        std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) {
+            if (cls && (*cls)[x] != (*cls)[y]) return (*cls)[x] < (*cls)[y];
+            return cost[x] > cost[y];
+        });
+        std::vector<int4> out(items.size());
+        for (size_t i = 0; i < idx.size(); i++) out[i] = items[idx[i]];
+        items.swap(out);
+    };
+    const int sms = device_sms();
     std::vector<int4> fp_all, bp_all;
     b->fp_segs.clear();
     b->bp_segs.clear();
     b->red_segs.clear();
+    b->fp_psegs.clear();
+    b->bp_psegs.clear();
+    b->n_cursor = 0;
     for (auto& kv : fpi) {
-        tomo_batch::FpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
-                             std::get<3>(kv.first), std::get<4>(kv.first), fpsmem[kv.first], (int)fp_all.size(),
-                             (int)kv.second.size()};
+        const int s = std::get<0>(kv.first), nt = std::get<2>(kv.first), zc = std::get<3>(kv.first);
+        if (std::get<1>(kv.first) < 0) {
+            if (!(b->persistent & kPersistListOrder)) by_cost(kv.second, fpcost[kv.first], &fpclass[kv.first]);
+            const int n = (int)kv.second.size();
+            const int grid = (b->persistent & kPersistFullGrid) ? n : std::min(n, (nt <= 256 ? 2 : 1) * sms);
+            b->fp_psegs.push_back(tomo_batch::FpPSeg{s, nt, zc, fpsmem[kv.first], (int)fp_all.size(), n,
+                                                     b->n_cursor++, grid});
+        } else {
+            b->fp_segs.push_back(tomo_batch::FpSeg{s, std::get<1>(kv.first), nt, zc, std::get<4>(kv.first),
+                                                   fpsmem[kv.first], (int)fp_all.size(), (int)kv.second.size()});
+        }
         fp_all.insert(fp_all.end(), kv.second.begin(), kv.second.end());
-        b->fp_segs.push_back(sg);
     }
     for (auto& kv : bpi) {
-        tomo_batch::BpSeg sg{std::get<0>(kv.first), std::get<1>(kv.first) != 0, std::get<2>(kv.first) != 0,
-                             std::get<3>(kv.first), std::get<4>(kv.first) != 0, (int)bp_all.size(),
-                             (int)kv.second.size()};
+        const int s = std::get<0>(kv.first), vt = std::get<3>(kv.first);
+        const bool san = std::get<1>(kv.first) != 0, pos = std::get<2>(kv.first) != 0, pairs = std::get<4>(kv.first) != 0;
+        if (b->persistent & kPersistBp) {
+            if (!(b->persistent & kPersistListOrder)) by_cost(kv.second, bpcost[kv.first], nullptr);
+            const int n = (int)kv.second.size();
+            const int grid = std::min(n, bp_persist_ctas_per_sm(vt, pairs) * sms);
+            b->bp_psegs.push_back(tomo_batch::BpPSeg{s, san, pos, vt, pairs, (int)bp_all.size(), n, b->n_cursor++,
+                                                     grid});
+        } else {
+            b->bp_segs.push_back(tomo_batch::BpSeg{s, san, pos, vt, pairs, (int)bp_all.size(), (int)kv.second.size()});
+        }
         bp_all.insert(bp_all.end(), kv.second.begin(), kv.second.end());
-        b->bp_segs.push_back(sg);
     }
+    BCKS(ensure(&b->d_cursor, &b->cap_cursor, (size_t)std::max(b->n_cursor, 1)));
     for (auto& kv : reds) {
         int maxT = 0;
         for (auto& r : kv.second) maxT = std::max(maxT, r.T);
@@ -252,20 +338,74 @@ tomo_status build_plan(tomo_batch* b) {
     return TOMO_OK;
 }
 
+// Runs the launches of one phase: the first on the batch stream, the others on side
+// streams forked from it and joined back, so that one launch's tail overlaps the next.
+tomo_status run_side_by_side(tomo_batch* b, const std::vector<std::function<cudaError_t(cudaStream_t)>>& jobs) {
+    if (jobs.empty()) return TOMO_OK;
+    if (b->persistent & kPersistSerial) {
+        for (auto& j : jobs) BCK(j(b->stream));
+        return TOMO_OK;
+    }
+    const size_t side = jobs.size() - 1;
+    while (b->aux.size() < side) {
+        int least = 0, greatest = 0;
+        BCK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        cudaStream_t q = nullptr;
+        cudaEvent_t e = nullptr;
+        BCK(cudaStreamCreateWithPriority(&q, cudaStreamNonBlocking, std::max(greatest, least - b->priority)));
+        b->aux.push_back(q);
+        BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->ev_join.push_back(e);
+    }
+    if (side > 0) {
+        if (!b->ev_fork) BCK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+        BCK(cudaEventRecord(b->ev_fork, b->stream));
+    }
+    for (size_t k = 1; k < jobs.size(); k++) {
+        BCK(cudaStreamWaitEvent(b->aux[k - 1], b->ev_fork, 0));
+        BCK(jobs[k](b->aux[k - 1]));
+        BCK(cudaEventRecord(b->ev_join[k - 1], b->aux[k - 1]));
+    }
+    BCK(jobs[0](b->stream));
+    for (size_t k = 1; k < jobs.size(); k++) BCK(cudaStreamWaitEvent(b->stream, b->ev_join[k - 1], 0));
+    return TOMO_OK;
+}
+
 tomo_status launch_step(tomo_batch* b) {
     for (tomo_projector* p : b->members) BCKS(handle_start_iteration(p));
+    if (b->n_cursor > 0) BCK(cudaMemsetAsync(b->d_cursor, 0, sizeof(int) * b->n_cursor, b->stream));
     for (int s = 0; s < b->max_nsub; s++) {
+        std::vector<std::function<cudaError_t(cudaStream_t)>> jobs;
+        for (auto& sg : b->fp_psegs)
+            if (sg.s == s)
+                jobs.push_back([b, sg](cudaStream_t q) {
+                    return launch_fp_persist(sg.nt, sg.zc, b->d_fp, b->d_fp_items + sg.off, sg.n,
+                                             b->d_cursor + sg.cursor, sg.grid, sg.smem, q);
+                });
+        BCKS(run_side_by_side(b, jobs));
         for (auto& sg : b->fp_segs)
             if (sg.s == s)
                 BCK(launch_fp_batch(sg.qp, sg.nt, b->d_fp, b->d_fp_items + sg.off, sg.n, sg.zc, sg.smem, sg.pk, b->stream));
         for (auto& sg : b->red_segs)
             if (sg.s == s) BCK(launch_reduce_err_batch(b->d_red + sg.off, sg.n, sg.maxT, b->stream));
-        for (tomo_projector* p : b->members) BCKS(handle_bp_pre(p, b->stream));
+        // storage hooks of the members that have an update s
+        auto in_s = [&](size_t m) { return s * b->upd[m] < b->members[m]->g.N; };
+        for (size_t m = 0; m < b->members.size(); m++)
+            if (in_s(m)) BCKS(handle_bp_pre(b->members[m], b->stream));
+        std::vector<std::function<cudaError_t(cudaStream_t)>> bjobs;
+        for (auto& sg : b->bp_psegs)
+            if (sg.s == s)
+                bjobs.push_back([b, sg](cudaStream_t q) {
+                    return launch_bp_persist(sg.sanitize, sg.pos, sg.vt, sg.pairs, b->d_bp, b->d_bp_items + sg.off,
+                                             sg.n, b->d_cursor + sg.cursor, sg.grid, q);
+                });
+        BCKS(run_side_by_side(b, bjobs));
         for (auto& sg : b->bp_segs)
             if (sg.s == s)
                 BCK(launch_bp_batch(sg.sanitize, sg.pos, sg.vt, sg.pairs, b->d_bp, b->d_bp_items + sg.off, sg.n,
                                     b->stream));
-        for (tomo_projector* p : b->members) BCKS(handle_bp_post(p, b->stream));
+        for (size_t m = 0; m < b->members.size(); m++)
+            if (in_s(m)) BCKS(handle_bp_post(b->members[m], b->stream));
     }
     for (tomo_projector* p : b->members) BCKS(handle_end_iteration(p));
     return TOMO_OK;
@@ -278,12 +418,53 @@ extern "C" {
 tomo_status tomo_batch_create(tomo_batch** out) {
     if (!out) return handle_fail(TOMO_ERR_INVALID, "null argument");
     tomo_batch* b = new tomo_batch();
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete b;
         return handle_fail(TOMO_ERR_CUDA, "cannot create the batch stream");
     }
+    b->stream = b->own_stream;
     *out = b;
+    return TOMO_OK;
+}
+
+tomo_status tomo_batch_set_priority(tomo_batch* b, int32_t priority) {
+    if (!b || priority < 0) return handle_fail(TOMO_ERR_INVALID, "bad argument");
+    int least = 0, greatest = 0;  // numerically: least >= greatest, lower is more urgent
+    BCK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = std::max(greatest, least - priority);
+    cudaStream_t s = nullptr;
+    BCK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio));
+    // a captured iteration is launched into whatever stream the batch holds
+    cudaStreamSynchronize(b->stream);
+    const bool own = b->stream == b->own_stream;
+    cudaStreamDestroy(b->own_stream);
+    b->own_stream = s;
+    if (own) b->stream = s;
+    b->priority = priority;
+    for (cudaStream_t& q : b->aux) {  // side streams follow
+        cudaStreamSynchronize(q);
+        cudaStreamDestroy(q);
+        BCK(cudaStreamCreateWithPriority(&q, cudaStreamNonBlocking, prio));
+    }
+    drop_graph(b);  // captured with the old side streams' dependencies
+    return TOMO_OK;
+}
+
+tomo_status tomo_batch_set_stream(tomo_batch* b, void* stream) {
+    if (!b) return handle_fail(TOMO_ERR_INVALID, "null batch");
+    BCK(cudaStreamSynchronize(b->stream));
+    b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+    return TOMO_OK;
+}
+
+tomo_status tomo_batch_set_persistent(tomo_batch* b, int32_t on) {
+    if (!b) return handle_fail(TOMO_ERR_INVALID, "null batch");
+    BCK(cudaStreamSynchronize(b->stream));
+    if (on < 0 || on > 63) return handle_fail(TOMO_ERR_INVALID, "persistent mode out of range");
+    b->persistent = on == 1 ? (kPersistFp | kPersistBp) : on;
+    b->plan_valid = false;
+    drop_graph(b);
     return TOMO_OK;
 }
 
@@ -296,7 +477,15 @@ tomo_status tomo_batch_destroy(tomo_batch* b) {
     cudaFree(b->d_red);
     cudaFree(b->d_fp_items);
     cudaFree(b->d_bp_items);
-    cudaStreamDestroy(b->stream);
+    cudaFree(b->d_cursor);
+    for (cudaStream_t q : b->aux) {
+        cudaStreamSynchronize(q);
+        cudaStreamDestroy(q);
+    }
+    for (cudaEvent_t e : b->ev_join) cudaEventDestroy(e);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->stream != b->own_stream) cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->own_stream);
     delete b;
     return TOMO_OK;
 }
@@ -397,7 +586,10 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
         BCK(cudaMemcpy(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost));
         if (st != 0) {
             cudaMemset(p->d_status, 0, sizeof(int));
-            return handle_fail(TOMO_ERR_DEVICE, "a kernel reported a bounded-wait timeout");
+            std::string why = "member " + std::to_string(m) + ": a kernel reported status " + std::to_string(st);
+            if (st & kStatusTimeout) why += " (bounded wait expired)";
+            if (st & (int)kStatusRange) why += " (a volume value left the FP16 range of its slab scale)";
+            return handle_fail(TOMO_ERR_DEVICE, why.c_str());
         }
         if (err_out) {
             const int N = p->g.N;

@@ -342,9 +342,12 @@ __device__ __forceinline__ PartialOut full_chunk_inl(const PT* __restrict__ P, l
 // BLEND: the fractional-row form (row maps, two staged rows per plane).  A separate
 // instantiation, so that the whole-row kernels compile without any of it.
 // PK: pair kind (0: FP32 volume, float2 pairs; 1: 16-bit volume, half2 pairs).
+// Returns false when a bounded wait ran out (the CTA recorded it and has nothing in
+// flight); with `retire` the chunk mbarrier is invalidated at the end so that a persistent
+// CTA can initialise it again for its next work item.
 template <int NT, int QP, int ZC, bool BLEND, int PK>
-__device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma,
-                                        const int zp) {
+__device__ __forceinline__ bool fp_body(const FpLaunch& a, const int g0, const int j, const int use_tma,
+                                        const int zp, const bool retire = false) {
     static_assert(!(BLEND && PK), "the fractional-row form is FP32 only");
     using PairT = typename std::conditional<PK == 1, __half2, float2>::type;
     constexpr int TGMAX = kFpRays / QP > 0 ? kFpRays / QP : 1;
@@ -454,7 +457,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
                     if (tid == 0) atomicOr(a.status, kStatusTimeout);
                     // let any copy still in flight land before the CTA's shared memory is released
                     if (!held) mbar_wait_bounded(bar, parity, kWaitTries);
-                    return;
+                    return false;
                 }
             } else {
                 __syncthreads();
@@ -500,6 +503,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             __syncthreads();
             if (c + 1 < c_end && !use_tma) stage(c + 1);
         }
+        if (retire && use_tma && tid == 0) mbar_inval(bar);  // every phase has completed
     }
 
     // Depth split: publish this part's sums; the last part to arrive adds all parts in
@@ -521,7 +525,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             if (s_last) *tk = 0u;  // every part has arrived: ready for the next launch
         }
         __syncthreads();
-        if (!s_last) return;
+        if (!s_last) return true;
         __threadfence();
 #pragma unroll
         for (int k = 0; k < NR; k++) {
@@ -585,6 +589,7 @@ __device__ __forceinline__ void fp_body(const FpLaunch& a, const int g0, const i
             __syncthreads();
         }
     }
+    return true;
 }
 
 template <int NT, int QP, int ZC, bool BLEND, int PK>
@@ -599,6 +604,79 @@ __global__ void __launch_bounds__(NT, fp_ctas_per_sm(NT))
     fp_kernel_batch(const FpLaunch* __restrict__ descs, const int4* __restrict__ items) {
     const int4 it = items[blockIdx.x];
     fp_body<NT, QP, ZC, false, PK>(descs[it.x], it.y, it.z, it.w, 0);
+}
+
+// Persistent batched form: a resident grid whose CTAs take work items {problem, first
+// tilt, row, flags} in list order through an atomic cursor until the list runs out, so a
+// forward phase of a batch is one launch per block size and chunk depth whatever the
+// members' widths and storage types: the item's flags select the body (bit 0 bulk
+// copies, bits 1-3 log2 of the detector columns per thread QP, bit 4 16-bit pairs).  The
+// host orders the list by decreasing work, so the last items to start are the shortest.
+// A bounded wait that runs out ends the CTA (recorded in the problem's status word).
+template <int NT>
+struct FpPersistQP;
+template <>
+struct FpPersistQP<256> {
+    static constexpr int lo = 0, hi = 1;  // QP 1, 2
+};
+template <>
+struct FpPersistQP<512> {
+    static constexpr int lo = 1, hi = 3;  // QP 2, 4, 8
+};
+
+// One work item as a call of its own: each body keeps the register allocation and
+// instruction schedule it has as a kernel (inlined into the item loop it ran slower).
+template <int NT, int QP, int ZC, int PK>
+__device__ __noinline__ bool fp_item_call(const FpLaunch* a, int g0, int j, int use_tma) {
+    return fp_body<NT, QP, ZC, false, PK>(*a, g0, j, use_tma, 0, true);
+}
+
+template <int NT, int ZC, int LQ>
+__device__ __forceinline__ bool fp_persist_item(const FpLaunch* a, int g0, int j, int use_tma, int lq, int pk) {
+#ifdef TOMO_PERSIST_ONE_BODY
+    if constexpr (NT == 256) return fp_item_call<256, 2, ZC, 0>(a, g0, j, use_tma);
+#endif
+    if constexpr (LQ > FpPersistQP<NT>::hi) {
+        return true;
+    } else {
+        if (lq == LQ)
+            return pk ? fp_item_call<NT, 1 << LQ, ZC, 1>(a, g0, j, use_tma)
+                      : fp_item_call<NT, 1 << LQ, ZC, 0>(a, g0, j, use_tma);
+        return fp_persist_item<NT, ZC, LQ + 1>(a, g0, j, use_tma, lq, pk);
+    }
+}
+
+template <int NT, int ZC>
+__global__ void __launch_bounds__(NT, fp_ctas_per_sm(NT))
+    fp_kernel_persist(const FpLaunch* __restrict__ descs, const int4* __restrict__ items, int n_items,
+                      int* __restrict__ cursor) {
+    __shared__ int s_item;
+    int next = 0;  // thread 0: the item after the current one, fetched while it runs
+    if (threadIdx.x == 0) next = atomicAdd(cursor, 1);
+    for (;;) {
+        if (threadIdx.x == 0) s_item = next;
+        __syncthreads();
+        const int i = s_item;
+        if (i >= n_items) return;
+        if (threadIdx.x == 0) next = atomicAdd(cursor, 1);
+        const int4 it = items[i];
+        const int f = it.w;
+        if (!fp_persist_item<NT, ZC, FpPersistQP<NT>::lo>(descs + it.x, it.y, it.z, f & 1, (f >> 1) & 7, (f >> 4) & 1))
+            return;
+        __syncthreads();  // shared memory (and s_item) are free for the next item
+    }
+}
+
+template <int NT, int ZC>
+cudaError_t persist_attr() {
+    return cudaFuncSetAttribute(fp_kernel_persist<NT, ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fp_smem_budget(NT));
+}
+
+template <int NT, int ZC>
+void persist_launch(const FpLaunch* descs, const int4* items, int n_items, int* cursor, int grid, size_t smem,
+                    cudaStream_t s) {
+    fp_kernel_persist<NT, ZC><<<grid, NT, smem, s>>>(descs, items, n_items, cursor);
 }
 
 template <int NT, int QP, int ZC>

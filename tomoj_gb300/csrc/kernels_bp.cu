@@ -664,10 +664,49 @@ __global__ void __launch_bounds__(kBpThreads, Bp2Occ<VT>::value)
     bp2_body<SANITIZE, POS, VT, KZ>(descs[it.x], it.y * kTX, it.z * Bp2<KZ>::kTZ2, it.w);
 }
 
+// Persistent batched forms: a resident grid whose CTAs take items in list order through
+// an atomic cursor until the list runs out (the host orders it by decreasing work).
+template <bool SANITIZE, bool POS, int VT>
+__global__ void __launch_bounds__(kBpThreads, Bp2Occ<VT>::value)
+    bp2_kernel_persist(const BpLaunch* __restrict__ descs, const int4* __restrict__ items, int n_items,
+                       int* __restrict__ cursor) {
+    constexpr int KZ = Bp2Occ<VT>::kz;
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int i = s_item;
+        __syncthreads();  // every thread has the index before thread 0 fetches the next
+        if (i >= n_items) return;
+        const int4 it = items[i];
+        bp2_body<SANITIZE, POS, VT, KZ>(descs[it.x], it.y * kTX, it.z * Bp2<KZ>::kTZ2, it.w);
+        __syncthreads();  // shared memory is free for the next item
+    }
+}
+
+template <bool SANITIZE, bool POS, int VT>
+__global__ void __launch_bounds__(kBpCtaThreads, BpOcc<VT>::value)
+    bp_kernel_persist(const BpLaunch* __restrict__ descs, const int4* __restrict__ items, int n_items,
+                      int* __restrict__ cursor) {
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int i = s_item;
+        __syncthreads();  // every thread has the index before thread 0 fetches the next
+        if (i >= n_items) return;
+        const int4 it = items[i];
+        bp_body<SANITIZE, POS, VT, 96>(descs[it.x], it.y * kTX, it.z * kTZ, it.w);
+        __syncthreads();
+    }
+}
+
 template <bool SANITIZE, bool POS, int VT>
 cudaError_t bp2_attr_one() {
     const int m = (int)Bp2<Bp2Occ<VT>::kz>::bytes(VT != kVolF32);
     cudaError_t e = cudaFuncSetAttribute(bp2_kernel<SANITIZE, POS, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(bp2_kernel_persist<SANITIZE, POS, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(bp2_kernel_batch<SANITIZE, POS, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
@@ -706,6 +745,37 @@ void bp2_batch_vt(bool sanitize, bool positivity, const BpLaunch* descs, const i
         (void)sanitize;
         (void)positivity;
         bp2_kernel_batch<false, false, VT><<<n, kBpThreads, sm, s>>>(descs, items);
+    }
+}
+
+template <int VT>
+void bp2_persist_vt(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n, int* cursor,
+                    int grid, cudaStream_t s) {
+    const size_t sm = Bp2<Bp2Occ<VT>::kz>::bytes(VT != kVolF32);
+    if constexpr (VT == kVolF32) {
+        if (sanitize) {
+            if (positivity) bp2_kernel_persist<true, true, VT><<<grid, kBpThreads, sm, s>>>(descs, items, n, cursor);
+            else bp2_kernel_persist<true, false, VT><<<grid, kBpThreads, sm, s>>>(descs, items, n, cursor);
+        } else {
+            if (positivity) bp2_kernel_persist<false, true, VT><<<grid, kBpThreads, sm, s>>>(descs, items, n, cursor);
+            else bp2_kernel_persist<false, false, VT><<<grid, kBpThreads, sm, s>>>(descs, items, n, cursor);
+        }
+    } else {
+        (void)sanitize;
+        (void)positivity;
+        bp2_kernel_persist<false, false, VT><<<grid, kBpThreads, sm, s>>>(descs, items, n, cursor);
+    }
+}
+
+template <int VT>
+void bp_persist_vt(bool sanitize, bool positivity, const BpLaunch* descs, const int4* items, int n, int* cursor,
+                   int grid, cudaStream_t s) {
+    if (sanitize) {
+        if (positivity) bp_kernel_persist<true, true, VT><<<grid, kBpCtaThreads, 0, s>>>(descs, items, n, cursor);
+        else bp_kernel_persist<true, false, VT><<<grid, kBpCtaThreads, 0, s>>>(descs, items, n, cursor);
+    } else {
+        if (positivity) bp_kernel_persist<false, true, VT><<<grid, kBpCtaThreads, 0, s>>>(descs, items, n, cursor);
+        else bp_kernel_persist<false, false, VT><<<grid, kBpCtaThreads, 0, s>>>(descs, items, n, cursor);
     }
 }
 
@@ -772,6 +842,30 @@ cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, bool pair
     else if (vtype == kVolBF16) bp_batch_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, s);
     else if (vtype == kVolF16) bp_batch_vt<kVolF16>(sanitize, positivity, descs, items, n_items, s);
     else return cudaErrorInvalidValue;
+    count_launch();
+    return cudaGetLastError();
+}
+
+int bp_persist_ctas_per_sm(int vtype, bool pairs) {
+    if (pairs) return vtype == kVolF32 ? Bp2Occ<kVolF32>::value : Bp2Occ<kVolF16>::value;
+    return vtype == kVolF32 ? BpOcc<kVolF32>::value : BpOcc<kVolF16>::value;
+}
+
+cudaError_t launch_bp_persist(bool sanitize, bool positivity, int vtype, bool pairs, const BpLaunch* descs,
+                              const int4* items, int n_items, int* cursor, int grid, cudaStream_t s) {
+    if (n_items <= 0) return cudaSuccess;
+    if (pairs) {
+        if (!bp_row_pairs(vtype, sanitize, positivity)) return cudaErrorInvalidValue;
+        if (vtype == kVolF32) bp2_persist_vt<kVolF32>(sanitize, positivity, descs, items, n_items, cursor, grid, s);
+        else if (vtype == kVolBF16) bp2_persist_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, cursor, grid, s);
+        else if (vtype == kVolF16) bp2_persist_vt<kVolF16>(sanitize, positivity, descs, items, n_items, cursor, grid, s);
+        else return cudaErrorInvalidValue;
+    } else {
+        if (vtype == kVolF32) bp_persist_vt<kVolF32>(sanitize, positivity, descs, items, n_items, cursor, grid, s);
+        else if (vtype == kVolBF16) bp_persist_vt<kVolBF16>(sanitize, positivity, descs, items, n_items, cursor, grid, s);
+        else if (vtype == kVolF16) bp_persist_vt<kVolF16>(sanitize, positivity, descs, items, n_items, cursor, grid, s);
+        else return cudaErrorInvalidValue;
+    }
     count_launch();
     return cudaGetLastError();
 }

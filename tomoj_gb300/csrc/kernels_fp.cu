@@ -20,6 +20,12 @@ cudaError_t fp_batch_t256_q2(const FpLaunch* d, const int4* it, int n, int zc, s
 cudaError_t fp_batch_t512_q2(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
 cudaError_t fp_batch_t512_q4(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
 cudaError_t fp_batch_t512_q8(const FpLaunch* d, const int4* it, int n, int zc, size_t smem, int pk, cudaStream_t s);
+cudaError_t fp_persist_attr_t256();
+cudaError_t fp_persist_attr_t512();
+cudaError_t fp_persist_t256(int zc, const FpLaunch* descs, const int4* items, int n_items, int* cursor, int grid,
+                            size_t smem, cudaStream_t s);
+cudaError_t fp_persist_t512(int zc, const FpLaunch* descs, const int4* items, int n_items, int* cursor, int grid,
+                            size_t smem, cudaStream_t s);
 
 // Raises the dynamic shared-memory limit of every forward-projector variant once,
 // outside any stream capture.
@@ -29,7 +35,22 @@ cudaError_t fp_init_attributes() {
     if ((e = fp_attr_t256_q2()) != cudaSuccess) return e;
     if ((e = fp_attr_t512_q2()) != cudaSuccess) return e;
     if ((e = fp_attr_t512_q4()) != cudaSuccess) return e;
+    if ((e = fp_persist_attr_t256()) != cudaSuccess) return e;
+    if ((e = fp_persist_attr_t512()) != cudaSuccess) return e;
     return fp_attr_t512_q8();
+}
+
+bool fp_persist_supported(int nt, int zc) { return (nt == 256 && zc == 16) || (nt == 512 && (zc == 16 || zc == 8)); }
+
+cudaError_t launch_fp_persist(int nt, int zc, const FpLaunch* descs, const int4* items, int n_items, int* cursor,
+                              int grid, size_t smem, cudaStream_t s) {
+    if (n_items <= 0) return cudaSuccess;
+    if (!fp_persist_supported(nt, zc) || smem > fp_smem_budget(nt) || grid <= 0) return cudaErrorInvalidValue;
+    const cudaError_t e = nt == 256 ? fp_persist_t256(zc, descs, items, n_items, cursor, grid, smem, s)
+                                    : fp_persist_t512(zc, descs, items, n_items, cursor, grid, smem, s);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    return cudaGetLastError();
 }
 
 int fp_threads(int w) { return w <= 512 ? 256 : 512; }

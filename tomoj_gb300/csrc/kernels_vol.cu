@@ -49,7 +49,7 @@ __global__ void rowmax_kernel(const float* __restrict__ src, int rows, int y0, i
 template <int VT>
 __global__ void pack_kernel(const float* __restrict__ src, int rows, int y0, int W, int H, int D,
                             uint16_t* __restrict__ vol, float* __restrict__ vscale, const unsigned* __restrict__ vmax,
-                            int* status) {
+                            int* status, bool floor) {
     const size_t n = (size_t)D * rows * W;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
@@ -58,7 +58,8 @@ __global__ void pack_kernel(const float* __restrict__ src, int rows, int y0, int
         const int rr = (int)(zr % rows);
         const int z = (int)(zr / rows);
         const int r = y0 + rr;
-        const float s = slab_scale_for(__uint_as_float(vmax[r]));
+        const float m = __uint_as_float(vmax[r]);
+        const float s = floor ? slab_scale_target(m, __uint_as_float(vmax[H])) : slab_scale_for(m);
         if (z == 0 && x == 0) vscale[r] = s;
         float v = src[e] / s;  // power of two: exact
         if (VT == kVolF16 && fabsf(v) > kF16Max && isfinite(v)) {
@@ -89,10 +90,10 @@ template <int VT>
 __global__ void rescale_kernel(uint16_t* __restrict__ vol, float* __restrict__ vscale,
                                const unsigned* __restrict__ vmax, int W, int H, int D, int* status) {
     const int r = blockIdx.x;
-    const float m = __uint_as_float(vmax[r]);
+    const float m = __uint_as_float(vmax[r]), M = __uint_as_float(vmax[H]);
     const float s = vscale[r];
-    if (!slab_needs_rescale(m, s)) return;
-    const float ns = slab_scale_for(m);
+    if (!slab_needs_rescale(m, s, M)) return;
+    const float ns = slab_scale_target(m, M);
     const float f = s / ns;  // ratio of powers of two: exact
     for (int z = 0; z < D; z++) {
         uint16_t* row = vol + ((size_t)z * H + r) * W;
@@ -110,13 +111,24 @@ __global__ void rescale_kernel(uint16_t* __restrict__ vol, float* __restrict__ v
 }
 
 template <int VT>
-__global__ void fill16_kernel(uint16_t* __restrict__ vol, size_t n, float stored, float* __restrict__ vscale, int H,
-                              float scale) {
+__global__ void fill16_kernel(uint16_t* __restrict__ vol, size_t n, float stored, float* __restrict__ vscale,
+                              unsigned* __restrict__ vmax, int H, float scale, float mag) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint16_t b = vol_store16<VT>(stored);
     for (size_t e = i0; e < n; e += stride) vol[e] = b;
     for (size_t r = i0; r < (size_t)H; r += stride) vscale[r] = scale;
+    // row maxima and the volume's maximum (entry H) of the filled volume
+    for (size_t r = i0; r <= (size_t)H; r += stride) vmax[r] = __float_as_uint(mag);
+}
+
+// One CTA: the volume's largest |value| (entry H) from the row maxima [0, H).
+__global__ void vmax_total_kernel(unsigned* __restrict__ vmax, int H) {
+    __shared__ float red[kThreads / 32];
+    float m = 0.0f;
+    for (int r = threadIdx.x; r < H; r += kThreads) m = fmaxf(m, __uint_as_float(vmax[r]));
+    m = block_max(m, red);
+    if (threadIdx.x == 0) vmax[H] = __float_as_uint(m);
 }
 
 template <int VT>
@@ -146,14 +158,18 @@ cudaError_t launch_vol_rowmax(const float* src, int rows, int y0, int W, int H, 
 }
 
 cudaError_t launch_vol_pack(const float* src, int rows, int y0, int W, int H, int D, int vtype, void* vol,
-                            float* vscale, const unsigned* vmax, int* status, cudaStream_t s) {
+                            float* vscale, unsigned* vmax, bool floor, int* status, cudaStream_t s) {
     if (rows <= 0) return cudaSuccess;
+    if (floor) {
+        vmax_total_kernel<<<1, kThreads, 0, s>>>(vmax, H);
+        count_launch();
+    }
     const int g = grid_for((size_t)D * rows * W);
     uint16_t* v = static_cast<uint16_t*>(vol);
     if (vtype == kVolBF16)
-        pack_kernel<kVolBF16><<<g, kThreads, 0, s>>>(src, rows, y0, W, H, D, v, vscale, vmax, status);
+        pack_kernel<kVolBF16><<<g, kThreads, 0, s>>>(src, rows, y0, W, H, D, v, vscale, vmax, status, floor);
     else if (vtype == kVolF16)
-        pack_kernel<kVolF16><<<g, kThreads, 0, s>>>(src, rows, y0, W, H, D, v, vscale, vmax, status);
+        pack_kernel<kVolF16><<<g, kThreads, 0, s>>>(src, rows, y0, W, H, D, v, vscale, vmax, status, floor);
     else
         return cudaErrorInvalidValue;
     count_launch();
@@ -175,9 +191,11 @@ cudaError_t launch_vol_unpack(const void* vol, int vtype, const float* vscale, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, const unsigned* vmax, int W, int H, int D,
+cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, unsigned* vmax, int W, int H, int D,
                                int* status, cudaStream_t s) {
     uint16_t* v = static_cast<uint16_t*>(vol);
+    vmax_total_kernel<<<1, kThreads, 0, s>>>(vmax, H);
+    count_launch();
     if (vtype == kVolBF16)
         rescale_kernel<kVolBF16><<<H, kThreads, 0, s>>>(v, vscale, vmax, W, H, D, status);
     else if (vtype == kVolF16)
@@ -188,15 +206,17 @@ cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, const unsign
     return cudaGetLastError();
 }
 
-cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, size_t nvox, int H, float value, cudaStream_t s) {
-    const float scale = slab_scale_for(std::fabs(value));
+cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, unsigned* vmax, size_t nvox, int H, float value,
+                            cudaStream_t s) {
+    const float mag = std::isfinite(value) ? std::fabs(value) : 0.0f;
+    const float scale = slab_scale_for(mag);
     const float stored = value / scale;
     uint16_t* v = static_cast<uint16_t*>(vol);
-    const int g = grid_for(nvox);
+    const int g = grid_for(nvox > (size_t)H + 1 ? nvox : (size_t)H + 1);
     if (vtype == kVolBF16)
-        fill16_kernel<kVolBF16><<<g, kThreads, 0, s>>>(v, nvox, stored, vscale, H, scale);
+        fill16_kernel<kVolBF16><<<g, kThreads, 0, s>>>(v, nvox, stored, vscale, vmax, H, scale, mag);
     else if (vtype == kVolF16)
-        fill16_kernel<kVolF16><<<g, kThreads, 0, s>>>(v, nvox, stored, vscale, H, scale);
+        fill16_kernel<kVolF16><<<g, kThreads, 0, s>>>(v, nvox, stored, vscale, vmax, H, scale, mag);
     else
         return cudaErrorInvalidValue;
     count_launch();

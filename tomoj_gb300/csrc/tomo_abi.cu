@@ -410,10 +410,14 @@ tomo_status apply_weighting(tomo_projector* p, float* imgs, int T) {
     return TOMO_OK;
 }
 
-// Reduced storage: row maxima are rebuilt by every backprojection, then slabs whose
-// maximum left the target band are re-scaled (a no-op launch for most rows).
+// Reduced storage: before a backprojection, rows whose scale is under the floor set by
+// the volume's maximum get room to grow to that level (a row of tiny values next to rows
+// of ordinary ones would otherwise leave FP16's range at the first update); row maxima
+// are then rebuilt by the backprojection, and slabs whose maximum left the target band
+// are re-scaled (no-op launches for most rows).
 tomo_status bp_pre(tomo_projector* p, cudaStream_t s) {
     if (p->vtype == kVolF32) return TOMO_OK;
+    CK(launch_vol_rescale(p->vol(), p->vtype, p->d_vscale, p->d_vmax, p->g.W, p->g.H, p->g.D, p->d_status, s));
     CK(cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * p->g.H, s));
     return TOMO_OK;
 }
@@ -517,8 +521,10 @@ tomo_status tv_denoise(tomo_projector* p) {
     if (red) {
         CK(cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * g.H, p->stream));
         CK(launch_vol_rowmax(p->d_tv_f, g.H, 0, g.W, g.H, g.D, p->d_vmax, p->stream));
-        CK(launch_vol_pack(p->d_tv_f, g.H, 0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax, p->d_status,
-                           p->stream));
+        // iteration-time pack: scales floored by the volume's maximum (a row the step
+        // flattened keeps room for the next update)
+        CK(launch_vol_pack(p->d_tv_f, g.H, 0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax, true,
+                           p->d_status, p->stream));
     }
     return TOMO_OK;
 }
@@ -631,7 +637,7 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
     } else {
         A(alloc_n(p, &p->d_vol16, p->nvox));
         A(alloc_n(p, &p->d_vscale, (size_t)g.H));
-        A(alloc_n(p, &p->d_vmax, (size_t)g.H));
+        A(alloc_n(p, &p->d_vmax, (size_t)g.H + 1));  // row maxima, then the volume's maximum
     }
     A(alloc_n(p, &p->d_raw, N * p->npix));
     A(alloc_n(p, &p->d_meas, N * p->npix));
@@ -674,8 +680,7 @@ tomo_status tomo_create(const tomo_geom* geom, const tomo_params* params, tomo_p
     if (p->vtype == kVolF32) {
         cudaMemsetAsync(p->d_vol, 0, sizeof(float) * p->nvox, p->stream);
     } else {
-        launch_vol_fill(p->d_vol16, p->vtype, p->d_vscale, p->nvox, g.H, 0.0f, p->stream);
-        cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * g.H, p->stream);
+        launch_vol_fill(p->d_vol16, p->vtype, p->d_vscale, p->d_vmax, p->nvox, g.H, 0.0f, p->stream);
     }
     cudaMemsetAsync(p->d_status, 0, sizeof(int), p->stream);
     cudaMemsetAsync(p->d_err, 0, sizeof(double) * N, p->stream);
@@ -729,6 +734,24 @@ tomo_status tomo_destroy(tomo_projector* p) {
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     if (p->wav) wavelet_plan_destroy(p->wav);
     delete p;
+    return TOMO_OK;
+}
+
+tomo_status tomo_set_priority(tomo_projector* p, int32_t priority) {
+    if (!p || priority < 0) return fail(TOMO_ERR_INVALID, "bad argument");
+    if (p->vol_owner) return fail(TOMO_ERR_STATE, "this handle works on another handle's volume");
+    int least = 0, greatest = 0;  // numerically: least >= greatest, lower is more urgent
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    cudaStream_t s = nullptr;
+    CK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, std::max(greatest, least - priority)));
+    CK(cudaStreamSynchronize(p->stream));
+    const bool own = (p->stream == p->own_stream);
+    cudaStreamDestroy(p->own_stream);
+    p->own_stream = s;
+    if (own) {
+        p->stream = s;
+        for (tomo_projector* q : p->vol_sharers) q->stream = s;
+    }
     return TOMO_OK;
 }
 
@@ -1002,6 +1025,8 @@ static tomo_status volume_copy(tomo_projector* p, float* host_or_dev, int on_dev
     // reduced storage: blocks of rows through the FP32 staging buffer
     size_t cap = 0;
     CKS(ensure_vtmp(p, &cap));
+    // a whole new volume: the old row maxima must not count towards its maximum
+    if (to_dev && rows == (size_t)g.H) CK(cudaMemsetAsync(p->d_vmax, 0, sizeof(unsigned) * g.H, p->stream));
     kind = on_device ? cudaMemcpyDeviceToDevice : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
     for (size_t a = 0; a < rows; a += cap) {
         const size_t n = std::min(cap, rows - a);
@@ -1012,7 +1037,7 @@ static tomo_status volume_copy(tomo_projector* p, float* host_or_dev, int on_dev
                                  sizeof(float) * g.W * n, g.D, kind, p->stream));
             CK(cudaMemsetAsync(p->d_vmax + r0, 0, sizeof(unsigned) * n, p->stream));
             CK(launch_vol_rowmax(p->d_vtmp, (int)n, r0, g.W, g.H, g.D, p->d_vmax, p->stream));
-            CK(launch_vol_pack(p->d_vtmp, (int)n, r0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax,
+            CK(launch_vol_pack(p->d_vtmp, (int)n, r0, g.W, g.H, g.D, p->vtype, p->vol(), p->d_vscale, p->d_vmax, false,
                                p->d_status, p->stream));
         } else {
             CK(launch_vol_unpack(p->vol(), p->vtype, p->d_vscale, (int)n, r0, g.W, g.H, g.D, p->d_vtmp, p->stream));
@@ -1047,7 +1072,7 @@ tomo_status tomo_fill_volume(tomo_projector* p, float value) {
     if (p->vtype == kVolF32)
         CK(launch_fill(p->d_vol, p->nvox, value, p->stream));
     else
-        CK(launch_vol_fill(p->vol(), p->vtype, p->d_vscale, p->nvox, p->g.H, value, p->stream));
+        CK(launch_vol_fill(p->vol(), p->vtype, p->d_vscale, p->d_vmax, p->nvox, p->g.H, value, p->stream));
     CK(cudaStreamSynchronize(p->stream));
     p->vol_flag() = !std::isfinite(value);
     return TOMO_OK;
@@ -1484,9 +1509,13 @@ tomo_status tomo_autotune(tomo_projector* p, int32_t update, int32_t reps, doubl
         const size_t vbytes = p->nvox * (p->vtype == kVolF32 ? sizeof(float) : sizeof(uint16_t));
         unsigned char* save = nullptr;
         float* save_sc = nullptr;
+        unsigned* save_mx = nullptr;
         CKS(alloc_n(p, &save, vbytes));
-        if (p->vtype != kVolF32 && alloc_n(p, &save_sc, (size_t)g.H) != TOMO_OK) {
+        if (p->vtype != kVolF32 &&
+            (alloc_n(p, &save_sc, (size_t)g.H) != TOMO_OK || alloc_n(p, &save_mx, (size_t)g.H + 1) != TOMO_OK)) {
             free_n(p, &save, vbytes);
+            free_n(p, &save_sc, (size_t)g.H);
+            free_n(p, &save_mx, (size_t)g.H + 1);
             return TOMO_ERR_NOMEM;
         }
         cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1496,6 +1525,8 @@ tomo_status tomo_autotune(tomo_projector* p, int32_t update, int32_t reps, doubl
         };
         ck(cudaMemcpyAsync(save, p->vol(), vbytes, cudaMemcpyDeviceToDevice, p->stream));
         if (save_sc) ck(cudaMemcpyAsync(save_sc, p->d_vscale, sizeof(float) * g.H, cudaMemcpyDeviceToDevice, p->stream));
+        if (save_mx)
+            ck(cudaMemcpyAsync(save_mx, p->d_vmax, sizeof(unsigned) * (g.H + 1), cudaMemcpyDeviceToDevice, p->stream));
         ck(cudaEventCreate(&e0));
         ck(cudaEventCreate(&e1));
         for (int i = 0; i < T; i++) p->batch.push_back(i);
@@ -1546,11 +1577,14 @@ tomo_status tomo_autotune(tomo_projector* p, int32_t update, int32_t reps, doubl
         p->bp_rows = best_r;
         ck(cudaMemcpyAsync(p->vol(), save, vbytes, cudaMemcpyDeviceToDevice, p->stream));
         if (save_sc) ck(cudaMemcpyAsync(p->d_vscale, save_sc, sizeof(float) * g.H, cudaMemcpyDeviceToDevice, p->stream));
+        if (save_mx)
+            ck(cudaMemcpyAsync(p->d_vmax, save_mx, sizeof(unsigned) * (g.H + 1), cudaMemcpyDeviceToDevice, p->stream));
         ck(cudaStreamSynchronize(p->stream));
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
         free_n(p, &save, vbytes);
         free_n(p, &save_sc, (size_t)g.H);
+        free_n(p, &save_mx, (size_t)g.H + 1);
         tomo_clear_projections(p);
         if (st != TOMO_OK) return st;
     }

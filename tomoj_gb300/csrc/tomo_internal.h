@@ -217,6 +217,11 @@ cudaError_t launch_bp_separable(const BpLaunch& a, cudaStream_t s);
 // first row of a pair of rows; z tiles of bp_pair_tile_z()).
 cudaError_t launch_bp_batch(bool sanitize, bool positivity, int vtype, bool pairs, const BpLaunch* descs,
                             const int4* items, int n_items, cudaStream_t s);
+// Persistent batched backprojection: `grid` resident CTAs take items in list order through
+// the atomic *cursor (zero before the launch).
+cudaError_t launch_bp_persist(bool sanitize, bool positivity, int vtype, bool pairs, const BpLaunch* descs,
+                              const int4* items, int n_items, int* cursor, int grid, cudaStream_t s);
+int bp_persist_ctas_per_sm(int vtype, bool pairs);
 int bp_tile_x();
 int bp_tile_z();
 // Whole-row backprojections of this kind run two volume rows per CTA (batch items then
@@ -272,6 +277,13 @@ size_t fp_smem_bytes(int ZC, int W, int qp, int rows = 1, int vtype = kVolF32);
 // pk = 1 when every descriptor of the launch has a 16-bit volume, 0 when all are FP32.
 cudaError_t launch_fp_batch(int qp, int nt, const FpLaunch* descs, const int4* items, int n_items, int zc,
                             size_t smem, int pk, cudaStream_t s);
+// Persistent batched forward projection: `grid` resident CTAs of nt threads take items
+// {descriptor, first tilt, row, flags} in list order through the atomic *cursor (zero
+// before the launch); flags: bit 0 bulk copies, bits 1-3 log2 QP, bit 4 16-bit pairs.
+// One kernel per (nt, zc) serves every QP of its block size and both pair kinds.
+bool fp_persist_supported(int nt, int zc);
+cudaError_t launch_fp_persist(int nt, int zc, const FpLaunch* descs, const int4* items, int n_items, int* cursor,
+                              int grid, size_t smem, cudaStream_t s);
 cudaError_t fp_init_attributes();
 cudaError_t misc_init_attributes();
 cudaError_t launch_reduce_err(const double* errpart, double* err, int T, int h, cudaStream_t s);
@@ -324,15 +336,22 @@ cudaError_t wavelet_read_threshold(const WaveletPlan* P, double* out, cudaStream
 // Max |value| of each of the rows into vmax[y0 + row] (float bits; vmax zeroed by the caller).
 cudaError_t launch_vol_rowmax(const float* src, int rows, int y0, int W, int H, int D, unsigned* vmax,
                               cudaStream_t s);
-// Picks each row's scale from vmax (slab_scale_for) and packs src into the reduced volume.
+// vmax holds H + 1 entries: the row maxima and, in entry H, the volume's maximum.
+// Picks each row's scale from its maximum (slab_scale_for) or, with `floor`, from its
+// maximum and the volume's (vmax[H] set here first; slab_scale_target), and packs src
+// into the reduced volume.
 cudaError_t launch_vol_pack(const float* src, int rows, int y0, int W, int H, int D, int vtype, void* vol,
-                            float* vscale, const unsigned* vmax, int* status, cudaStream_t s);
+                            float* vscale, unsigned* vmax, bool floor, int* status, cudaStream_t s);
 cudaError_t launch_vol_unpack(const void* vol, int vtype, const float* vscale, int rows, int y0, int W, int H,
                               int D, float* dst, cudaStream_t s);
-// Re-scales the rows whose max (vmax, after a backprojection) left the target band.
-cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, const unsigned* vmax, int W, int H, int D,
+// Sets vmax[H] from the row maxima, then re-scales the rows whose scale
+// slab_needs_rescale rejects (before a backprojection: rows under the floor; after it:
+// rows whose maximum left the band as well).
+cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, unsigned* vmax, int W, int H, int D,
                                int* status, cudaStream_t s);
-cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, size_t nvox, int H, float value, cudaStream_t s);
+// Fills the volume with `value`: scales, row maxima and the volume's maximum follow.
+cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, unsigned* vmax, size_t nvox, int H, float value,
+                            cudaStream_t s);
 cudaError_t launch_scan_nonfinite_vol(const void* vol, int vtype, size_t n, int* flags, cudaStream_t s);
 
 // Streaming multiprocessors of the current device (queried once per device ordinal and

@@ -57,11 +57,32 @@ __host__ __device__ inline float slab_scale_for(float m) {
     return s;
 }
 
-// A row is re-scaled after a backprojection when max / scale leaves [1, 2^10).
-__host__ __device__ inline bool slab_needs_rescale(float m, float scale) {
+// Lower bound of every row's scale, given the volume's largest |value| M: 2^-11 of the
+// scale of M.  A row whose own values are tiny (a background row, a row that a TV step
+// flattened) then keeps room up to about M before FP16 overflows, so the next
+// backprojection can raise it to the level of the rest of the volume; its values stay
+// normal down to about M * 2^-29.  A volume of zeros (M = 0) keeps 1.
+__host__ __device__ inline float slab_scale_floor(float M) {
+    if (!(M > 0.0f) || !(M < 3.0e38f)) return 1.0f;
+    return slab_scale_for(M) * (1.0f / 2048.0f);
+}
+
+// Scale of a row whose largest |value| is m in a volume whose largest is M.
+__host__ __device__ inline float slab_scale_target(float m, float M) {
+    const float a = slab_scale_for(m), b = slab_scale_floor(M);
+    return a > b ? a : b;
+}
+
+// A row is re-scaled when max / scale reaches 2^10 (FP16 room running out), or when it
+// fell below 1 or the row's scale is under the floor and the target differs (precision,
+// headroom).  A zero maximum (a row of zeros, or a row the backprojection did not reach)
+// and a non-finite one leave the row as it is.
+__host__ __device__ inline bool slab_needs_rescale(float m, float scale, float M) {
     if (!(m > 0.0f) || !(m < 3.0e38f)) return false;
+    const float fl = slab_scale_floor(M);
     const float q = m / scale;
-    return q < 1.0f || q >= 1024.0f;
+    if (q >= 1024.0f) return true;
+    return (q < 1.0f || scale < fl) && slab_scale_target(m, M) != scale;
 }
 
 }  // namespace tomo
