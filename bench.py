@@ -712,7 +712,7 @@ def run_serving_leg(args):
     p50 drift check serves one short schedule at the start and again at the end."""
     import torch
     from tomoj_gb300 import _abi
-    from tomoj_gb300.serving import EngineAdapter, Server, simulate, summarize, synthetic_requests
+    from tomoj_gb300.serving import EngineAdapter, Server, lane_summary, simulate, summarize, synthetic_requests
     prec = _abi.PREC_FP16
     # admission is by free HBM: hand back what earlier legs left in torch's allocator cache
     torch.cuda.empty_cache()
@@ -722,17 +722,19 @@ def run_serving_leg(args):
     def serve(reqs):
         eng = EngineAdapter(lanes=3)
         try:
+            srv = Server(eng, max_active=64)
             t0 = time.perf_counter()
-            res = Server(eng, max_active=64).run(reqs)
+            res = srv.run(reqs)
             wall = time.perf_counter() - t0
         finally:
             eng.close()
         s = summarize(res, requests=reqs)
         s["wall_s"] = wall
+        s["lanes_observed"] = lane_summary(srv.lane_log, wall)
         return s
 
     def short(s):
-        return {k: s[k] for k in ("requests", "p50_s", "p99_s", "mean_s", "voxel_updates_per_s")}
+        return {k: s[k] for k in ("requests", "p50_s", "p99_s", "mean_s", "voxel_updates_per_s") if k in s}
 
     drift_reqs = synthetic_requests(24, seed=9, sizes=(512, 1024), precision=prec)
     drift0 = serve(drift_reqs)

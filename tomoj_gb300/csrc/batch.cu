@@ -90,7 +90,30 @@ struct tomo_batch {
     uint64_t graph_kernels = 0;
     std::vector<int> host_orders;
     std::vector<double> host_err;
+    std::vector<int> host_status;
 };
+
+#ifdef TOMO_TRACE_BATCH
+#include <chrono>
+#include <cstdio>
+#define TRACE_MARK(name) trace_mark(name)
+static thread_local std::chrono::steady_clock::time_point g_tr0;
+static thread_local char g_trbuf[512];
+static thread_local int g_trlen = 0;
+static void trace_mark(const char* name) {
+    const auto t = std::chrono::steady_clock::now();
+    if (name[0] == '<') {
+        g_tr0 = t;
+        g_trlen = 0;
+        return;
+    }
+    const double ms = std::chrono::duration<double, std::milli>(t - g_tr0).count();
+    g_trlen += snprintf(g_trbuf + g_trlen, sizeof(g_trbuf) - g_trlen, " %s=%.2f", name, ms);
+    if (name[0] == '>') fprintf(stderr, "[batch %p]%s\n", (void*)&g_tr0, g_trbuf);
+}
+#else
+#define TRACE_MARK(name) ((void)0)
+#endif
 
 namespace {
 
@@ -112,13 +135,15 @@ constexpr int kPersistFp = 2, kPersistBp = 4, kPersistListOrder = 8, kPersistSer
         if (_s != TOMO_OK) return _s; \
     } while (0)
 
+// Plan buffers grow by half again and come from the engine's stream-ordered pool: a batch
+// whose membership grows while other batches run never waits for the whole device.
 template <class T>
-tomo_status ensure(T** ptr, size_t* cap, size_t n) {
+tomo_status ensure(T** ptr, size_t* cap, size_t n, cudaStream_t s) {
     if (n <= *cap && *ptr) return TOMO_OK;
-    if (*ptr) cudaFree(*ptr);
+    if (*ptr) pool_free(*ptr, s);
     *ptr = nullptr;
-    size_t c = std::max<size_t>(n, 16);
-    if (cudaMalloc(reinterpret_cast<void**>(ptr), c * sizeof(T)) != cudaSuccess) {
+    size_t c = std::max<size_t>(std::max<size_t>(n, *cap + *cap / 2), 16);
+    if (pool_malloc(reinterpret_cast<void**>(ptr), c * sizeof(T)) != cudaSuccess) {
         cudaGetLastError();
         *cap = 0;
         return handle_fail(TOMO_ERR_NOMEM, "batch plan allocation failed");
@@ -311,18 +336,18 @@ tomo_status build_plan(tomo_batch* b) {
         }
         bp_all.insert(bp_all.end(), kv.second.begin(), kv.second.end());
     }
-    BCKS(ensure(&b->d_cursor, &b->cap_cursor, (size_t)std::max(b->n_cursor, 1)));
+    BCKS(ensure(&b->d_cursor, &b->cap_cursor, (size_t)std::max(b->n_cursor, 1), b->stream));
     for (auto& kv : reds) {
         int maxT = 0;
         for (auto& r : kv.second) maxT = std::max(maxT, r.T);
         b->red_segs.push_back(tomo_batch::RedSeg{kv.first, (int)red.size(), (int)kv.second.size(), maxT});
         red.insert(red.end(), kv.second.begin(), kv.second.end());
     }
-    BCKS(ensure(&b->d_fp, &b->cap_fp, fp.size()));
-    BCKS(ensure(&b->d_bp, &b->cap_bp, bp.size()));
-    BCKS(ensure(&b->d_red, &b->cap_red, red.size()));
-    BCKS(ensure(&b->d_fp_items, &b->cap_fpi, fp_all.size()));
-    BCKS(ensure(&b->d_bp_items, &b->cap_bpi, bp_all.size()));
+    BCKS(ensure(&b->d_fp, &b->cap_fp, fp.size(), b->stream));
+    BCKS(ensure(&b->d_bp, &b->cap_bp, bp.size(), b->stream));
+    BCKS(ensure(&b->d_red, &b->cap_red, red.size(), b->stream));
+    BCKS(ensure(&b->d_fp_items, &b->cap_fpi, fp_all.size(), b->stream));
+    BCKS(ensure(&b->d_bp_items, &b->cap_bpi, bp_all.size(), b->stream));
     BCK(cudaMemcpyAsync(b->d_fp, fp.data(), sizeof(FpLaunch) * fp.size(), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->d_bp, bp.data(), sizeof(BpLaunch) * bp.size(), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->d_red, red.data(), sizeof(ErrReduce) * red.size(), cudaMemcpyHostToDevice, b->stream));
@@ -472,12 +497,10 @@ tomo_status tomo_batch_destroy(tomo_batch* b) {
     if (!b) return TOMO_OK;
     cudaStreamSynchronize(b->stream);
     drop_graph(b);
-    cudaFree(b->d_fp);
-    cudaFree(b->d_bp);
-    cudaFree(b->d_red);
-    cudaFree(b->d_fp_items);
-    cudaFree(b->d_bp_items);
-    cudaFree(b->d_cursor);
+    for (void* q : {(void*)b->d_fp, (void*)b->d_bp, (void*)b->d_red, (void*)b->d_fp_items, (void*)b->d_bp_items,
+                    (void*)b->d_cursor})
+        if (q) pool_free(q, b->stream);
+    cudaStreamSynchronize(b->stream);
     for (cudaStream_t q : b->aux) {
         cudaStreamSynchronize(q);
         cudaStreamDestroy(q);
@@ -510,8 +533,10 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
     if (!b || !relax || !update || !first) return handle_fail(TOMO_ERR_INVALID, "null argument");
     const size_t M = b->members.size();
     if (M == 0) return TOMO_OK;
+    TRACE_MARK("<");
     // the members' own streams must be idle: their buffers are used on the batch stream
     for (tomo_projector* p : b->members) BCK(cudaStreamSynchronize(p->stream));
+    TRACE_MARK("own");
     std::vector<int> upd(M);
     std::vector<double> fac(M);
     for (size_t m = 0; m < M; m++) {
@@ -526,6 +551,7 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
         b->factor = fac;
         BCKS(build_plan(b));
     }
+    TRACE_MARK("plan");
     // orderings of this iteration into each member's batch buffer
     size_t total = 0;
     for (size_t m = 0; m < M; m++) total += b->members[m]->g.N;
@@ -538,6 +564,7 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
                             b->stream));
         o += p->g.N;
     }
+    TRACE_MARK("orders");
     // the members' start/end-of-iteration work (TVM, FISTA) joins the batch stream
     std::vector<cudaStream_t> saved(M);
     for (size_t m = 0; m < M; m++) {
@@ -571,21 +598,29 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
     } else {
         BCKS(launch_step(b));
     }
+    TRACE_MARK("launch");
+    // residuals and status words on the batch stream (a copy on the legacy default stream
+    // waited for every other stream's work here: a small batch's iteration took as long as
+    // a large batch's running beside it)
     b->host_err.resize(total);
+    b->host_status.assign(M, 0);
     o = 0;
     for (size_t m = 0; m < M; m++) {
         tomo_projector* p = b->members[m];
         BCK(cudaMemcpyAsync(&b->host_err[o], p->d_err, sizeof(double) * p->g.N, cudaMemcpyDeviceToHost, b->stream));
+        BCK(cudaMemcpyAsync(&b->host_status[m], p->d_status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
         o += p->g.N;
     }
+    TRACE_MARK("errcopy");
     BCK(cudaStreamSynchronize(b->stream));
+    TRACE_MARK(">sync");
     o = 0;
     for (size_t m = 0; m < M; m++) {
         tomo_projector* p = b->members[m];
-        int st = 0;
-        BCK(cudaMemcpy(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+        const int st = b->host_status[m];
         if (st != 0) {
-            cudaMemset(p->d_status, 0, sizeof(int));
+            cudaMemsetAsync(p->d_status, 0, sizeof(int), b->stream);
+            cudaStreamSynchronize(b->stream);
             std::string why = "member " + std::to_string(m) + ": a kernel reported status " + std::to_string(st);
             if (st & kStatusTimeout) why += " (bounded wait expired)";
             if (st & (int)kStatusRange) why += " (a volume value left the FP16 range of its slab scale)";

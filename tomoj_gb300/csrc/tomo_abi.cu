@@ -557,6 +557,16 @@ tomo_status start_iteration(tomo_projector* p) {
 }  // namespace
 
 namespace tomo {
+// Buffers outside a handle (batch plans) from the same stream-ordered pool: no device-wide
+// synchronisation when a plan grows while other streams run.
+cudaError_t pool_malloc(void** ptr, size_t bytes) {
+    DevicePool* d = device_pool();
+    if (!d) return cudaMalloc(ptr, bytes);
+    cudaError_t e = cudaMallocFromPoolAsync(ptr, bytes, d->pool, d->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+    return e;
+}
+void pool_free(void* ptr, cudaStream_t stream) { dfree(ptr, stream); }
 tomo_status handle_fail(tomo_status code, const char* msg) { return fail(code, msg); }
 tomo_status handle_need_series(tomo_projector* p) { return need_series(p); }
 tomo_status handle_start_iteration(tomo_projector* p) { return start_iteration(p); }

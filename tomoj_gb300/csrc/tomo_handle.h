@@ -138,6 +138,10 @@ struct tomo_projector {
 
 namespace tomo {
 // Helpers of tomo_abi.cu used by the batch driver.
+// Device buffers from the engine's stream-ordered pool; pool_free orders the release after
+// the work queued on `stream`.
+cudaError_t pool_malloc(void** ptr, size_t bytes);
+void pool_free(void* ptr, cudaStream_t stream);
 tomo_status handle_fail(tomo_status code, const char* msg);
 tomo_status handle_need_series(tomo_projector* p);
 tomo_status handle_start_iteration(tomo_projector* p);

@@ -5,8 +5,8 @@ iteration count and volume storage precision) arrive over time.  The server keep
 every admitted request's volume, series and residuals resident in HBM.
 
 * Admission (one host thread): requests queue in arrival order per lane (below);
-  the head of the most urgent lane that fits is admitted when an active slot is
-  free and the engine can allocate its buffers (tomo_create's admission by free
+  the head of the most urgent lane that fits is admitted when its lane has a free
+  active slot and the engine can allocate its buffers (tomo_create's admission by free
   HBM, TOMO_ERR_NOMEM otherwise; handle buffers come from the engine's
   stream-ordered pool, so a retired request's memory is reused without a
   device-wide synchronisation).  A large request waiting for HBM therefore does
@@ -18,8 +18,9 @@ every admitted request's volume, series and residuals resident in HBM.
   launch per kernel variant covers every member, the iteration replayed as a CUDA
   graph) driven by its own host thread, on its own stream, at its own priority:
   lanes iterate independently, so a 512^2 request is not paced by the iterations
-  of 2048^2 ones, and the lanes of smaller requests are more urgent (their CTAs are
-  dispatched first as SMs free up).  Requests join a lane between two of its
+  of 2048^2 ones, and the lanes of smaller requests are more urgent: their CTAs
+  are dispatched first as SMs free up (measured: a 10.5 ms iteration of five
+  512^2 series takes 10.9 ms beside a 2048^2 x 512 iteration of 200 ms).  Requests join a lane between two of its
   iterations and leave when their last iteration is done.
 * WBP requests (one weighted backprojection) run on a worker thread, each on its
   handle's own stream at the most urgent priority.
@@ -141,6 +142,15 @@ class EngineAdapter:
             self.lib.tomo_batch_destroy(b)
         self.batches = []
 
+    def fits(self, req: Request) -> bool:
+        """Whether free HBM (with the engine pool's idle blocks) holds the request's estimated
+        footprint: a cheap test before tomo_create, which would otherwise allocate and
+        release most of a request that cannot be admitted yet."""
+        free, total = C.c_uint64(), C.c_uint64()
+        if self.lib.tomo_device_memory(C.byref(free), C.byref(total)) != _abi.OK:
+            return True
+        return request_bytes(req) <= free.value
+
     def create(self, req: Request):
         """Handle with the request's series loaded; None if HBM is short (TOMO_ERR_NOMEM)."""
         lib = self.lib
@@ -159,14 +169,24 @@ class EngineAdapter:
             eul = np.ascontiguousarray([euler_angles_to_matrix(0.0, a, -0.0) for a in req.angles], np.float64)
             T = None if req.transforms is None else np.ascontiguousarray(req.transforms, np.float64)
             pix = np.ascontiguousarray(req.series, np.float32)
-            _abi.check(lib.tomo_load_series(hd, pix.ctypes.data, 0, _abi.ptr(eul, C.c_double),
-                                            None if T is None else _abi.ptr(T, C.c_double), None))
+            # the series tables and the TV scratch are allocated here too: HBM short for
+            # them defers the request like a short tomo_create
+            rc = lib.tomo_load_series(hd, pix.ctypes.data, 0, _abi.ptr(eul, C.c_double),
+                                      None if T is None else _abi.ptr(T, C.c_double), None)
+            if rc == _abi.ERR_NOMEM:
+                lib.tomo_destroy(hd)
+                return None
+            _abi.check(rc)
             if req.kind == WBP:
                 _abi.check(lib.tomo_set_weighting(hd, req.weighting, 0.5, None, None))
                 _abi.check(lib.tomo_set_priority(hd, self.top_priority))
             if req.kind == TVM:
                 th, gg, dt, it = req.tvm
-                _abi.check(lib.tomo_set_tvm(hd, th, gg, dt, it))
+                rc = lib.tomo_set_tvm(hd, th, gg, dt, it)
+                if rc == _abi.ERR_NOMEM:
+                    lib.tomo_destroy(hd)
+                    return None
+                _abi.check(rc)
         except Exception:
             lib.tomo_destroy(hd)
             raise
@@ -202,8 +222,11 @@ class EngineAdapter:
 
 class Server:
     def __init__(self, engine=None, max_active: int = 64, lane_bounds=None):
+        """max_active: active requests per lane.  After run(), `lane_log` holds one
+        (lane, start, end, members, voxel-updates) tuple per batched iteration."""
         self.engine = engine if engine is not None else EngineAdapter()
         self.max_active = max_active
+        self.lane_log: list[tuple] = []
         n = getattr(self.engine, "n_lanes", 1)
         bounds = DEFAULT_LANE_BOUNDS if lane_bounds is None else tuple(lane_bounds)
         if len(bounds) < n - 1:
@@ -225,22 +248,25 @@ class Server:
         stop = threading.Event()
         all_done = threading.Event()
         results: dict[int, Result] = {}
-        slots = threading.Semaphore(self.max_active)
+        # active slots per lane (WBP requests count in their size's lane), so that large
+        # requests filling their lane's slots never hold back smaller ones
+        slots = [threading.Semaphore(self.max_active) for _ in range(n_lanes)]
         errors: list[BaseException] = []
         inflight = [0]  # admitted requests not yet completed (guarded by lock)
         lock = threading.Lock()
         n_total = len(requests)
+        self.lane_log = []
         if n_total == 0:
             return []
 
-        def finish(res: Result, hd):
+        def finish(res: Result, hd, req: Request):
             eng.destroy(hd)
             with lock:
                 inflight[0] -= 1
                 results[res.rid] = res
                 if len(results) == n_total:
                     all_done.set()
-            slots.release()
+            slots[lane_of(req, self.bounds)].release()
             freed.set()
 
         def fail(e: BaseException):
@@ -266,20 +292,27 @@ class Server:
                         continue
                     queues[lane_of(r, self.bounds)].append(r)
                 admitted = False
-                for q in queues:
+                for li, q in enumerate(queues):
                     if not q:
                         continue
-                    if not slots.acquire(blocking=False):
-                        break
+                    if not slots[li].acquire(blocking=False):
+                        continue
                     req = q[0]
+                    fits = getattr(eng, "fits", None)
+                    if fits is not None and not fits(req):
+                        with lock:
+                            alone = inflight[0] == 0
+                        if not alone:  # HBM short for this head: try the next lane
+                            slots[li].release()
+                            continue
                     try:
                         hd = eng.create(req)
                     except BaseException as e:  # surfaced to the caller
-                        slots.release()
+                        slots[li].release()
                         fail(e)
                         return
                     if hd is None:  # HBM short for this head: try the next lane
-                        slots.release()
+                        slots[li].release()
                         with lock:
                             alone = inflight[0] == 0
                         if alone:  # nothing running will free memory: the request can never fit
@@ -310,7 +343,7 @@ class Server:
                     eng.run_wbp(hd, req)
                     vol = eng.read_volume(hd, req) if req.keep_volume else None
                     finish(Result(req.rid, req.kind, req.arrival * time_scale, adm, now(), req.updates(), [], vol,
-                                  req.W, -1), hd)
+                                  req.W, -1), hd, req)
                 except BaseException as e:
                     fail(e)
                     return
@@ -332,8 +365,11 @@ class Server:
                     if dirty:
                         eng.set_members([a[1] for a in active], lane=li)
                         dirty = False
+                    t_it = now()
                     err = eng.iterate([a[1] for a in active], [a[0] for a in active], [a[3] for a in active],
                                       lane=li)
+                    self.lane_log.append((li, t_it, now(), len(active),
+                                          sum(a[0].updates_per_iteration() for a in active)))
                     done = []
                     for a, e in zip(active, err):
                         a[3] += 1
@@ -351,7 +387,7 @@ class Server:
                         for a in done:
                             req = a[0]
                             finish(Result(req.rid, req.kind, req.arrival * time_scale, a[2], t_done, req.updates(),
-                                          a[4], vols[id(a)], req.W, li), a[1])
+                                          a[4], vols[id(a)], req.W, li), a[1], req)
             except BaseException as e:
                 fail(e)
 
@@ -373,6 +409,20 @@ class Server:
             for th in threads:
                 th.join(timeout=30)
         return [results[r.rid] for r in requests]
+
+
+def lane_summary(lane_log: list, span: float) -> dict:
+    """Per lane: iterations, fraction of the span with an iteration in flight, mean members,
+    mean seconds per iteration and voxel-updates/s while iterating."""
+    out = {}
+    for li in sorted({x[0] for x in lane_log}):
+        xs = [x for x in lane_log if x[0] == li]
+        busy = sum(x[2] - x[1] for x in xs)
+        out[str(li)] = {"iterations": len(xs), "busy_fraction": busy / span if span > 0 else 0.0,
+                        "mean_members": float(np.mean([x[3] for x in xs])),
+                        "mean_iteration_s": busy / len(xs),
+                        "voxel_updates_per_s_while_busy": sum(x[4] for x in xs) / busy if busy > 0 else 0.0}
+    return out
 
 
 def _pcts(res: list) -> dict:
@@ -485,10 +535,15 @@ class CostModel:
 
 def request_bytes(req: Request) -> int:
     """Device bytes of a request's handle, as the engine allocates them (volume in its storage
-    type, the series, three projection-sized work buffers, the per-tilt tables)."""
+    type, the series, three projection-sized work buffers, the per-tilt tables; a TVM
+    request adds its TV scratch: six FP32 volumes of dual variables, and an FP32 copy of a
+    16-bit volume)."""
     N, h, w = req.series.shape
-    vol = req.W * req.H * req.D * (4 if req.precision == _abi.PREC_FP32 else 2)
-    return vol + 4 * N * h * w * 4 + 64 * N * w
+    nvox = req.W * req.H * req.D
+    red = req.precision != _abi.PREC_FP32
+    vol = nvox * (2 if red else 4)
+    tv = nvox * 4 * (7 if red else 6) if req.kind == TVM else 0
+    return vol + tv + 4 * N * h * w * 4 + 64 * N * w
 
 
 def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lane_bounds=DEFAULT_LANE_BOUNDS,
@@ -505,7 +560,7 @@ def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lan
     i_arr = 0
     waiting = [deque() for _ in range(n_lanes)]  # arrived, not admitted (FIFO per lane)
     used = 0.0
-    n_active = 0
+    n_active = [0] * n_lanes  # per lane, WBP requests in their size's lane
     joining = [[] for _ in range(n_lanes)]  # (ready time, req, admitted)
     members = [[] for _ in range(n_lanes)]  # [req, admitted, iterations done]
     work = [0.0] * n_lanes                  # GPU seconds left of the lane's current iteration
@@ -516,12 +571,12 @@ def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lan
     INF = float("inf")
 
     def admit():
-        nonlocal used, n_active
+        nonlocal used
         progress = True
-        while progress and n_active < max_active:
+        while progress:
             progress = False
-            for q in waiting:  # most urgent lane first; a head short of HBM lets the next lane try
-                if not q:
+            for li, q in enumerate(waiting):  # most urgent lane first; a head short of HBM lets the next lane try
+                if not q or n_active[li] >= max_active:
                     continue
                 r = q[0]
                 need = request_bytes(r)
@@ -531,7 +586,7 @@ def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lan
                     continue
                 q.popleft()
                 used += need
-                n_active += 1
+                n_active[li] += 1
                 ready = t + cost.upload_s(r)
                 if r.kind == WBP:
                     wbp_q.append((ready, r, t))
@@ -541,9 +596,9 @@ def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lan
                 break
 
     def release(r: Request):
-        nonlocal used, n_active
+        nonlocal used
         used -= request_bytes(r)
-        n_active -= 1
+        n_active[lane_of(r, bounds)] -= 1
 
     def start_iterations():
         for li in range(n_lanes):
