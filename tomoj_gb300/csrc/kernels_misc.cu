@@ -312,50 +312,90 @@ __device__ __forceinline__ float tv_u_point(const float* f, const float* __restr
 }
 
 constexpr int kTvX = 32, kTvY = 8, kTvZ = 32;  // CTA: 32 x 8 columns, marching 32 planes
+// One thread per element of the tile and its +x / +y halo (33 x 9): every u of a plane is
+// one thread's, computed once.  A thread keeps its column's p_k of the current plane in
+// registers (the update reads them, and pz of the plane is the next plane's -z neighbour),
+// so a plane costs it f, px, py, pz and the -x / -y neighbours (L1 hits of the adjacent
+// threads' loads).
+constexpr int kTvFX = kTvX + 1, kTvFY = kTvY + 1, kTvThreads = kTvFX * kTvFY;
 
 // One inner step: p_b = updateP(u_a, p_a) with u_a = updateU(f, p_a); FIRST: p_a = 0, u_a = f.
 template <bool FIRST>
-__global__ void __launch_bounds__(kTvX * kTvY) tv_step_kernel(const float* __restrict__ f, const float* __restrict__ pxa,
+__global__ void __launch_bounds__(kTvThreads) tv_step_kernel(const float* __restrict__ f, const float* __restrict__ pxa,
                                                            const float* __restrict__ pya, const float* __restrict__ pza,
                                                            float* __restrict__ pxb, float* __restrict__ pyb,
                                                            float* __restrict__ pzb, int W, int H, int D, float theta,
                                                            float g, float dt) {
-    __shared__ float us[2][kTvY + 1][kTvX + 1];  // u of planes z and z + 1 over the tile and its +x / +y halo
-    const int tx = threadIdx.x % kTvX, ty = threadIdx.x / kTvX;
-    const int x0 = blockIdx.x * kTvX, y0 = blockIdx.y * kTvY, z0 = blockIdx.z * kTvZ;
-    const int z1 = min(z0 + kTvZ, D);
+    __shared__ float us[2][kTvFY][kTvFX];  // u of planes z and z + 1 over the tile and its halo
+    const int lx = threadIdx.x % kTvFX, ly = threadIdx.x / kTvFX;
+    const int x = blockIdx.x * kTvX + lx, y = blockIdx.y * kTvY + ly;
+    const int z0 = blockIdx.z * kTvZ, z1 = min(z0 + kTvZ, D);
     const size_t WH = (size_t)W * H;
-    auto fill = [&](int b, int z) {
-        for (int e = threadIdx.x; e < (kTvY + 1) * (kTvX + 1); e += kTvX * kTvY) {
-            const int ly = e / (kTvX + 1), lx = e - ly * (kTvX + 1);
-            const int x = x0 + lx, y = y0 + ly;
-            float v = 0.0f;
-            if (x < W && y < H) {
-                const size_t o = (size_t)z * WH + (size_t)y * W + x;
-                v = FIRST ? f[o] : tv_u_point(f, pxa, pya, pza, o, x, y, z, W, H, D, theta);
-            }
-            us[b][ly][lx] = v;
-        }
-    };
-    fill(0, z0);
-    const int x = x0 + tx, y = y0 + ty;
+    const bool in = x < W && y < H;
+    const bool inner = in && lx < kTvX && ly < kTvY;  // writes p_b
     const float k = dt / theta;
+    // A plane's inputs are loaded one iteration before its u is computed, so the loads
+    // overlap the update of the plane before.
+    struct In {
+        float f, px, py, pz, pxm, pym;  // pxm / pym: the -x / -y neighbours' p (0 where unused)
+    };
+    auto load = [&](int z) -> In {
+        In v{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (!in) return v;
+        const size_t o = (size_t)z * WH + (size_t)y * W + x;
+        v.f = f[o];
+        if (!FIRST) {
+            v.px = pxa[o];
+            v.py = pya[o];
+            v.pz = pza[o];
+            if (x > 0 && x < W - 1) v.pxm = pxa[o - 1];
+            if (y > 0 && y < H - 1) v.pym = pya[o - W];
+        }
+        return v;
+    };
+    // pz of this column at the plane before the one whose u is computed next
+    float pzm = 0.0f;
+    if (!FIRST && in && z0 > 0 && z0 < D - 1) pzm = pza[(size_t)(z0 - 1) * WH + (size_t)y * W + x];
+    // u from loaded inputs (updateU's expressions and order, as tv_u_point)
+    auto u_of = [&](const In& v, int z) -> float {
+        if (!in) return 0.0f;
+        if (FIRST) return v.f;
+        float div;
+        if (x == 0) div = v.px;
+        else if (x == W - 1) div = -v.px;
+        else div = v.px - v.pxm;
+        if (y == 0) div += v.py;
+        else if (y == H - 1) div += -v.py;
+        else div += v.py - v.pym;
+        if (z == 0) div += v.pz;
+        else if (z == D - 1) div += -v.pz;
+        else div += v.pz - pzm;
+        pzm = v.pz;
+        return v.f - theta * div;
+    };
+    In c = load(z0);                             // plane z0
+    In nx = z0 + 1 < D ? load(z0 + 1) : c;      // plane z0 + 1, in flight
+    us[0][ly][lx] = u_of(c, z0);
     int cur = 0;
     for (int z = z0; z < z1; z++) {
-        if (z + 1 < D) fill(cur ^ 1, z + 1);
+        const float cpx = c.px, cpy = c.py, cpz = c.pz;  // p_a at (x, y, z)
+        if (z + 1 < D) {
+            us[cur ^ 1][ly][lx] = u_of(nx, z + 1);
+            c = nx;
+            if (z + 2 < D && z + 1 < z1) nx = load(z + 2);
+        }
         __syncthreads();
-        if (x < W && y < H) {
+        if (inner) {
             const size_t o = (size_t)z * WH + (size_t)y * W + x;
-            const float u0 = us[cur][ty][tx];
-            const float duy = (y < H - 1) ? us[cur][ty + 1][tx] - u0 : 0.0f;
-            const float dux = (x < W - 1) ? us[cur][ty][tx + 1] - u0 : 0.0f;
-            const float duz = (z < D - 1) ? us[cur ^ 1][ty][tx] - u0 : 0.0f;
+            const float u0 = us[cur][ly][lx];
+            const float duy = (y < H - 1) ? us[cur][ly + 1][lx] - u0 : 0.0f;
+            const float dux = (x < W - 1) ? us[cur][ly][lx + 1] - u0 : 0.0f;
+            const float duz = (z < D - 1) ? us[cur ^ 1][ly][lx] - u0 : 0.0f;
             const float s = duy * duy + dux * dux + duz * duz;
             const float dd1 = 1.0f + dt / theta / g * fabsf(__fsqrt_rn(s));
-            const float ox = FIRST ? 0.0f : pxa[o], oy = FIRST ? 0.0f : pya[o], oz = FIRST ? 0.0f : pza[o];
-            pxb[o] = __fdiv_rn(ox - k * dux, dd1);
-            pyb[o] = __fdiv_rn(oy - k * duy, dd1);
-            pzb[o] = __fdiv_rn(oz - k * duz, dd1);
+            pxb[o] = __fdiv_rn(cpx - k * dux, dd1);
+            pyb[o] = __fdiv_rn(cpy - k * duy, dd1);
+            pzb[o] = __fdiv_rn(cpz - k * duz, dd1);
         }
         __syncthreads();
         cur ^= 1;
@@ -767,11 +807,11 @@ cudaError_t launch_tv_step(const float* f, const float* const pa[3], float* cons
                            int D, float theta, float g, float dt, cudaStream_t s) {
     dim3 grid((W + kTvX - 1) / kTvX, (H + kTvY - 1) / kTvY, (D + kTvZ - 1) / kTvZ);
     if (first)
-        tv_step_kernel<true><<<grid, kTvX * kTvY, 0, s>>>(f, pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], W, H, D, theta,
-                                                          g, dt);
+        tv_step_kernel<true><<<grid, kTvThreads, 0, s>>>(f, pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], W, H, D, theta,
+                                                         g, dt);
     else
-        tv_step_kernel<false><<<grid, kTvX * kTvY, 0, s>>>(f, pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], W, H, D, theta,
-                                                           g, dt);
+        tv_step_kernel<false><<<grid, kTvThreads, 0, s>>>(f, pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], W, H, D, theta,
+                                                          g, dt);
     count_launch();
     return cudaGetLastError();
 }
