@@ -491,6 +491,7 @@ def run_engine(args, wl):
     batched = run_batched_leg(lib, args) if want(args, "batched") else None
     serving = run_serving_leg(args) if want(args, "serving") else None
     precision = run_precision_leg(lib, args) if want(args, "precision") else None
+    tv = run_tv_leg(lib, args) if want(args, "tv") else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": world, "steps": args.steps,
@@ -501,7 +502,7 @@ def run_engine(args, wl):
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps, "phases_s": phase},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
             "row_streams": row_leg, "compressed_sensing": cs_leg, "config1_full": config1, "batched": batched,
-            "serving": serving, "precision": precision,
+            "serving": serving, "precision": precision, "tv_denoise": tv,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)
@@ -668,6 +669,44 @@ def run_batched_leg(lib, args):
     out["persistent_speedup_vs_one_by_one"] = out["persistent"]["voxel_updates_per_s"] / one
     out["fp16_speedup_vs_one_by_one"] = out["fp16"]["voxel_updates_per_s"] / one
     out["inputs_s"] = time.time() - t_in
+    return out
+
+
+def run_tv_leg(lib, args):
+    """The TV denoise of a TVM iteration (TVMProjector3D.endOfIteration: 5 inner steps,
+    theta 25, g 1, dt = lambda = 0.01) timed alone with CUDA events on a args.tv_size volume of
+    uniform random values, FP32 and FP16 storage (16-bit: unpack and pack included), with the
+    inner step's algorithmic DRAM rate (28 B per voxel: f and p read, p written)."""
+    import torch
+    from tomoj_gb300 import _abi
+    W, H, D = args.tv_size
+    stream = torch.cuda.current_stream()
+    out = {"volume": f"{W}x{H}x{D}", "inner_steps": 5}
+    for name, prec in (("fp32", _abi.PREC_FP32), ("fp16", _abi.PREC_FP16)):
+        g = _abi.make_geom(W, H, D, W, H, 3)
+        prm = _abi.make_params(precision=prec)
+        h = C.c_void_p()
+        _abi.check(lib.tomo_create(C.byref(g), C.byref(prm), C.byref(h)))
+        try:
+            _abi.check(lib.tomo_set_stream(h, C.c_void_p(stream.cuda_stream)))
+            vol = torch.rand((D, H, W), device="cuda", dtype=torch.float32, generator=torch.Generator("cuda").manual_seed(5))
+            _abi.check(lib.tomo_set_volume(h, C.c_void_p(vol.data_ptr()), 1, 0, H))
+            del vol
+            _abi.check(lib.tomo_set_tvm(h, 25.0, 1.0, 0.01, 5))
+            _abi.check(lib.tomo_end_iteration(h))  # warm-up
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 3
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                _abi.check(lib.tomo_end_iteration(h))
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out[name] = {"ms_per_denoise": ms, "step_GBs_upper_bound": 28.0 * W * H * D * 5 / (ms / 1000.0) / 1e9}
+        finally:
+            lib.tomo_destroy(h)
+            torch.cuda.empty_cache()
     return out
 
 
@@ -1059,7 +1098,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the batched, serving and precision legs")
     ap.add_argument("--legs", default="all",
                     help="comma list of extra legs to run: row_streams, compressed_sensing, config1, batched, "
-                         "serving, precision (default all)")
+                         "serving, precision, tv (default all)")
+    ap.add_argument("--tv-size", type=int, nargs=3, default=[2048, 512, 2048], metavar=("W", "H", "D"),
+                    help="volume of the TV denoise leg")
     ap.add_argument("--serve-requests", type=int, default=128)
     ap.add_argument("--prec-size", type=int, nargs=3, default=[2048, 512, 2048], metavar=("W", "H", "D"),
                     help="volume of the reduced-precision leg")

@@ -54,6 +54,12 @@ struct tomo_batch {
     struct RedSeg {
         int s, off, n, maxT;
     };
+    struct VolSeg {  // the 16-bit members with an update s (slab-scale passes)
+        int s, off, n, maxH;
+    };
+    std::vector<VolSeg> vol_segs;
+    VolJob* d_vjobs = nullptr;
+    size_t cap_vjobs = 0;
     // persistent launches: one per (s, block size, chunk depth) for the forward phase and
     // per (s, flags, storage type, row pairs) for the backprojection; cursor: its slot of
     // d_cursor, zeroed at the start of every iteration
@@ -171,6 +177,7 @@ tomo_status build_plan(tomo_batch* b) {
     std::map<std::tuple<int, int, int, int, int>, std::vector<double>> fpcost, bpcost;  // per item, persistent
     std::map<std::tuple<int, int, int, int, int>, std::vector<int>> fpclass;  // kernel body of a persistent item
     std::map<int, std::vector<ErrReduce>> reds;
+    std::map<int, std::vector<VolJob>> vjobs;
     b->max_nsub = 0;
     b->has_fista = false;
     const int tx = bp_tile_x(), tz = bp_tile_z();
@@ -242,6 +249,8 @@ tomo_status build_plan(tomo_batch* b) {
                     }
                 }
             reds[s].push_back(ErrReduce{a.errpart, p->d_err + slot, T, g.h});
+            if (p->vtype != kVolF32)
+                vjobs[s].push_back(VolJob{p->vol(), p->d_vscale, p->d_vmax, p->vtype, g.W, g.H, g.D, p->d_status});
             BpLaunch c{};
             c.vol = p->bp_target();
             c.vtype = p->bayes ? kVolF32 : p->vtype;
@@ -337,6 +346,17 @@ tomo_status build_plan(tomo_batch* b) {
         bp_all.insert(bp_all.end(), kv.second.begin(), kv.second.end());
     }
     BCKS(ensure(&b->d_cursor, &b->cap_cursor, (size_t)std::max(b->n_cursor, 1), b->stream));
+    std::vector<VolJob> vall;
+    b->vol_segs.clear();
+    for (auto& kv : vjobs) {
+        int maxH = 0;
+        for (auto& j : kv.second) maxH = std::max(maxH, j.H);
+        b->vol_segs.push_back(tomo_batch::VolSeg{kv.first, (int)vall.size(), (int)kv.second.size(), maxH});
+        vall.insert(vall.end(), kv.second.begin(), kv.second.end());
+    }
+    BCKS(ensure(&b->d_vjobs, &b->cap_vjobs, std::max<size_t>(vall.size(), 1), b->stream));
+    if (!vall.empty())
+        BCK(cudaMemcpyAsync(b->d_vjobs, vall.data(), sizeof(VolJob) * vall.size(), cudaMemcpyHostToDevice, b->stream));
     for (auto& kv : reds) {
         int maxT = 0;
         for (auto& r : kv.second) maxT = std::max(maxT, r.T);
@@ -413,10 +433,9 @@ tomo_status launch_step(tomo_batch* b) {
                 BCK(launch_fp_batch(sg.qp, sg.nt, b->d_fp, b->d_fp_items + sg.off, sg.n, sg.zc, sg.smem, sg.pk, b->stream));
         for (auto& sg : b->red_segs)
             if (sg.s == s) BCK(launch_reduce_err_batch(b->d_red + sg.off, sg.n, sg.maxT, b->stream));
-        // storage hooks of the members that have an update s
-        auto in_s = [&](size_t m) { return s * b->upd[m] < b->members[m]->g.N; };
-        for (size_t m = 0; m < b->members.size(); m++)
-            if (in_s(m)) BCKS(handle_bp_pre(b->members[m], b->stream));
+        // slab-scale passes of the 16-bit members that have an update s, one launch each
+        for (auto& vs : b->vol_segs)
+            if (vs.s == s) BCK(launch_vol_hooks_batch(b->d_vjobs + vs.off, vs.n, vs.maxH, true, b->stream));
         std::vector<std::function<cudaError_t(cudaStream_t)>> bjobs;
         for (auto& sg : b->bp_psegs)
             if (sg.s == s)
@@ -429,8 +448,8 @@ tomo_status launch_step(tomo_batch* b) {
             if (sg.s == s)
                 BCK(launch_bp_batch(sg.sanitize, sg.pos, sg.vt, sg.pairs, b->d_bp, b->d_bp_items + sg.off, sg.n,
                                     b->stream));
-        for (size_t m = 0; m < b->members.size(); m++)
-            if (in_s(m)) BCKS(handle_bp_post(b->members[m], b->stream));
+        for (auto& vs : b->vol_segs)
+            if (vs.s == s) BCK(launch_vol_hooks_batch(b->d_vjobs + vs.off, vs.n, vs.maxH, false, b->stream));
     }
     for (tomo_projector* p : b->members) BCKS(handle_end_iteration(p));
     return TOMO_OK;
@@ -498,7 +517,7 @@ tomo_status tomo_batch_destroy(tomo_batch* b) {
     cudaStreamSynchronize(b->stream);
     drop_graph(b);
     for (void* q : {(void*)b->d_fp, (void*)b->d_bp, (void*)b->d_red, (void*)b->d_fp_items, (void*)b->d_bp_items,
-                    (void*)b->d_cursor})
+                    (void*)b->d_cursor, (void*)b->d_vjobs})
         if (q) pool_free(q, b->stream);
     cudaStreamSynchronize(b->stream);
     for (cudaStream_t q : b->aux) {

@@ -87,9 +87,9 @@ __global__ void unpack_kernel(const uint16_t* __restrict__ vol, const float* __r
 
 // One CTA per volume row: re-scales the row when its max left the band.
 template <int VT>
-__global__ void rescale_kernel(uint16_t* __restrict__ vol, float* __restrict__ vscale,
-                               const unsigned* __restrict__ vmax, int W, int H, int D, int* status) {
-    const int r = blockIdx.x;
+__device__ __forceinline__ void rescale_row(uint16_t* __restrict__ vol, float* __restrict__ vscale,
+                                            const unsigned* __restrict__ vmax, int W, int H, int D, int* status,
+                                            int r) {
     const float m = __uint_as_float(vmax[r]), M = __uint_as_float(vmax[H]);
     const float s = vscale[r];
     if (!slab_needs_rescale(m, s, M)) return;
@@ -108,6 +108,36 @@ __global__ void rescale_kernel(uint16_t* __restrict__ vol, float* __restrict__ v
     }
     __syncthreads();
     if (threadIdx.x == 0) vscale[r] = ns;
+}
+
+template <int VT>
+__global__ void rescale_kernel(uint16_t* __restrict__ vol, float* __restrict__ vscale,
+                               const unsigned* __restrict__ vmax, int W, int H, int D, int* status) {
+    rescale_row<VT>(vol, vscale, vmax, W, H, D, status, blockIdx.x);
+}
+
+// Batched forms over many volumes (a batch's 16-bit members): CTA y works on volume
+// jobs[y]; the same per-volume passes, one launch each for all of them.
+__global__ void vmax_total_batch_kernel(const VolJob* __restrict__ jobs) {
+    __shared__ float red[kThreads / 32];
+    const VolJob j = jobs[blockIdx.x];
+    float m = 0.0f;
+    for (int r = threadIdx.x; r < j.H; r += kThreads) m = fmaxf(m, __uint_as_float(j.vmax[r]));
+    m = block_max(m, red);
+    if (threadIdx.x == 0) j.vmax[j.H] = __float_as_uint(m);
+}
+
+__global__ void rescale_batch_kernel(const VolJob* __restrict__ jobs) {
+    const VolJob j = jobs[blockIdx.y];
+    if ((int)blockIdx.x >= j.H) return;
+    uint16_t* v = static_cast<uint16_t*>(j.vol);
+    if (j.vtype == kVolBF16) rescale_row<kVolBF16>(v, j.vscale, j.vmax, j.W, j.H, j.D, j.status, blockIdx.x);
+    else rescale_row<kVolF16>(v, j.vscale, j.vmax, j.W, j.H, j.D, j.status, blockIdx.x);
+}
+
+__global__ void vmax_zero_batch_kernel(const VolJob* __restrict__ jobs) {
+    const VolJob j = jobs[blockIdx.x];
+    for (int r = threadIdx.x; r < j.H; r += kThreads) j.vmax[r] = 0u;
 }
 
 template <int VT>
@@ -203,6 +233,18 @@ cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, unsigned* vm
     else
         return cudaErrorInvalidValue;
     count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vol_hooks_batch(const VolJob* jobs, int n_jobs, int max_H, bool before, cudaStream_t s) {
+    if (n_jobs <= 0) return cudaSuccess;
+    vmax_total_batch_kernel<<<n_jobs, kThreads, 0, s>>>(jobs);
+    rescale_batch_kernel<<<dim3(max_H, n_jobs), kThreads, 0, s>>>(jobs);
+    count_launch(2);
+    if (before) {
+        vmax_zero_batch_kernel<<<n_jobs, kThreads, 0, s>>>(jobs);
+        count_launch();
+    }
     return cudaGetLastError();
 }
 

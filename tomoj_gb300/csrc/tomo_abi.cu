@@ -572,8 +572,6 @@ tomo_status handle_need_series(tomo_projector* p) { return need_series(p); }
 tomo_status handle_start_iteration(tomo_projector* p) { return start_iteration(p); }
 tomo_status handle_end_iteration(tomo_projector* p) { return end_iteration(p); }
 int handle_tilts_per_cta(const tomo_projector* p, int T) { return auto_tilts_per_cta(p, T, 0); }
-tomo_status handle_bp_pre(tomo_projector* p, cudaStream_t s) { return bp_pre(p, s); }
-tomo_status handle_bp_post(tomo_projector* p, cudaStream_t s) { return bp_post(p, s); }
 }  // namespace tomo
 
 extern "C" {

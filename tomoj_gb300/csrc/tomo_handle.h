@@ -147,8 +147,4 @@ tomo_status handle_need_series(tomo_projector* p);
 tomo_status handle_start_iteration(tomo_projector* p);
 tomo_status handle_end_iteration(tomo_projector* p);
 int handle_tilts_per_cta(const tomo_projector* p, int T);
-// Reduced-precision bookkeeping around a backprojection: zero the row maxima before,
-// re-scale the slabs that left their band after.
-tomo_status handle_bp_pre(tomo_projector* p, cudaStream_t s);
-tomo_status handle_bp_post(tomo_projector* p, cudaStream_t s);
 }  // namespace tomo

@@ -349,6 +349,17 @@ cudaError_t launch_vol_unpack(const void* vol, int vtype, const float* vscale, i
 // rows whose maximum left the band as well).
 cudaError_t launch_vol_rescale(void* vol, int vtype, float* vscale, unsigned* vmax, int W, int H, int D,
                                int* status, cudaStream_t s);
+// The slab-scale passes around a backprojection for many 16-bit volumes in one launch each
+// (a batch's members): before (rows under the floor raised, row maxima zeroed) or after (rows
+// whose maximum left the band re-scaled); the same per-volume work as launch_vol_rescale.
+struct VolJob {
+    void* vol;
+    float* vscale;
+    unsigned* vmax;
+    int vtype, W, H, D;
+    int* status;
+};
+cudaError_t launch_vol_hooks_batch(const VolJob* jobs, int n_jobs, int max_H, bool before, cudaStream_t s);
 // Fills the volume with `value`: scales, row maxima and the volume's maximum follow.
 cudaError_t launch_vol_fill(void* vol, int vtype, float* vscale, unsigned* vmax, size_t nvox, int H, float value,
                             cudaStream_t s);
