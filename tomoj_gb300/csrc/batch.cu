@@ -25,6 +25,31 @@
 
 using namespace tomo;
 
+// Page-locked host staging of a batch's per-iteration orderings, residuals and status
+// words.  Copies from or to pageable memory go through the driver's staging path, where a
+// small copy of one lane waited behind the large series uploads of requests being
+// admitted on other threads.
+template <class T>
+struct Pinned {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        const size_t c = std::max<size_t>(std::max<size_t>(n, cap + cap / 2), 64);
+        cap = 0;
+        const cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p), c * sizeof(T), cudaHostAllocDefault);
+        if (e == cudaSuccess) cap = c;
+        else p = nullptr;
+        return e;
+    }
+    T& operator[](size_t i) { return p[i]; }
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 struct tomo_batch {
     std::vector<tomo_projector*> members;
     std::vector<int> upd;        // update size of each member in the cached plan
@@ -94,9 +119,9 @@ struct tomo_batch {
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     uint64_t graph_kernels = 0;
-    std::vector<int> host_orders;
-    std::vector<double> host_err;
-    std::vector<int> host_status;
+    Pinned<int> host_orders;
+    Pinned<double> host_err;
+    Pinned<int> host_status;
 };
 
 #ifdef TOMO_TRACE_BATCH
@@ -574,7 +599,9 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
     // orderings of this iteration into each member's batch buffer
     size_t total = 0;
     for (size_t m = 0; m < M; m++) total += b->members[m]->g.N;
-    b->host_orders.resize(total);
+    BCK(b->host_orders.reserve(total));
+    BCK(b->host_err.reserve(total));
+    BCK(b->host_status.reserve(M));
     size_t o = 0;
     for (size_t m = 0; m < M; m++) {
         tomo_projector* p = b->members[m];
@@ -621,8 +648,7 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
     // residuals and status words on the batch stream (a copy on the legacy default stream
     // waited for every other stream's work here: a small batch's iteration took as long as
     // a large batch's running beside it)
-    b->host_err.resize(total);
-    b->host_status.assign(M, 0);
+    for (size_t m = 0; m < M; m++) b->host_status[m] = 0;
     o = 0;
     for (size_t m = 0; m < M; m++) {
         tomo_projector* p = b->members[m];

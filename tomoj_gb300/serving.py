@@ -6,13 +6,14 @@ every admitted request's volume, series and residuals resident in HBM.
 
 * Admission (one host thread): requests queue in arrival order per lane (below);
   the head of the most urgent lane that fits is admitted when its lane has a free
-  active slot and the engine can allocate its buffers (tomo_create's admission by free
-  HBM, TOMO_ERR_NOMEM otherwise; handle buffers come from the engine's
+  active slot and the engine can allocate its buffers (a free-HBM check first,
+  leaving a per-lane headroom for more urgent lanes, then tomo_create's admission
+  by free HBM, TOMO_ERR_NOMEM otherwise; handle buffers come from the engine's
   stream-ordered pool, so a retired request's memory is reused without a
   device-wide synchronisation).  A large request waiting for HBM therefore does
   not hold back smaller ones; under sustained overload large requests wait
-  longest.  The series upload runs on this thread, beside the GPU work of the
-  running requests.
+  longest.  The series upload runs on the admission thread, beside the GPU work
+  of the running requests.
 * Iterative requests (SIRT, OS-SART, TVM) join a lane by the size of one of their
   iterations (voxel-updates).  Each lane is one batch (tomo_batch_iteration: one
   launch per kernel variant covers every member, the iteration replayed as a CUDA
@@ -22,8 +23,8 @@ every admitted request's volume, series and residuals resident in HBM.
   are dispatched first as SMs free up (measured: a 10.5 ms iteration of five
   512^2 series takes 10.9 ms beside a 2048^2 x 512 iteration of 200 ms).  Requests join a lane between two of its
   iterations and leave when their last iteration is done.
-* WBP requests (one weighted backprojection) run on a worker thread, each on its
-  handle's own stream at the most urgent priority.
+* WBP requests (one weighted backprojection) run on a worker thread per lane, each
+  on its handle's own stream at the most urgent priority.
 
 Reported: per request time-to-reconstruction (completion - arrival), p50/p99 over
 all requests and per method and size, aggregate voxel-updates/s, and the offered
@@ -108,6 +109,7 @@ class Result:
     volume: np.ndarray | None = None
     size: int = 0
     lane: int = -1               # -1: WBP worker
+    create_s: float = 0.0        # handle creation and series upload
 
     @property
     def latency(self) -> float:
@@ -142,14 +144,15 @@ class EngineAdapter:
             self.lib.tomo_batch_destroy(b)
         self.batches = []
 
-    def fits(self, req: Request) -> bool:
+    def fits(self, req: Request, headroom: float = 0.0) -> bool:
         """Whether free HBM (with the engine pool's idle blocks) holds the request's estimated
-        footprint: a cheap test before tomo_create, which would otherwise allocate and
-        release most of a request that cannot be admitted yet."""
+        footprint and still leaves `headroom` (a fraction of the device's HBM): a cheap test
+        before tomo_create, which would otherwise allocate and release most of a request
+        that cannot be admitted yet."""
         free, total = C.c_uint64(), C.c_uint64()
         if self.lib.tomo_device_memory(C.byref(free), C.byref(total)) != _abi.OK:
             return True
-        return request_bytes(req) <= free.value
+        return request_bytes(req) + headroom * total.value <= free.value
 
     def create(self, req: Request):
         """Handle with the request's series loaded; None if HBM is short (TOMO_ERR_NOMEM)."""
@@ -221,8 +224,10 @@ class EngineAdapter:
 
 
 class Server:
-    def __init__(self, engine=None, max_active: int = 64, lane_bounds=None):
-        """max_active: active requests per lane.  After run(), `lane_log` holds one
+    def __init__(self, engine=None, max_active: int = 64, lane_bounds=None, headroom=None):
+        """max_active: active requests per lane.  headroom: per lane, the fraction of HBM its
+        admissions must leave free for more urgent lanes (default 0 for the most urgent lane,
+        0.05 for the next, 0.15 for the others).  After run(), `lane_log` holds one
         (lane, start, end, members, voxel-updates) tuple per batched iteration."""
         self.engine = engine if engine is not None else EngineAdapter()
         self.max_active = max_active
@@ -232,6 +237,8 @@ class Server:
         if len(bounds) < n - 1:
             raise ValueError(f"{n} lanes need {n - 1} lane bounds")
         self.bounds = tuple(bounds[:n - 1])
+        self.headroom = tuple(headroom) if headroom is not None else tuple(
+            0.0 if i == 0 else 0.05 if i == 1 else 0.15 for i in range(n))
 
     def run(self, requests: list[Request], time_scale: float = 1.0) -> list[Result]:
         """Serve `requests` (arrival times scaled by time_scale) to completion."""
@@ -241,13 +248,14 @@ class Server:
         now = lambda: time.perf_counter() - t0  # noqa: E731
         pending = [(r.arrival * time_scale, r.rid, r) for r in requests]
         heapq.heapify(pending)
-        arrived: queue.Queue = queue.Queue()      # arrived, not yet admitted (FIFO)
+        arrived = [queue.Queue() for _ in range(n_lanes)]  # per lane: arrived, not yet admitted (FIFO)
         inbox = [queue.Queue() for _ in range(n_lanes)]
-        wbp_q: queue.Queue = queue.Queue()
-        freed = threading.Event()
+        wbp_q = [queue.Queue() for _ in range(n_lanes)]
+        freed = [threading.Event() for _ in range(n_lanes)]  # a completion: admitters retry
         stop = threading.Event()
         all_done = threading.Event()
         results: dict[int, Result] = {}
+        created: dict[int, float] = {}
         # active slots per lane (WBP requests count in their size's lane), so that large
         # requests filling their lane's slots never hold back smaller ones
         slots = [threading.Semaphore(self.max_active) for _ in range(n_lanes)]
@@ -260,6 +268,7 @@ class Server:
             return []
 
         def finish(res: Result, hd, req: Request):
+            res.create_s = created.get(res.rid, 0.0)
             eng.destroy(hd)
             with lock:
                 inflight[0] -= 1
@@ -267,7 +276,8 @@ class Server:
                 if len(results) == n_total:
                     all_done.set()
             slots[lane_of(req, self.bounds)].release()
-            freed.set()
+            for ev in freed:
+                ev.set()
 
         def fail(e: BaseException):
             errors.append(e)
@@ -276,21 +286,20 @@ class Server:
         def admitter():
             # one FIFO per lane (WBP requests by their size too); the most urgent lane whose
             # head fits is admitted first, so small requests are not held behind a large one
-            # that waits for HBM
+            # that waits for HBM.  One thread: concurrent series uploads slowed each other
+            # (measured: 0.5 s median creation of a 512^2 request with one admission thread
+            # per lane, p50 over all requests 18 s instead of 9.6 s).
             queues = [deque() for _ in range(n_lanes)]
             while not stop.is_set():
-                while True:
-                    try:
-                        r = arrived.get_nowait()
-                    except queue.Empty:
-                        break
-                    queues[lane_of(r, self.bounds)].append(r)
+                for li in range(n_lanes):
+                    while True:
+                        try:
+                            queues[li].append(arrived[li].get_nowait())
+                        except queue.Empty:
+                            break
                 if not any(queues):
-                    try:
-                        r = arrived.get(timeout=0.01)
-                    except queue.Empty:
-                        continue
-                    queues[lane_of(r, self.bounds)].append(r)
+                    time.sleep(0.002)
+                    continue
                 admitted = False
                 for li, q in enumerate(queues):
                     if not q:
@@ -299,12 +308,12 @@ class Server:
                         continue
                     req = q[0]
                     fits = getattr(eng, "fits", None)
-                    if fits is not None and not fits(req):
-                        with lock:
-                            alone = inflight[0] == 0
-                        if not alone:  # HBM short for this head: try the next lane
-                            slots[li].release()
-                            continue
+                    with lock:
+                        alone = inflight[0] == 0
+                    if fits is not None and not alone and not fits(req, self.headroom[li]):
+                        slots[li].release()  # HBM short for this head: try the next lane
+                        continue
+                    t_create = time.perf_counter()
                     try:
                         hd = eng.create(req)
                     except BaseException as e:  # surfaced to the caller
@@ -319,24 +328,25 @@ class Server:
                             fail(_abi.NoMemoryError(-3, f"request {req.rid} does not fit in free HBM"))
                             return
                         continue
+                    created[req.rid] = time.perf_counter() - t_create
                     q.popleft()
                     with lock:
                         inflight[0] += 1
                     item = (req, hd, now())
                     if req.kind == WBP:
-                        wbp_q.put(item)
+                        wbp_q[li].put(item)
                     else:
-                        inbox[lane_of(req, self.bounds)].put(item)
+                        inbox[li].put(item)
                     admitted = True
                     break  # start again from the most urgent lane
                 if not admitted:
-                    freed.clear()
-                    freed.wait(0.02)  # wait for a completion (or a new arrival)
+                    freed[0].clear()
+                    freed[0].wait(0.02)  # wait for a completion (or a new arrival)
 
-        def wbp_worker():
+        def wbp_worker(li: int):
             while not stop.is_set():
                 try:
-                    req, hd, adm = wbp_q.get(timeout=0.01)
+                    req, hd, adm = wbp_q[li].get(timeout=0.01)
                 except queue.Empty:
                     continue
                 try:
@@ -391,15 +401,18 @@ class Server:
             except BaseException as e:
                 fail(e)
 
-        threads = [threading.Thread(target=admitter, daemon=True), threading.Thread(target=wbp_worker, daemon=True)]
-        threads += [threading.Thread(target=lane_worker, args=(i,), daemon=True) for i in range(n_lanes)]
+        threads = [threading.Thread(target=admitter, daemon=True)]
+        for i in range(n_lanes):
+            threads += [threading.Thread(target=wbp_worker, args=(i,), daemon=True),
+                        threading.Thread(target=lane_worker, args=(i,), daemon=True)]
         for th in threads:
             th.start()
         try:
             while not all_done.is_set():
                 t = now()
                 while pending and pending[0][0] <= t:
-                    arrived.put(heapq.heappop(pending)[2])
+                    r = heapq.heappop(pending)[2]
+                    arrived[lane_of(r, self.bounds)].put(r)
                 wait = (pending[0][0] - now()) if pending else 0.05
                 all_done.wait(min(max(wait, 0.0005), 0.05))
             if errors:
@@ -433,7 +446,8 @@ def _pcts(res: list) -> dict:
     serv = np.array([r.completed - r.admitted for r in res], np.float64)
     return {"n": int(lat.size), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()), "wait_p50_s": float(np.percentile(wait, 50)),
-            "service_p50_s": float(np.percentile(serv, 50))}
+            "service_p50_s": float(np.percentile(serv, 50)),
+            "create_p50_s": float(np.percentile([r.create_s for r in res], 50))}
 
 
 def summarize(results: list[Result], wall_s: float | None = None, requests: list[Request] | None = None) -> dict:
