@@ -124,32 +124,10 @@ struct tomo_batch {
     Pinned<int> host_status;
 };
 
-#ifdef TOMO_TRACE_BATCH
-#include <chrono>
-#include <cstdio>
-#define TRACE_MARK(name) trace_mark(name)
-static thread_local std::chrono::steady_clock::time_point g_tr0;
-static thread_local char g_trbuf[512];
-static thread_local int g_trlen = 0;
-static void trace_mark(const char* name) {
-    const auto t = std::chrono::steady_clock::now();
-    if (name[0] == '<') {
-        g_tr0 = t;
-        g_trlen = 0;
-        return;
-    }
-    const double ms = std::chrono::duration<double, std::milli>(t - g_tr0).count();
-    g_trlen += snprintf(g_trbuf + g_trlen, sizeof(g_trbuf) - g_trlen, " %s=%.2f", name, ms);
-    if (name[0] == '>') fprintf(stderr, "[batch %p]%s\n", (void*)&g_tr0, g_trbuf);
-}
-#else
-#define TRACE_MARK(name) ((void)0)
-#endif
-
 namespace {
 
 // tomo_batch_set_persistent modes (1 = forward and backprojection persistent, longest first)
-constexpr int kPersistFp = 2, kPersistBp = 4, kPersistListOrder = 8, kPersistSerial = 16, kPersistFullGrid = 32;
+constexpr int kPersistFp = 2, kPersistBp = 4, kPersistListOrder = 8, kPersistSerial = 16;
 
 #define BCK(expr)                                                                              \
     do {                                                                                       \
@@ -347,7 +325,7 @@ tomo_status build_plan(tomo_batch* b) {
         if (std::get<1>(kv.first) < 0) {
             if (!(b->persistent & kPersistListOrder)) by_cost(kv.second, fpcost[kv.first], &fpclass[kv.first]);
             const int n = (int)kv.second.size();
-            const int grid = (b->persistent & kPersistFullGrid) ? n : std::min(n, (nt <= 256 ? 2 : 1) * sms);
+            const int grid = std::min(n, fp_ctas_per_sm(nt) * sms);
             b->fp_psegs.push_back(tomo_batch::FpPSeg{s, nt, zc, fpsmem[kv.first], (int)fp_all.size(), n,
                                                      b->n_cursor++, grid});
         } else {
@@ -530,7 +508,7 @@ tomo_status tomo_batch_set_stream(tomo_batch* b, void* stream) {
 tomo_status tomo_batch_set_persistent(tomo_batch* b, int32_t on) {
     if (!b) return handle_fail(TOMO_ERR_INVALID, "null batch");
     BCK(cudaStreamSynchronize(b->stream));
-    if (on < 0 || on > 63) return handle_fail(TOMO_ERR_INVALID, "persistent mode out of range");
+    if (on < 0 || on > 31) return handle_fail(TOMO_ERR_INVALID, "persistent mode out of range");
     b->persistent = on == 1 ? (kPersistFp | kPersistBp) : on;
     b->plan_valid = false;
     drop_graph(b);
@@ -577,10 +555,8 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
     if (!b || !relax || !update || !first) return handle_fail(TOMO_ERR_INVALID, "null argument");
     const size_t M = b->members.size();
     if (M == 0) return TOMO_OK;
-    TRACE_MARK("<");
     // the members' own streams must be idle: their buffers are used on the batch stream
     for (tomo_projector* p : b->members) BCK(cudaStreamSynchronize(p->stream));
-    TRACE_MARK("own");
     std::vector<int> upd(M);
     std::vector<double> fac(M);
     for (size_t m = 0; m < M; m++) {
@@ -595,7 +571,6 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
         b->factor = fac;
         BCKS(build_plan(b));
     }
-    TRACE_MARK("plan");
     // orderings of this iteration into each member's batch buffer
     size_t total = 0;
     for (size_t m = 0; m < M; m++) total += b->members[m]->g.N;
@@ -610,7 +585,6 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
                             b->stream));
         o += p->g.N;
     }
-    TRACE_MARK("orders");
     // the members' start/end-of-iteration work (TVM, FISTA) joins the batch stream
     std::vector<cudaStream_t> saved(M);
     for (size_t m = 0; m < M; m++) {
@@ -644,7 +618,6 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
     } else {
         BCKS(launch_step(b));
     }
-    TRACE_MARK("launch");
     // residuals and status words on the batch stream (a copy on the legacy default stream
     // waited for every other stream's work here: a small batch's iteration took as long as
     // a large batch's running beside it)
@@ -656,9 +629,7 @@ tomo_status tomo_batch_iteration(tomo_batch* b, const double* relax, const int32
         BCK(cudaMemcpyAsync(&b->host_status[m], p->d_status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
         o += p->g.N;
     }
-    TRACE_MARK("errcopy");
     BCK(cudaStreamSynchronize(b->stream));
-    TRACE_MARK(">sync");
     o = 0;
     for (size_t m = 0; m < M; m++) {
         tomo_projector* p = b->members[m];

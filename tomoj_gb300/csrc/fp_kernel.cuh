@@ -633,9 +633,6 @@ __device__ __noinline__ bool fp_item_call(const FpLaunch* a, int g0, int j, int 
 
 template <int NT, int ZC, int LQ>
 __device__ __forceinline__ bool fp_persist_item(const FpLaunch* a, int g0, int j, int use_tma, int lq, int pk) {
-#ifdef TOMO_PERSIST_ONE_BODY
-    if constexpr (NT == 256) return fp_item_call<256, 2, ZC, 0>(a, g0, j, use_tma);
-#endif
     if constexpr (LQ > FpPersistQP<NT>::hi) {
         return true;
     } else {
