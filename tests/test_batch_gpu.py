@@ -126,3 +126,40 @@ def test_persistent_launches_equal_per_variant_launches(engine, use_graph):
         assert np.array_equal(vols[0][m], vols[1][m]), m
         assert np.isfinite(vols[1][m]).all() and np.abs(vols[1][m]).max() > 0, m
     assert launches[1] < launches[0], launches
+
+
+def test_batch_stream_and_priority_do_not_change_results(engine):
+    """A batch on a caller's stream at a more urgent priority, and a handle whose own stream
+    was recreated at a priority, compute bitwise what the defaults compute."""
+    torch = pytest.importorskip("torch")
+    c = series_case(W=64, H=6, D=24, n=11, seed=41)
+    vols = []
+    for variant in (0, 1):
+        hs = [_prec_handle(engine, c, _abi.PREC_FP32) for _ in range(2)]
+        b = C.c_void_p()
+        _abi.check(engine.tomo_batch_create(C.byref(b)))
+        side = torch.cuda.Stream()
+        try:
+            if variant:
+                _abi.check(engine.tomo_batch_set_priority(b, 2))
+                _abi.check(engine.tomo_batch_set_stream(b, C.c_void_p(side.cuda_stream)))
+                _abi.check(engine.tomo_set_priority(hs[1], 1))
+            arr = (C.c_void_p * 1)(hs[0].value)
+            _abi.check(engine.tomo_batch_set(b, arr, 1))
+            rel, upd = np.ones(1), np.zeros(1, np.int32)
+            for it in range(2):
+                first = np.array([engine.tomo_first_index(3, it, c["n"])], np.int32)
+                _abi.check(engine.tomo_batch_iteration(b, _abi.ptr(rel, C.c_double), _abi.ptr(upd, C.c_int32),
+                                                       _abi.ptr(first, C.c_int32), 1, None))
+            _abi.check(engine.tomo_run_ossart(hs[1], 2, 1.0, 0, 3, 0, c["H"], 1, None))
+            out = []
+            for h in hs:
+                v = np.empty((c["D"], c["H"], c["W"]), np.float32)
+                _abi.check(engine.tomo_get_volume(h, v.ctypes.data, 0, 0, c["H"]))
+                out.append(v)
+            vols.append(out)
+        finally:
+            engine.tomo_batch_destroy(b)
+            for h in hs:
+                engine.tomo_destroy(h)
+    assert np.array_equal(vols[0][0], vols[1][0]) and np.array_equal(vols[0][1], vols[1][1])
