@@ -561,14 +561,17 @@ def request_bytes(req: Request) -> int:
 
 
 def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lane_bounds=DEFAULT_LANE_BOUNDS,
-             hbm_bytes: float = 2.6e11) -> list[Result]:
+             hbm_bytes: float = 2.6e11, headroom=None) -> list[Result]:
     """Replays the server's policy in virtual time: admission by slots and HBM from one FIFO
-    per lane, most urgent lane first (a request joins its work when its upload ends), lanes that iterate independently with strict
+    per lane, most urgent lane first, each lane leaving its headroom of HBM free for more
+    urgent ones (a request joins its work when its upload ends), lanes that iterate independently with strict
     priority on the GPU (smallest lane first; WBP requests above all lanes, one at a time), a
     member joining or leaving between two of its lane's iterations.  The GPU is shared as a
     fluid: the most urgent runnable job gets all of it."""
     bounds = tuple(lane_bounds)
     n_lanes = len(bounds) + 1
+    room = tuple(headroom) if headroom is not None else tuple(
+        0.0 if i == 0 else 0.05 if i == 1 else 0.15 for i in range(n_lanes))
     reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
     t = 0.0
     i_arr = 0
@@ -596,7 +599,7 @@ def simulate(requests: list[Request], cost: CostModel, max_active: int = 64, lan
                 need = request_bytes(r)
                 if need > hbm_bytes:
                     raise _abi.NoMemoryError(-3, f"request {r.rid} does not fit in HBM")
-                if used + need > hbm_bytes:
+                if used + need + room[li] * hbm_bytes > hbm_bytes and used > 0:
                     continue
                 q.popleft()
                 used += need
