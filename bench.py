@@ -348,6 +348,10 @@ def run_engine(args, wl):
     d2h = vol_pin.nbytes
     e2e_steps = max(1, min(args.steps, 3))
     phase = {"load_s": 0.0, "job_s": 0.0, "readback_s": 0.0}
+    # first use of the two pinned buffers outside the timed region (a reused staging
+    # buffer, as a caller keeps one)
+    load(series_pin)
+    _abi.check(lib.tomo_get_volume(h, vol_pin.ctypes.data, 0, 0, H))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
