@@ -251,7 +251,7 @@ class Server:
         arrived = [queue.Queue() for _ in range(n_lanes)]  # per lane: arrived, not yet admitted (FIFO)
         inbox = [queue.Queue() for _ in range(n_lanes)]
         wbp_q = [queue.Queue() for _ in range(n_lanes)]
-        freed = [threading.Event() for _ in range(n_lanes)]  # a completion: admitters retry
+        freed = threading.Event()  # a completion: the admitter retries
         stop = threading.Event()
         all_done = threading.Event()
         results: dict[int, Result] = {}
@@ -276,8 +276,7 @@ class Server:
                 if len(results) == n_total:
                     all_done.set()
             slots[lane_of(req, self.bounds)].release()
-            for ev in freed:
-                ev.set()
+            freed.set()
 
         def fail(e: BaseException):
             errors.append(e)
@@ -340,8 +339,8 @@ class Server:
                     admitted = True
                     break  # start again from the most urgent lane
                 if not admitted:
-                    freed[0].clear()
-                    freed[0].wait(0.02)  # wait for a completion (or a new arrival)
+                    freed.clear()
+                    freed.wait(0.02)  # wait for a completion (or a new arrival)
 
         def wbp_worker(li: int):
             while not stop.is_set():
