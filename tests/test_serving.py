@@ -195,3 +195,20 @@ def test_small_request_is_not_held_behind_a_large_one_waiting_for_memory():
     assert r1.admitted >= r0.completed - 1e-3     # the second large request waited for the first
     assert r2.admitted < r0.completed and r2.completed < r0.completed
     assert eng.refused > 0 and eng.used == 0
+
+
+def test_lane_summary_and_per_class_statistics():
+    from tomoj_gb300.serving import Result, lane_summary
+    log = [(0, 0.0, 0.5, 2, 1e9), (0, 1.0, 1.5, 1, 5e8), (1, 0.0, 2.0, 3, 4e9)]
+    s = lane_summary(log, span=4.0)
+    assert s["0"]["iterations"] == 2 and s["0"]["busy_fraction"] == pytest.approx(0.25)
+    assert s["0"]["voxel_updates_per_s_while_busy"] == pytest.approx(1.5e9)
+    assert s["1"]["mean_members"] == 3 and s["1"]["mean_iteration_s"] == pytest.approx(2.0)
+    res = [Result(0, SIRT, 0.0, 1.0, 3.0, 10, size=512, lane=0, create_s=0.2),
+           Result(1, WBP, 0.5, 0.5, 0.7, 5, size=512, lane=-1, create_s=0.1),
+           Result(2, SIRT, 1.0, 4.0, 9.0, 40, size=2048, lane=2, create_s=0.5)]
+    out = summarize(res)
+    assert out["per_size"]["512"]["n"] == 2 and out["per_size"]["2048"]["wait_p50_s"] == pytest.approx(3.0)
+    assert out["per_kind"][SIRT]["service_p50_s"] == pytest.approx(3.5)
+    assert out["per_size"]["512"]["create_p50_s"] == pytest.approx(0.15)
+    assert out["voxel_updates_per_s"] == pytest.approx(55 / 9.0)
