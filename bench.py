@@ -299,6 +299,13 @@ def run_engine(args, wl):
     load(series)
     nvox = W * H * D
     updates_per_step = nvox * n * (1 + wl["n_iter"])
+    # kernel shapes for this series from the engine's autotuner (one update, 3 launches per
+    # candidate; the volume is put back), as a caller would run it once per series
+    tune = np.zeros(4)
+    _abi.check(lib.tomo_set_fill(h, _abi.FILL_NAN))
+    _abi.check(lib.tomo_autotune(h, wl["update"], 3, _abi.ptr(tune, C.c_double)))
+    autotune = {"tilts_per_cta": int(tune[0]) or "auto", "bp_rows": int(tune[1]) or "auto",
+                "fp_ms": float(tune[2]), "bp_ms": float(tune[3])}
 
     def step(errs=None):
         # WBP on FILL_AVG projections, then OS-SART on FILL_NAN projections, as the
@@ -506,7 +513,7 @@ def run_engine(args, wl):
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps, "phases_s": phase},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
             "row_streams": row_leg, "compressed_sensing": cs_leg, "config1_full": config1, "batched": batched,
-            "serving": serving, "precision": precision, "tv_denoise": tv,
+            "serving": serving, "precision": precision, "tv_denoise": tv, "autotune": autotune,
             "sirt_error_last_iteration": float(errs[-1, 0]),
         }
         print(json.dumps(line), flush=True)
