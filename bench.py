@@ -49,8 +49,9 @@ def log(*a):
 
 
 def want(args, leg):
-    """Whether the extra leg `leg` runs (not --no-extra, and named by --legs or --legs all)."""
-    if args.no_extra:
+    """Whether the extra leg `leg` runs (not --no-extra, and named by --legs or --legs all).
+    The extra legs characterise one GPU: a multi-rank run (scaling) times the main job only."""
+    if args.no_extra or int(os.environ.get("WORLD_SIZE", "1")) > 1:
         return False
     return args.legs == "all" or leg in args.legs.split(",")
 
