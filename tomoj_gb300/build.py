@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libtomoj_gb300.so")
-SOURCES = ["tomo_abi.cu", "kernels_fp.cu", "fp_kernel_q1.cu", "fp_kernel_q2.cu", "fp_kernel_q4.cu", "fp_kernel_q8.cu", "fp_persist_t256.cu", "fp_persist_t512.cu", "kernels_bp.cu", "kernels_misc.cu", "kernels_vol.cu", "kernels_generic.cu", "geometry.cpp", "noalloc.cu", "batch.cu",
+SOURCES = ["tomo_abi.cu", "kernels_fp.cu", "fp_kernel_q1.cu", "fp_kernel_q2.cu", "fp_kernel_q2w.cu", "fp_kernel_q4.cu", "fp_kernel_q8.cu", "fp_persist_t256.cu", "fp_persist_t512.cu", "kernels_bp.cu", "kernels_misc.cu", "kernels_vol.cu", "kernels_generic.cu", "geometry.cpp", "noalloc.cu", "batch.cu",
            "kernels_wavelet.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
